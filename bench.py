@@ -1,0 +1,317 @@
+#!/usr/bin/env python
+"""Benchmark: rays/s of the plain trace on one GB300 (single parabolic heliostat workload).
+
+Workload (default): 10 x 10 m paraboloid (focal length 100 m) at (0,100,0) aimed at a cylindrical
+receiver r = 2 m, h = 4 m centred (0,0,100); Gaussian sun 2.5 mrad; slope error 1.5 mrad;
+16,777,216 rays, float32, synthetic (the reference ships no benchmark scenes).
+
+One step = one trace of all rays: generation, closest-hit search, shading, and the full rewrite of
+the dense 16M x 5 float4 hit buffer (1.34 GB, larger than L2, so no flush is needed between steps).
+
+  value      rays/s with the scene resident in HBM: K trace launches timed with CUDA events on the
+             launching stream.
+  e2e        rays/s through the public C ABI with host buffers: per step, upload of the element list
+             (csp_set_elements + csp_update: H2D, refit, sun plane) and csp_run_to_host (trace +
+             D2H of every hit record into page-locked memory), wall-clock timed.
+  roofline   HBM: algorithmic bytes = 80 B per ray (the dense hit records) / per-launch time.
+  cpu_baseline  the oracle port of the reference algorithm on all host cores, bounded sample.
+
+--impl reference times the reference algorithm's CPU implementation (the oracle port: the
+reference's own programs cannot run this workload's Gaussian sun and slope error) on all host
+cores, on the same workload and metric.
+
+Multi-GPU: replicas only (each rank traces its own copy of the workload; no exchange), launched by
+torchrun; value = all rays / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "rays/s on 1 GB300 (batched/served vs plain trace) at flux L2<=1%; p50/p99 latency"
+BYTES_PER_RAY = 80  # 5 float4 hit records per ray, fully rewritten by every trace
+# dram__bytes_read.sum + dram__bytes_write.sum of one trace_kernel launch of this workload, from the
+# ncu capture summarised in profiles/trace_kernel_single_parabolic.md (None until captured)
+NCU_TRAFFIC_PER_LAUNCH = None
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=400)
+    p.add_argument("--warmup", type=int, default=10)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--rays", type=int, default=1 << 24)
+    p.add_argument("--e2e-steps", type=int, default=10)
+    p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-accuracy", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "100"], stdout=open(self.path, "w"),
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(seconds: float, rays: int):
+    """Oracle port of the reference algorithm on all host cores over a bounded sample."""
+    from oracle import oracle
+    from optixsoltracedemos_gb300 import scenes
+    oracle.build(with_ref=False)
+    o = oracle.Oracle("f32")
+    sc = scenes.single_parabolic(num_rays=rays)
+    cores = os.cpu_count() or 1
+    chunk = 1 << 20
+    o.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, first_ray=0, count=chunk // 8, nthreads=cores,
+            with_ids=False)
+    done, first, t0 = 0, 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        o.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, first_ray=first, count=chunk, nthreads=cores,
+                with_ids=False)
+        done += chunk
+        first = (first + chunk) % rays
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": "rays/s", "cores": cores, "kind": "port",
+            "sample": f"{done} rays ({done // chunk} chunks of {chunk}) of the single_parabolic workload, "
+                      f"{dt:.1f} s, OpenMP over {cores} threads"}
+
+
+def config(rays):
+    return {"workload": "single_parabolic_heliostat_cylinder_receiver", "rays": rays, "elements": 2,
+            "sun": "gaussian 2.5 mrad", "slope_error_rad": 1.5e-3, "focal_length_m": 100.0,
+            "hit_buffer_bytes": rays * BYTES_PER_RAY,
+            "l2_policy": "hit buffer (1.34 GB) larger than L2; no flush needed between steps",
+            "parallelism": "replicas"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle
+    from optixsoltracedemos_gb300 import scenes
+    oracle.build(with_ref=False)
+    o = oracle.Oracle("f32")
+    sc = scenes.single_parabolic(num_rays=args.rays)
+    cores = os.cpu_count() or 1
+    sample = 1 << 20
+    for w in range(args.warmup):
+        o.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, first_ray=w * sample % args.rays, count=sample,
+                nthreads=cores, with_ids=False)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        o.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, first_ray=(k * sample) % args.rays,
+                count=sample, nthreads=cores, with_ids=False)
+    dt = time.perf_counter() - t0
+    v = args.steps * sample / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "rays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config(args.rays),
+            "cpu_baseline": {"value": v, "unit": "rays/s", "cores": cores, "kind": "port",
+                             "sample": f"each step traces {sample} of the {args.rays} rays (oracle port of the "
+                                       f"reference algorithm, OpenMP over {cores} threads)"},
+            "e2e": {"value": v, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        pg = dist
+
+    from optixsoltracedemos_gb300 import build as nbuild
+    if rank == 0:
+        nbuild.build()
+    if pg:
+        pg.barrier()
+    from optixsoltracedemos_gb300 import native, scenes
+    from optixsoltracedemos_gb300.flux import flux_map_from_hits, flux_l2
+
+    sc = scenes.single_parabolic(num_rays=args.rays)
+    N = args.rays
+    tr = native.tracer_for(sc, device=local, record_ids=False)
+    stream = torch.cuda.Stream(device=local)
+    sp = stream.cuda_stream
+
+    for w in range(args.warmup):
+        tr.set_seed(w)
+        tr.trace_async(sp)
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+
+    clk = ClockSampler(local)
+    clk.start()
+    time.sleep(0.3)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for k in range(args.steps):
+        tr.set_seed(1000 + k)
+        starts[k].record(stream)
+        tr.trace_async(sp)
+        ends[k].record(stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    total_s = e0.elapsed_time(e1) * 1e-3
+    launch_s = statistics.mean(s.elapsed_time(e) for s, e in zip(starts, ends)) * 1e-3
+    if pg:
+        t = torch.tensor([total_s], device=f"cuda:{local}", dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = world * N * args.steps / total_s
+
+    # end to end through the C ABI with host buffers
+    host = torch.empty(N * 5 * 4, dtype=torch.float32, pin_memory=True)
+    elements = sc.elements.copy()
+    for _ in range(2):
+        tr.set_elements(elements)
+        tr.update()
+        tr.run_to_host_ptr(host.data_ptr())
+    if pg:
+        pg.barrier()
+    t0 = time.perf_counter()
+    for k in range(args.e2e_steps):
+        tr.set_seed(5000 + k)
+        tr.set_elements(elements)
+        tr.update()
+        tr.run_to_host_ptr(host.data_ptr())
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    if pg:
+        t = torch.tensor([e2e_s], device=f"cuda:{local}", dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    peak, peak_kind = peaks()
+    achieved = BYTES_PER_RAY * N / launch_s / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": config(N),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": NCU_TRAFFIC_PER_LAUNCH, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": BYTES_PER_RAY * N, "launch_ms": launch_s * 1e3},
+        "e2e": {"value": world * N / e2e_s, "unit": "rays/s",
+                "h2d_bytes_per_step": int(elements.nbytes + 3 * 8),
+                "d2h_bytes_per_step": int(N * BYTES_PER_RAY)},
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_accuracy:
+        try:
+            from oracle import oracle
+            oracle.build(with_ref=False)
+            tr.set_seed(0)
+            tr.run()
+            hits = host.numpy().reshape(N, 5, 4)
+            tr.run_to_host(hits.reshape(-1))
+            o64 = oracle.Oracle("f64")
+            oh, _ = o64.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, count=N, with_ids=False)
+            line["flux_l2_vs_fp64"] = flux_l2(flux_map_from_hits(hits, sc.elements[-1], N),
+                                              flux_map_from_hits(oh, sc.elements[-1], N))
+            del oh
+        except Exception as exc:  # accuracy is reported, not required for the timing line
+            line["flux_l2_vs_fp64"] = f"unavailable: {exc}"
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.cpu_seconds, N)
+    tr.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

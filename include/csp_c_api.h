@@ -1,0 +1,139 @@
+/*
+ * csp_c_api.h -- C ABI of the GB300 concentrated-solar ray tracer (libcsp_gb300.so).
+ *
+ * Plain C types only (pointers, sizes, integers, doubles); no CUDA or PyTorch types cross it.  Every
+ * call returns a csp_status (0 = OK); on failure csp_last_error() returns a thread-local message.
+ * The C++ drop-in classes (SolTraceSystem, Element, ...) sit on top of this ABI and turn a non-zero
+ * status into std::runtime_error, as the reference's CUDA_CHECK/OPTIX_CHECK do
+ * (lib/util_check.hpp:54-63,93-104 of the reference).
+ *
+ * Reference interface each entry point replaces (paths inside uwsbel/optixSoltraceDemos):
+ *   csp_create / csp_destroy      SolTraceSystem::SolTraceSystem(int)   lib/soltrace_system.cpp:49-70
+ *                                 SolTraceSystem::clean_up()            lib/soltrace_system.cpp:267-297
+ *   csp_set_num_rays              SolTraceSystem::set_sun_points(int)   lib/soltrace_system.h:49
+ *   csp_add_element /
+ *   csp_set_elements              SolTraceSystem::add_element(...)      lib/soltrace_system.cpp:427-433
+ *                                 (+ Element setters, lib/element.h:41-102)
+ *   csp_set_sun_vector            SolTraceSystem::set_sun_vector(...)   lib/soltrace_system.cpp:443-447
+ *   csp_set_sun_shape             SolTraceSystem::set_sun_angle(double) lib/soltrace_system.h:57
+ *   csp_initialize                SolTraceSystem::initialize()          lib/soltrace_system.cpp:76-143
+ *   csp_run                       SolTraceSystem::run()                 lib/soltrace_system.cpp:145-170
+ *   csp_update                    SolTraceSystem::update()              lib/soltrace_system.cpp:172-184
+ *   csp_read_stinput              SolTraceSystem::read_st_input(...)    lib/soltrace_system.cpp:186-206
+ *   csp_write_output              SolTraceSystem::write_output(...)     lib/soltrace_system.cpp:208-264
+ *   csp_get_timing                get_time_trace / get_time_setup       lib/soltrace_system.cpp:435-441
+ *   csp_get_sun_plane             print_launch_params                   lib/soltrace_system.cpp:24-47
+ *   csp_copy_hits                 the hit_point_buffer D2H copy         lib/soltrace_system.cpp:209-211
+ *   csp_flux_map                  FluxMapCalculator.calculate_flux_map  scripts/post_processing/
+ *                                                                        flux_map_calculator.py:135-179
+ * Additions with no single reference counterpart: csp_trace_async (enqueue on a caller stream),
+ * csp_get_device_buffers (zero-copy consumers), csp_set_seed, csp_set_record_ids.
+ */
+#ifndef CSP_C_API_H
+#define CSP_C_API_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CSP_API __attribute__((visibility("default")))
+
+/* Slots per ray in the hit buffer: MAX_TRACE_DEPTH of the reference (cuda/Soltrace.h:11). */
+#define CSP_MAX_TRACE_DEPTH 5
+#define CSP_ABI_VERSION 1
+/* element id recorded for the sun-plane slot and for unused slots */
+#define CSP_NO_ELEMENT 0xFFFFFFFFu
+
+typedef struct csp_system* csp_handle;
+
+typedef enum csp_status {
+    CSP_OK = 0,
+    CSP_ERR_INVALID_ARGUMENT = -1,
+    CSP_ERR_CUDA = -2,
+    CSP_ERR_OUT_OF_MEMORY = -3,
+    CSP_ERR_BAD_SCENE = -4,
+    CSP_ERR_TIMEOUT = -5,
+    CSP_ERR_STATE = -6,
+    CSP_ERR_IO = -7,
+    CSP_ERR_PARSE = -8
+} csp_status;
+
+/* SurfaceType / ApertureType values of lib/soltrace_type.h:4-15 */
+enum { CSP_SURFACE_FLAT = 0, CSP_SURFACE_PARABOLIC = 1, CSP_SURFACE_CYLINDER = 3 };
+enum { CSP_APERTURE_RECTANGLE = 0, CSP_APERTURE_CIRCLE = 1 };
+enum { CSP_SUN_PILLBOX = 0, CSP_SUN_GAUSSIAN = 1 };
+
+/* One optical element, as the reference's Element holds it (lib/element.h:41-102): origin, aim
+ * point, z rotation in degrees, rectangular aperture (for a cylinder: width = 2 * radius, height =
+ * full height, axis along the element's local y, lib/element.cpp:146-160), parabolic curvatures.
+ * reflectivity / slope_error / specularity_error (radians, Gaussian sigma) are optical properties the
+ * reference parses but never applies; 1 / 0 / 0 reproduces the reference's trace exactly.
+ * The last element of a scene is the receiver (lib/geometry_manager.cpp:78-90). */
+typedef struct csp_element {
+    double origin[3];
+    double aim_point[3];
+    double zrot_deg;
+    double width;
+    double height;
+    double curv_x;
+    double curv_y;
+    double reflectivity;
+    double slope_error;
+    double specularity_error;
+    int32_t surface;
+    int32_t aperture;
+} csp_element;
+
+CSP_API const char* csp_last_error(void);
+CSP_API int csp_abi_version(void);
+
+/* Create a tracer bound to CUDA device `device`.  num_rays = number of sun points (rays). */
+CSP_API int csp_create(csp_handle* out, int device, uint64_t num_rays);
+/* Free every device buffer and the handle (clean_up + destructor). */
+CSP_API int csp_destroy(csp_handle h);
+
+CSP_API int csp_set_num_rays(csp_handle h, uint64_t num_rays);
+CSP_API int csp_add_element(csp_handle h, const csp_element* element);
+CSP_API int csp_set_elements(csp_handle h, const csp_element* elements, uint32_t count);
+CSP_API int csp_get_num_elements(csp_handle h, uint32_t* count);
+CSP_API int csp_get_elements(csp_handle h, csp_element* out, uint32_t capacity);
+CSP_API int csp_set_sun_vector(csp_handle h, double x, double y, double z);
+/* shape CSP_SUN_PILLBOX: param = half angle (rad), the reference's max_sun_angle;
+ * shape CSP_SUN_GAUSSIAN: param = sigma (rad) per tangent-plane axis (extension). */
+CSP_API int csp_set_sun_shape(csp_handle h, int shape, double param_rad);
+/* Philox key of the random draws (seed) and the instance word of their counter. */
+CSP_API int csp_set_seed(csp_handle h, uint64_t seed, uint32_t instance);
+/* Also record the element index of every slot (uint32 per slot, CSP_NO_ELEMENT when empty). */
+CSP_API int csp_set_record_ids(csp_handle h, int enable);
+
+/* Build device geometry, acceleration structure and sun plane; allocate the hit buffer. */
+CSP_API int csp_initialize(csp_handle h);
+/* Trace num_rays rays and wait for them (run()).  Fully rewrites the num_rays x 5 hit buffer. */
+CSP_API int csp_run(csp_handle h);
+/* Enqueue the trace on `stream` (a cudaStream_t, NULL = the handle's own stream); no host sync. */
+CSP_API int csp_trace_async(csp_handle h, void* stream);
+/* Re-read the element poses given since initialize (same count), refit the acceleration structure
+ * in place and recompute the sun plane (update()). */
+CSP_API int csp_update(csp_handle h);
+
+/* Copy hit records of rays [first_ray, first_ray + count) to host memory: dst holds count * 5 * 4
+ * floats {stage, x, y, z}; ids (may be NULL) count * 5 uint32. */
+CSP_API int csp_copy_hits(csp_handle h, float* dst, uint32_t* ids, uint64_t first_ray, uint64_t count);
+/* Trace and copy every hit record to host memory in one call (run() + the D2H copy of
+ * write_output), pipelining the copy of finished chunks behind the trace of later ones.  dst (and
+ * ids when not NULL) should be page-locked for full speed. */
+CSP_API int csp_run_to_host(csp_handle h, float* dst, uint32_t* ids);
+/* Device pointers of the hit buffer ([num_rays*5] float4) and id buffer (NULL unless recorded). */
+CSP_API int csp_get_device_buffers(csp_handle h, void** hits, void** ids);
+
+CSP_API int csp_get_timing(csp_handle h, double* setup_s, double* trace_s);
+/* out[16]: sun vector (3), v0 (3), v1 (3), v2 (3), v3 (3), plane distance (1). */
+CSP_API int csp_get_sun_plane(csp_handle h, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CSP_C_API_H */

@@ -1,0 +1,435 @@
+// csp_c_api.cpp -- the C ABI (include/csp_c_api.h): handle lifecycle, device buffers, launches.
+#include "csp_c_api.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "csp_kernels.cuh"
+#include "csp_scene.h"
+#include "csp_system.h"
+
+namespace {
+
+thread_local std::string t_last_error;
+
+int fail(int status, const std::string& msg) {
+    t_last_error = msg;
+    return status;
+}
+
+}  // namespace
+
+namespace csp {
+
+int set_error(int status, const std::string& msg) { return fail(status, msg); }
+
+int cuda_status(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return CSP_OK;
+    const int st = (e == cudaErrorMemoryAllocation) ? CSP_ERR_OUT_OF_MEMORY : CSP_ERR_CUDA;
+    cudaGetLastError();  // clear the sticky-free error state of the runtime API
+    return fail(st, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+static int upload(T*& dptr, size_t& cap, const std::vector<T>& host, cudaStream_t st, const char* what) {
+    const size_t n = host.size();
+    if (n > cap) {
+        if (dptr) cudaFree(dptr);
+        dptr = nullptr;
+        cap = 0;
+        int rc = cuda_status(cudaMalloc((void**)&dptr, std::max<size_t>(n, 1) * sizeof(T)), what);
+        if (rc) return rc;
+        cap = n;
+    }
+    if (n) return cuda_status(cudaMemcpyAsync(dptr, host.data(), n * sizeof(T), cudaMemcpyHostToDevice, st), what);
+    return CSP_OK;
+}
+
+System::~System() { release(); }
+
+void System::release() {
+    if (device >= 0) cudaSetDevice(device);
+    cudaFree(d_nodes);
+    cudaFree(d_prims);
+    cudaFree(d_optics);
+    cudaFree(d_aabbs);
+    cudaFree(d_sun);
+    cudaFree(d_hits);
+    cudaFree(d_ids);
+    d_nodes = nullptr;
+    d_prims = nullptr;
+    d_optics = nullptr;
+    d_aabbs = nullptr;
+    d_sun = nullptr;
+    d_hits = nullptr;
+    d_ids = nullptr;
+    cap_nodes = cap_prims = cap_optics = cap_aabbs = 0;
+    cap_rays = 0;
+    ids_allocated = false;
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (copy_stream) cudaStreamDestroy(copy_stream);
+    if (stream) cudaStreamDestroy(stream);
+    ev0 = ev1 = nullptr;
+    stream = copy_stream = nullptr;
+    initialized = false;
+}
+
+int System::ensure_streams() {
+    if (stream) return CSP_OK;
+    int rc = cuda_status(cudaSetDevice(device), "cudaSetDevice");
+    if (rc) return rc;
+    if ((rc = cuda_status(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate"))) return rc;
+    if ((rc = cuda_status(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "cudaStreamCreate")))
+        return rc;
+    if ((rc = cuda_status(cudaEventCreate(&ev0), "cudaEventCreate"))) return rc;
+    return cuda_status(cudaEventCreate(&ev1), "cudaEventCreate");
+}
+
+int System::upload_scene() {
+    int rc;
+    if ((rc = upload(d_prims, cap_prims, scene.prims, stream, "upload prims"))) return rc;
+    if ((rc = upload(d_optics, cap_optics, scene.optics, stream, "upload optics"))) return rc;
+    if ((rc = upload(d_aabbs, cap_aabbs, scene.aabbs, stream, "upload aabbs"))) return rc;
+    if ((rc = upload(d_nodes, cap_nodes, scene.nodes, stream, "upload bvh"))) return rc;
+    if (!d_sun) {
+        if ((rc = cuda_status(cudaMalloc((void**)&d_sun, sizeof(SunFrame)), "cudaMalloc sun"))) return rc;
+    }
+    return CSP_OK;
+}
+
+float System::pad_angle() const {
+    // the reference pads the sun plane by the pillbox half angle (lib/geometry_manager.cpp:129);
+    // the Gaussian sun pads by 5 sigma
+    return (float)(sun_shape == CSP_SUN_GAUSSIAN ? 5.0 * sun_param : sun_param);
+}
+
+int System::prepare_sun() {
+    float s[3];
+    sun_vector_f(sun_dir, s);
+    scene.sun[0] = s[0];
+    scene.sun[1] = s[1];
+    scene.sun[2] = s[2];
+    const float tan_pad = tanf(pad_angle());
+    return cuda_status(launch_prepare_sun(d_aabbs, (int)scene.prims.size(), s[0], s[1], s[2], tan_pad, sun_shape,
+                                          (float)sun_param, d_sun, stream),
+                       "prepare_sun_kernel");
+}
+
+int System::ensure_hit_buffers() {
+    if (num_rays > cap_rays || (record_ids && !ids_allocated)) {
+        cudaFree(d_hits);
+        cudaFree(d_ids);
+        d_hits = nullptr;
+        d_ids = nullptr;
+        cap_rays = 0;
+        ids_allocated = false;
+        const size_t n = std::max<uint64_t>(num_rays, 1);
+        int rc = cuda_status(cudaMalloc((void**)&d_hits, n * kMaxDepth * sizeof(float4)), "cudaMalloc hit buffer");
+        if (rc) return rc;
+        if (record_ids) {
+            rc = cuda_status(cudaMalloc((void**)&d_ids, n * kMaxDepth * sizeof(uint32_t)), "cudaMalloc id buffer");
+            if (rc) return rc;
+            ids_allocated = true;
+        }
+        cap_rays = num_rays;
+    }
+    return CSP_OK;
+}
+
+int System::initialize() {
+    const auto t0 = std::chrono::steady_clock::now();
+    int rc = ensure_streams();
+    if (rc) return rc;
+    std::string err;
+    if ((rc = build_elements(elements.data(), (uint32_t)elements.size(), scene, err))) return fail(rc, err);
+    build_bvh(scene);
+    if ((rc = upload_scene())) return rc;
+    if ((rc = prepare_sun())) return rc;
+    if ((rc = ensure_hit_buffers())) return rc;
+    if ((rc = cuda_status(cudaStreamSynchronize(stream), "initialize"))) return rc;
+    initialized = true;
+    time_setup = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return CSP_OK;
+}
+
+int System::update() {
+    if (!initialized) return fail(CSP_ERR_STATE, "update() before initialize()");
+    if (elements.size() != scene.prims.size())
+        return fail(CSP_ERR_STATE, "update() needs the element count of initialize(); call initialize() again");
+    std::string err;
+    int rc = build_elements(elements.data(), (uint32_t)elements.size(), scene, err);
+    if (rc) return fail(rc, err);
+    refit_bvh(scene);
+    if ((rc = upload_scene())) return rc;
+    if ((rc = prepare_sun())) return rc;
+    if ((rc = ensure_hit_buffers())) return rc;
+    return cuda_status(cudaStreamSynchronize(stream), "update");
+}
+
+TraceArgs System::args(uint64_t begin, uint64_t count) const {
+    TraceArgs a;
+    a.nodes = d_nodes;
+    a.prims = d_prims;
+    a.optics = d_optics;
+    a.sun = d_sun;
+    a.hits = d_hits + begin * kMaxDepth;
+    a.ids = (record_ids && d_ids) ? d_ids + begin * kMaxDepth : nullptr;
+    a.ray_begin = begin;
+    a.count = count;
+    a.seed = seed;
+    a.instance = instance;
+    a.pad = 0;
+    return a;
+}
+
+int System::trace_async(cudaStream_t st) {
+    if (!initialized) return fail(CSP_ERR_STATE, "trace before initialize()");
+    int rc = ensure_hit_buffers();
+    if (rc) return rc;
+    return cuda_status(launch_trace(args(0, num_rays), st ? st : stream), "trace_kernel");
+}
+
+int System::run() {
+    if (!initialized) return fail(CSP_ERR_STATE, "run() before initialize()");
+    int rc = ensure_hit_buffers();
+    if (rc) return rc;
+    if ((rc = cuda_status(cudaEventRecord(ev0, stream), "cudaEventRecord"))) return rc;
+    if ((rc = cuda_status(launch_trace(args(0, num_rays), stream), "trace_kernel"))) return rc;
+    if ((rc = cuda_status(cudaEventRecord(ev1, stream), "cudaEventRecord"))) return rc;
+    if ((rc = cuda_status(cudaEventSynchronize(ev1), "trace"))) return rc;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    time_trace = ms * 1e-3;
+    return CSP_OK;
+}
+
+int System::run_to_host(float* dst, uint32_t* ids_dst) {
+    if (!initialized) return fail(CSP_ERR_STATE, "run() before initialize()");
+    int rc = ensure_hit_buffers();
+    if (rc) return rc;
+    const uint64_t chunk = std::max<uint64_t>(1u << 20, (num_rays + 15) / 16);
+    std::vector<cudaEvent_t> done;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (uint64_t b = 0; b < num_rays; b += chunk) {
+        const uint64_t c = std::min(chunk, num_rays - b);
+        if ((rc = cuda_status(launch_trace(args(b, c), stream), "trace_kernel"))) break;
+        cudaEvent_t ev;
+        if ((rc = cuda_status(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate"))) break;
+        done.push_back(ev);
+        if ((rc = cuda_status(cudaEventRecord(ev, stream), "cudaEventRecord"))) break;
+        if ((rc = cuda_status(cudaStreamWaitEvent(copy_stream, ev, 0), "cudaStreamWaitEvent"))) break;
+        rc = cuda_status(cudaMemcpyAsync(dst + b * kMaxDepth * 4, d_hits + b * kMaxDepth, c * kMaxDepth * sizeof(float4),
+                                         cudaMemcpyDeviceToHost, copy_stream),
+                         "D2H hit records");
+        if (rc) break;
+        if (ids_dst && record_ids && d_ids) {
+            rc = cuda_status(cudaMemcpyAsync(ids_dst + b * kMaxDepth, d_ids + b * kMaxDepth,
+                                             c * kMaxDepth * sizeof(uint32_t), cudaMemcpyDeviceToHost, copy_stream),
+                             "D2H ids");
+            if (rc) break;
+        }
+    }
+    const int sync_rc = cuda_status(cudaStreamSynchronize(copy_stream), "D2H sync");
+    const int sync_rc2 = cuda_status(cudaStreamSynchronize(stream), "trace sync");
+    for (cudaEvent_t ev : done) cudaEventDestroy(ev);
+    if (rc) return rc;
+    if (sync_rc) return sync_rc;
+    if (sync_rc2) return sync_rc2;
+    time_trace = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return CSP_OK;
+}
+
+}  // namespace csp
+
+using csp::System;
+
+#define CSP_GUARD(h)                                                              \
+    do {                                                                          \
+        if (!(h)) return fail(CSP_ERR_INVALID_ARGUMENT, "null handle");           \
+    } while (0)
+
+extern "C" {
+
+const char* csp_last_error(void) { return t_last_error.c_str(); }
+int csp_abi_version(void) { return CSP_ABI_VERSION; }
+
+int csp_create(csp_handle* out, int device, uint64_t num_rays) {
+    if (!out) return fail(CSP_ERR_INVALID_ARGUMENT, "null output handle");
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess) return csp::cuda_status(e, "cudaGetDeviceCount");
+    if (device < 0 || device >= count) return fail(CSP_ERR_INVALID_ARGUMENT, "no such CUDA device");
+    System* s = new (std::nothrow) System();
+    if (!s) return fail(CSP_ERR_OUT_OF_MEMORY, "host allocation failed");
+    s->device = device;
+    s->num_rays = num_rays;
+    *out = reinterpret_cast<csp_handle>(s);
+    return CSP_OK;
+}
+
+int csp_destroy(csp_handle h) {
+    CSP_GUARD(h);
+    delete reinterpret_cast<System*>(h);
+    return CSP_OK;
+}
+
+int csp_set_num_rays(csp_handle h, uint64_t num_rays) {
+    CSP_GUARD(h);
+    reinterpret_cast<System*>(h)->num_rays = num_rays;
+    return CSP_OK;
+}
+
+int csp_add_element(csp_handle h, const csp_element* e) {
+    CSP_GUARD(h);
+    if (!e) return fail(CSP_ERR_INVALID_ARGUMENT, "null element");
+    reinterpret_cast<System*>(h)->elements.push_back(*e);
+    return CSP_OK;
+}
+
+int csp_set_elements(csp_handle h, const csp_element* e, uint32_t n) {
+    CSP_GUARD(h);
+    if (!e && n) return fail(CSP_ERR_INVALID_ARGUMENT, "null elements");
+    System* s = reinterpret_cast<System*>(h);
+    s->elements.assign(e, e + n);
+    return CSP_OK;
+}
+
+int csp_get_num_elements(csp_handle h, uint32_t* n) {
+    CSP_GUARD(h);
+    if (!n) return fail(CSP_ERR_INVALID_ARGUMENT, "null output");
+    *n = (uint32_t)reinterpret_cast<System*>(h)->elements.size();
+    return CSP_OK;
+}
+
+int csp_get_elements(csp_handle h, csp_element* out, uint32_t cap) {
+    CSP_GUARD(h);
+    System* s = reinterpret_cast<System*>(h);
+    if (!out || cap < s->elements.size()) return fail(CSP_ERR_INVALID_ARGUMENT, "output too small");
+    std::copy(s->elements.begin(), s->elements.end(), out);
+    return CSP_OK;
+}
+
+int csp_set_sun_vector(csp_handle h, double x, double y, double z) {
+    CSP_GUARD(h);
+    System* s = reinterpret_cast<System*>(h);
+    s->sun_dir[0] = x;
+    s->sun_dir[1] = y;
+    s->sun_dir[2] = z;
+    return CSP_OK;
+}
+
+int csp_set_sun_shape(csp_handle h, int shape, double param) {
+    CSP_GUARD(h);
+    if (shape != CSP_SUN_PILLBOX && shape != CSP_SUN_GAUSSIAN) return fail(CSP_ERR_INVALID_ARGUMENT, "unknown sun shape");
+    if (!(param >= 0.0) || param > 0.5) return fail(CSP_ERR_INVALID_ARGUMENT, "sun shape parameter out of range");
+    System* s = reinterpret_cast<System*>(h);
+    s->sun_shape = shape;
+    s->sun_param = param;
+    return CSP_OK;
+}
+
+int csp_set_seed(csp_handle h, uint64_t seed, uint32_t instance) {
+    CSP_GUARD(h);
+    System* s = reinterpret_cast<System*>(h);
+    s->seed = seed;
+    s->instance = instance;
+    return CSP_OK;
+}
+
+int csp_set_record_ids(csp_handle h, int enable) {
+    CSP_GUARD(h);
+    reinterpret_cast<System*>(h)->record_ids = enable != 0;
+    return CSP_OK;
+}
+
+int csp_initialize(csp_handle h) {
+    CSP_GUARD(h);
+    return reinterpret_cast<System*>(h)->initialize();
+}
+
+int csp_run(csp_handle h) {
+    CSP_GUARD(h);
+    return reinterpret_cast<System*>(h)->run();
+}
+
+int csp_trace_async(csp_handle h, void* stream) {
+    CSP_GUARD(h);
+    return reinterpret_cast<System*>(h)->trace_async(reinterpret_cast<cudaStream_t>(stream));
+}
+
+int csp_update(csp_handle h) {
+    CSP_GUARD(h);
+    return reinterpret_cast<System*>(h)->update();
+}
+
+int csp_copy_hits(csp_handle h, float* dst, uint32_t* ids, uint64_t first, uint64_t count) {
+    CSP_GUARD(h);
+    System* s = reinterpret_cast<System*>(h);
+    if (!s->initialized || !s->d_hits) return fail(CSP_ERR_STATE, "no hit buffer (initialize first)");
+    if (first > s->num_rays || count > s->num_rays - first) return fail(CSP_ERR_INVALID_ARGUMENT, "ray range out of bounds");
+    if (!dst && count) return fail(CSP_ERR_INVALID_ARGUMENT, "null destination");
+    int rc = csp::cuda_status(cudaStreamSynchronize(s->stream), "sync");
+    if (rc) return rc;
+    if (count) {
+        rc = csp::cuda_status(cudaMemcpy(dst, s->d_hits + first * csp::kMaxDepth, count * csp::kMaxDepth * sizeof(float4),
+                                         cudaMemcpyDeviceToHost),
+                              "D2H hit records");
+        if (rc) return rc;
+    }
+    if (ids) {
+        if (!s->record_ids || !s->d_ids) return fail(CSP_ERR_STATE, "element ids are not being recorded");
+        if (count)
+            return csp::cuda_status(cudaMemcpy(ids, s->d_ids + first * csp::kMaxDepth,
+                                               count * csp::kMaxDepth * sizeof(uint32_t), cudaMemcpyDeviceToHost),
+                                    "D2H ids");
+    }
+    return CSP_OK;
+}
+
+int csp_run_to_host(csp_handle h, float* dst, uint32_t* ids) {
+    CSP_GUARD(h);
+    if (!dst) return fail(CSP_ERR_INVALID_ARGUMENT, "null destination");
+    return reinterpret_cast<System*>(h)->run_to_host(dst, ids);
+}
+
+int csp_get_device_buffers(csp_handle h, void** hits, void** ids) {
+    CSP_GUARD(h);
+    System* s = reinterpret_cast<System*>(h);
+    if (hits) *hits = s->d_hits;
+    if (ids) *ids = s->record_ids ? s->d_ids : nullptr;
+    return CSP_OK;
+}
+
+int csp_get_timing(csp_handle h, double* setup_s, double* trace_s) {
+    CSP_GUARD(h);
+    System* s = reinterpret_cast<System*>(h);
+    if (setup_s) *setup_s = s->time_setup;
+    if (trace_s) *trace_s = s->time_trace;
+    return CSP_OK;
+}
+
+int csp_get_sun_plane(csp_handle h, float* out) {
+    CSP_GUARD(h);
+    System* s = reinterpret_cast<System*>(h);
+    if (!out) return fail(CSP_ERR_INVALID_ARGUMENT, "null output");
+    if (!s->initialized) return fail(CSP_ERR_STATE, "initialize first");
+    csp::SunFrame f;
+    int rc = csp::cuda_status(cudaMemcpy(&f, s->d_sun, sizeof(f), cudaMemcpyDeviceToHost), "D2H sun frame");
+    if (rc) return rc;
+    const float v[16] = {f.s_d.x, f.s_d.y, f.s_d.z, f.v0.x, f.v0.y, f.v0.z, f.v1.x, f.v1.y,
+                         f.v1.z,  f.v2.x,  f.v2.y,  f.v2.z, f.v3.x, f.v3.y, f.v3.z, f.s_d.w};
+    std::memcpy(out, v, sizeof(v));
+    return CSP_OK;
+}
+
+}  // extern "C"

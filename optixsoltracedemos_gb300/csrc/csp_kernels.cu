@@ -1,0 +1,474 @@
+// csp_kernels.cu -- sm_103a kernels of the trace path.
+//
+// Built with -fmad=false (plus IEEE division and square root): every expression below rounds
+// exactly as written, which is what makes the hit records bit-identical to the host restatement of
+// the reference.  Fused multiply-adds appear only as explicit fmaf() calls in csp_math.cuh.
+//
+// Kernel map (reference counterpart in parentheses, paths inside the reference project):
+//   prepare_sun_kernel  sun-plane distance, u/v bounds, parallelogram, cone frame
+//                       (lib/sun_utils.cu:53-179, lib/geometry_manager.cpp:97-148, cuda/sun.cu:76-79)
+//   trace_kernel        ray generation (cuda/sun.cu:16-38,72-134), closest-hit search over the
+//                       elements whose AABB the ray overlaps (OptiX traversal + the intersection
+//                       programs of cuda/intersection.cu:47-85,177-296,318-448), shading
+//                       (cuda/materials.cu:26-231) and the hit_point_buffer write.
+#include <cfloat>
+
+#include "csp_kernels.cuh"
+#include "csp_math.cuh"
+
+namespace csp {
+namespace {
+
+constexpr int kTraceBlock = 256;
+constexpr int kPrepBlock = 512;
+constexpr float kTwoPi = 2.0f * 3.14159265358979323846f;  // 2.0f * M_PIf, cuda/sun.cu:85
+
+// ------------------------------------------------------------------------------ sun plane -----
+__device__ __forceinline__ float3 corner(const Aabb& b, int k) {
+    return make_float3((k & 1) ? b.hi.x : b.lo.x, (k & 2) ? b.hi.y : b.lo.y, (k & 4) ? b.hi.z : b.lo.z);
+}
+
+template <bool kMax>
+__device__ float block_reduce(float v, float* scratch) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const float w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = kMax ? fmaxf(v, w) : fminf(v, w);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) scratch[warp] = v;
+    __syncthreads();
+    v = scratch[0];
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) v = kMax ? fmaxf(v, scratch[i]) : fminf(v, scratch[i]);
+    return v;
+}
+
+__global__ void __launch_bounds__(kPrepBlock) prepare_sun_kernel(const Aabb* __restrict__ aabbs, int n, float3 s,
+                                                                   float tan_pad, int shape, float param,
+                                                                   SunFrame* __restrict__ out) {
+    __shared__ float scratch[kPrepBlock / 32];
+    // plane distance: max over every AABB corner of |c . s| (and 0), lib/sun_utils.cu:53-104
+    float md = 0.0f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const Aabb b = aabbs[i];
+        for (int k = 0; k < 8; ++k) md = fmaxf(md, fabsf(dot(corner(b, k), s)));
+    }
+    const float d = block_reduce<true>(md, scratch);
+
+    const float3 axis = (fabsf(s.x) < 0.9f) ? f3(1.0f, 0.0f, 0.0f) : f3(0.0f, 1.0f, 0.0f);
+    const float3 su = normalize(cross(axis, s));
+    const float3 sv = normalize(cross(s, su));
+    const float3 pc = scale(d, s);
+    // u/v bounds padded by |c . s| tan(angle), lib/sun_utils.cu:106-179
+    float umin = FLT_MAX, umax = -FLT_MAX, vmin = FLT_MAX, vmax = -FLT_MAX;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const Aabb b = aabbs[i];
+        for (int k = 0; k < 8; ++k) {
+            const float3 pt = corner(b, k);
+            const float buf = fabsf(dot(pt, s)) * tan_pad;
+            const float3 proj = sub(pt, scale(dot(sub(pt, pc), s), s));
+            const float u = dot(proj, su), v = dot(proj, sv);
+            umin = fminf(umin, u - buf);
+            umax = fmaxf(umax, u + buf);
+            vmin = fminf(vmin, v - buf);
+            vmax = fmaxf(vmax, v + buf);
+        }
+    }
+    umin = block_reduce<false>(umin, scratch);
+    umax = block_reduce<true>(umax, scratch);
+    vmin = block_reduce<false>(vmin, scratch);
+    vmax = block_reduce<true>(vmax, scratch);
+    if (threadIdx.x != 0) return;
+    const float3 ds = scale(d, s);
+    const float3 v0 = add(add(scale(umin, su), scale(vmin, sv)), ds);
+    const float3 v1 = add(add(scale(umax, su), scale(vmin, sv)), ds);
+    const float3 v2 = add(add(scale(umax, su), scale(vmax, sv)), ds);
+    const float3 v3 = add(add(scale(umin, su), scale(vmax, sv)), ds);
+    // cone frame, cuda/sun.cu:76-79 with dir = -normalize(sun_vector) (cuda/sun.cu:106)
+    const float3 w = normalize(neg(normalize(s)));
+    const float3 cu = normalize(cross(fabsf(w.x) > 0.99f ? f3(0.0f, 1.0f, 0.0f) : f3(1.0f, 0.0f, 0.0f), w));
+    const float3 cv = cross(w, cu);
+    SunFrame f;
+    f.s_d = make_float4(s.x, s.y, s.z, d);
+    f.v0 = make_float4(v0.x, v0.y, v0.z, 0.f);
+    const float3 e1 = sub(v1, v0), e2 = sub(v3, v0);
+    f.e1 = make_float4(e1.x, e1.y, e1.z, 0.f);
+    f.e2 = make_float4(e2.x, e2.y, e2.z, 0.f);
+    f.v1 = make_float4(v1.x, v1.y, v1.z, 0.f);
+    f.v2 = make_float4(v2.x, v2.y, v2.z, 0.f);
+    f.v3 = make_float4(v3.x, v3.y, v3.z, 0.f);
+    f.w = make_float4(w.x, w.y, w.z, 0.f);
+    f.u = make_float4(cu.x, cu.y, cu.z, 0.f);
+    f.v = make_float4(cv.x, cv.y, cv.z, 0.f);
+    if (shape == 1) {
+        f.cos_theta = 1.0f;
+        f.sigma = param;
+    } else {
+        float sn, cs;
+        det_sincos(param, sn, cs);  // cosf(half_angle), cuda/sun.cu:82
+        f.cos_theta = cs;
+        f.sigma = 0.0f;
+    }
+    f.tan_pad = tan_pad;
+    f.pad = 0.f;
+    f.shape = shape;
+    f.n_prims = n;
+    f.pad1 = f.pad2 = 0;
+    *out = f;
+}
+
+// ------------------------------------------------------------------------------ sampling ------
+// Halton radical inverse, cuda/sun.cu:16-24: f /= b; r += f * (i mod b); i /= b, in float.
+__device__ __forceinline__ float halton2(uint64_t i) {
+    if (i < (1ull << 24)) {
+        // every partial sum is a dyadic fraction of at most 24 bits, so the float loop is exact and
+        // equals the bit-reversed index scaled by 2^-32
+        return (float)__brev((uint32_t)i) * 0x1p-32f;
+    }
+    float f = 1.0f, r = 0.0f;
+    while (i > 0) {
+        f = f * 0.5f;  // f / 2 is exact
+        r = r + f * (float)(uint32_t)(i & 1u);
+        i >>= 1;
+    }
+    return r;
+}
+
+__device__ __forceinline__ float halton3(uint64_t i) {
+    float r = 0.0f;
+    int k = 0;
+    while (i >= (1ull << 32)) {
+        const uint64_t q = i / 3u;
+        r = r + c_halton3_f[k++] * (float)(uint32_t)(i - 3u * q);
+        i = q;
+    }
+    uint32_t j = (uint32_t)i;
+    while (j > 0) {
+        const uint32_t q = j / 3u;
+        r = r + c_halton3_f[k++] * (float)(j - 3u * q);
+        j = q;
+    }
+    return r;
+}
+
+__device__ __forceinline__ float3 perturb(float3 n, float sigma, float g1, float g2) {
+    const float3 t1 = normalize(cross(fabsf(n.x) > 0.9f ? f3(0.0f, 1.0f, 0.0f) : f3(1.0f, 0.0f, 0.0f), n));
+    const float3 t2 = cross(n, t1);
+    return normalize(add(add(n, scale(sigma * g1, t1)), scale(sigma * g2, t2)));
+}
+
+// ------------------------------------------------------------------------------ intersection --
+// Rectangle_Flat, cuda/intersection.cu:47-85.
+__device__ __forceinline__ bool hit_flat(const Prim& p, float3 o, float3 d, float tmin, float& tout) {
+    const float3 n = xyz(p.a);
+    const float dt = dot(d, n);
+    const float t = (p.a.w - dot(n, o)) / dt;
+    if (!(t > tmin && t < kTmax)) return false;
+    const float3 v = sub(add(o, scale(t, d)), xyz(p.b));
+    const float x = dot(xyz(p.c), v), y = dot(xyz(p.d), v);
+    const float hw = p.b.w, hh = p.c.w;
+    if (x >= -hw && x <= hw && y >= -hh && y <= hh) {
+        tout = t;
+        return true;
+    }
+    return false;
+}
+
+
+// Rectangle_Parabolic, cuda/intersection.cu:318-419.  The reference's bounds test
+// a = x_hit / (L/2.) evaluated in double then rounded to float, |a| <= 1, is decided here as
+// |x_hit| <= L/2 in float: for floats x, h > 0, fl32(fl64(x/h)) > 1 exactly when x > h (if x > h
+// then x >= succ(h), so x/h >= 1 + 2^-24 + 2^-48 and both roundings stay above 1; if x <= h the
+// quotient is <= 1), and symmetrically for -1; NaN passes both forms.
+__device__ __forceinline__ bool hit_parab(const Prim& p, float3 o, float3 d, float tmin, float& tout) {
+    const float3 e1 = xyz(p.a), e2 = xyz(p.b), n = xyz(p.c), c = xyz(p.d);
+    const float cx = p.c.w, cy = p.d.w;
+    const float3 dd = sub(o, c);
+    const float ox = dot(dd, e1), oy = dot(dd, e2), oz = dot(dd, n);
+    const float dx = dot(d, e1), dy = dot(d, e2), dz = dot(d, n);
+    const float A = (cx * 0.5f) * (dx * dx) + (cy * 0.5f) * (dy * dy);
+    const float B = cx * (ox * dx) + cy * (oy * dy) - dz;
+    const float C = (cx * 0.5f) * (ox * ox) + (cy * 0.5f) * (oy * oy) - oz;
+    float t = 0.0f;
+    bool valid = false;
+    if (fabsf(A) < 1e-12f) {
+        t = -C / B;
+        valid = (t > 0.0f);
+    } else {
+        const float disc = B * B - 4.0f * A * C;
+        if (disc >= 0.0f) {
+            const float sq = sqrtf(disc);
+            const float t1 = (-B - sq) / (2.0f * A);
+            const float t2 = (-B + sq) / (2.0f * A);
+            if (t1 > 0.0f && t1 < t2) {
+                t = t1;
+                valid = true;
+            } else if (t2 > 0.0f) {
+                t = t2;
+                valid = true;
+            }
+        }
+    }
+    if (!valid || t < tmin || t > kTmax) return false;
+    const float xh = ox + t * dx, yh = oy + t * dy;
+    const float h1 = p.a.w, h2 = p.b.w;
+    if (xh > h1 || xh < -h1 || yh > h2 || yh < -h2) return false;
+    tout = t;
+    return true;
+}
+
+// World normal the parabolic intersection program reports for a hit at t (cuda/intersection.cu:
+// 354-361 local coordinates again, then :430-436).
+__device__ __forceinline__ float3 parab_normal(const Prim& p, float3 o, float3 d, float t) {
+    const float3 e1 = xyz(p.a), e2 = xyz(p.b), n = xyz(p.c);
+    const float3 dd = sub(o, xyz(p.d));
+    const float ox = dot(dd, e1), oy = dot(dd, e2);
+    const float dx = dot(d, e1), dy = dot(d, e2);
+    const float xh = ox + t * dx, yh = oy + t * dy;
+    const float3 nl = normalize(f3(-p.c.w * xh, -p.d.w * yh, 1.0f));
+    return normalize(add(add(scale(nl.x, e1), scale(nl.y, e2)), scale(nl.z, n)));
+}
+
+// Cylinder_Y with caps, cuda/intersection.cu:177-296.
+__device__ __forceinline__ bool hit_cyl(const Prim& p, float3 o, float3 draw, float tmin, float& tout) {
+    const float3 d = normalize(draw);
+    const float3 lo = sub(o, xyz(p.a));
+    const float3 lx = xyz(p.b), ly = xyz(p.c), lz = xyz(p.d);
+    const float Ox = dot(lo, lx), Oy = dot(lo, ly), Oz = dot(lo, lz);
+    const float Dx = dot(d, lx), Dy = dot(d, ly), Dz = dot(d, lz);
+    const float half = p.b.w, r2 = p.c.w;
+    const float A = Dx * Dx + Dz * Dz;
+    const float B = 2.0f * (Ox * Dx + Oz * Dz);
+    const float C = Ox * Ox + Oz * Oz - r2;
+    const float det = B * B - 4.0f * A * C;
+    const float inval = kTmax + 1.0f;
+    float tc = inval;
+    if (det >= 0.0f) {
+        const float sq = sqrtf(det);
+        const float t1 = (-B - sq) / (2.0f * A);
+        const float t2 = (-B + sq) / (2.0f * A);
+        if (t1 > tmin && t1 < kTmax && fabsf(Oy + t1 * Dy) <= half) tc = t1;
+        else if (t2 > tmin && t2 < kTmax && fabsf(Oy + t2 * Dy) <= half) tc = t2;
+    }
+    float tcap = inval;
+    if (fabsf(Dy) > 1e-6f) {
+        const float tb = (-half - Oy) / Dy;
+        const float bx = Ox + tb * Dx, bz = Oz + tb * Dz;
+        if (tb > tmin && tb < kTmax && bx * bx + bz * bz <= r2) tcap = tb;
+        const float tt = (half - Oy) / Dy;
+        const float tx = Ox + tt * Dx, tz = Oz + tt * Dz;
+        if (tt > tmin && tt < kTmax && tx * tx + tz * tz <= r2) tcap = fminf(tcap, tt);
+    }
+    const float t = fminf(tc, tcap);
+    if (t >= kTmax || t <= tmin) return false;
+    tout = t;
+    return true;
+}
+
+__device__ __forceinline__ bool hit_prim(uint32_t type, const Prim& p, float3 o, float3 d, float tmin, float& t) {
+    if (type == kParabolicMirror) return hit_parab(p, o, d, tmin, t);
+    if (type == kCylReceiver) return hit_cyl(p, o, d, tmin, t);
+    return hit_flat(p, o, d, tmin, t);
+}
+
+__device__ __forceinline__ Prim load_prim(const Prim* prims, uint32_t i) {
+    const float4* q = reinterpret_cast<const float4*>(prims + i);
+    Prim p;
+    p.a = __ldg(q);
+    p.b = __ldg(q + 1);
+    p.c = __ldg(q + 2);
+    p.d = __ldg(q + 3);
+    return p;
+}
+
+// Closest hit among the elements whose AABB the segment [tmin, kTmax] overlaps; equal t keeps the
+// lower element index.  Internal nodes are pruned against the closest hit so far with slack
+// (their boxes bound every surface below them with a margin); leaves test the exact AABB.
+__device__ __forceinline__ int traverse(const Node* __restrict__ nodes, const Prim* __restrict__ prims, float3 o,
+                                        float3 d, float tmin, float& best_t, uint32_t& best_type) {
+    const float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    int best = -1;
+    best_t = __int_as_float(0x7f800000);
+    float prune = kTmax;
+    int node = 0;
+    while (node >= 0) {
+        const float4* q = reinterpret_cast<const float4*>(nodes + node);
+        const float4 lo = __ldg(q), hi = __ldg(q + 1);
+        const float t0x = (lo.x - o.x) * inv.x, t1x = (hi.x - o.x) * inv.x;
+        const float t0y = (lo.y - o.y) * inv.y, t1y = (hi.y - o.y) * inv.y;
+        const float t0z = (lo.z - o.z) * inv.z, t1z = (hi.z - o.z) * inv.z;
+        const float tn = fmaxf(tmin, fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z)));
+        const float tf = fminf(fmaxf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+        const uint32_t hitw = __float_as_uint(lo.w);
+        const int miss = __float_as_int(hi.w);
+        if (hitw & kLeafFlag) {
+            if (tn <= fminf(kTmax, tf)) {
+                const uint32_t prim = hitw & kPrimMask;
+                const uint32_t type = (hitw >> kTypeShift) & 7u;
+                float t;
+                if (hit_prim(type, load_prim(prims, prim), o, d, tmin, t) &&
+                    (t < best_t || (t == best_t && (int)prim < best))) {
+                    best = (int)prim;
+                    best_t = t;
+                    best_type = type;
+                    prune = fminf(kTmax, best_t + best_t * 1e-3f + 1e-3f);
+                }
+            }
+            node = miss;
+        } else {
+            node = (tn <= fminf(prune, tf)) ? (int)hitw : miss;
+        }
+    }
+    return best;
+}
+
+// ------------------------------------------------------------------------------ trace ---------
+// Records go straight into this thread's slots of the shared-memory staging area (slot index is
+// data dependent; a register array would be demoted to local memory).
+__device__ void trace_ray(const TraceArgs& A, uint64_t ray, const SunFrame& S, float4* slot, uint32_t* id) {
+    // ray generation, cuda/sun.cu:28-38 and :94-115
+    const float hu = halton2(ray), hv = halton3(ray);
+    const float3 pos = add(add(xyz(S.v0), scale(hu, xyz(S.e1))), scale(hv, xyz(S.e2)));
+    const u32x4 r0 = draw_block(ray, 0, 0, A.instance, A.seed);
+    const float3 w = xyz(S.w), cu = xyz(S.u), cv = xyz(S.v);
+    float3 dir;
+    if (S.shape == 1) {
+        float g1, g2;
+        box_muller(u01(r0.x), u01(r0.y), g1, g2);
+        dir = normalize(add(add(w, scale(S.sigma * g1, cu)), scale(S.sigma * g2, cv)));
+    } else {
+        const float rand1 = u01(r0.x), rand2 = u01(r0.y);
+        const float phi = kTwoPi * rand1;
+        const float z = S.cos_theta + (1.0f - S.cos_theta) * rand2;
+        const float r = sqrtf(1.0f - z * z);
+        float sp, cp;
+        det_sincos(phi, sp, cp);
+        dir = normalize(add(scale(r, add(scale(cp, cu), scale(sp, cv))), scale(z, w)));
+    }
+    slot[0] = make_float4(0.0f, pos.x, pos.y, pos.z);
+
+    float3 o = pos, d = dir;
+    float tmin = kTminSun;
+    int depth = 0;
+    for (;;) {
+        float t;
+        uint32_t type = 0;
+        const int best = traverse(A.nodes, A.prims, o, d, tmin, t, type);
+        if (best < 0) break;  // __miss__ms, cuda/materials.cu:236-253
+        const int nd = depth + 1;
+        const float3 hit = add(o, scale(t, d));
+        if (type == kFlatMirror || type == kParabolicMirror) {
+            // __closesthit__mirror / __closesthit__mirror__parabolic, cuda/materials.cu:26-84,170-231
+            if (nd >= kMaxDepth) break;
+            const Prim p = load_prim(A.prims, (uint32_t)best);
+            float3 wn;
+            if (type == kFlatMirror) {
+                wn = normalize(xyz(p.a));
+            } else {
+                wn = normalize(parab_normal(p, o, d, t));
+            }
+            float3 ffn = (dot(neg(d), wn) >= 0.0f) ? wn : neg(wn);
+            slot[nd] = make_float4(1.0f, hit.x, hit.y, hit.z);
+            id[nd] = (uint32_t)best;
+            const Optics op = A.optics[best];
+            const bool need_rng = (op.slope > 0.0f) || (op.spec > 0.0f) || !(op.reflectivity >= 1.0f);
+            u32x4 ra = {0u, 0u, 0u, 0u};
+            if (need_rng) ra = draw_block(ray, (uint32_t)nd, 0, A.instance, A.seed);
+            if (op.slope > 0.0f) {
+                float g1, g2;
+                box_muller(u01(ra.y), u01(ra.z), g1, g2);
+                ffn = perturb(ffn, op.slope, g1, g2);
+            }
+            float3 rd = reflect(d, ffn);
+            if (op.spec > 0.0f) {
+                const u32x4 rb = draw_block(ray, (uint32_t)nd, 1, A.instance, A.seed);
+                float g1, g2;
+                box_muller(u01(rb.x), u01(rb.y), g1, g2);
+                rd = perturb(normalize(rd), op.spec, g1, g2);
+            }
+            if (need_rng && u01(ra.x) > op.reflectivity) break;  // absorbed at the mirror
+            depth = nd;
+            o = hit;
+            d = rd;
+            tmin = kTminBounce;
+            continue;
+        }
+        if (type == kFlatReceiver) {
+            // __closesthit__receiver, cuda/materials.cu:86-121: front face only
+            const Prim p = load_prim(A.prims, (uint32_t)best);
+            const float3 rn = cross(xyz(p.c), xyz(p.d));
+            if (dot(d, rn) < 0.0f && nd < kMaxDepth) {
+                slot[nd] = make_float4(2.0f, hit.x, hit.y, hit.z);
+                id[nd] = (uint32_t)best;
+            }
+            break;
+        }
+        // __closesthit__receiver__cylinder__y, cuda/materials.cu:123-163
+        if (nd < kMaxDepth) {
+            slot[nd] = make_float4(2.0f, hit.x, hit.y, hit.z);
+            id[nd] = (uint32_t)best;
+        }
+        break;
+    }
+}
+
+__global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceArgs A) {
+    __shared__ float4 s_hits[kTraceBlock * kMaxDepth];
+    __shared__ uint32_t s_ids[kTraceBlock * kMaxDepth];
+    __shared__ SunFrame s_sun;
+    if (threadIdx.x < sizeof(SunFrame) / 4)
+        reinterpret_cast<uint32_t*>(&s_sun)[threadIdx.x] = reinterpret_cast<const uint32_t*>(A.sun)[threadIdx.x];
+    __syncthreads();
+
+    const uint64_t k = (uint64_t)blockIdx.x * kTraceBlock + threadIdx.x;
+    // the warp's 32 x 80 B of records are staged in shared memory (stride 80 B per lane: the
+    // 16-byte stores of each quarter warp hit distinct banks), then written as 5 fully coalesced
+    // 512-byte rows in the ray-major layout of the reference's hit_point_buffer
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float4* wh = s_hits + warp * 32 * kMaxDepth;
+    uint32_t* wi = s_ids + warp * 32 * kMaxDepth;
+    float4* slot = wh + lane * kMaxDepth;
+    uint32_t* id = wi + lane * kMaxDepth;
+#pragma unroll
+    for (int s = 0; s < kMaxDepth; ++s) {
+        slot[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+        id[s] = kNoElement;
+    }
+    if (k < A.count) trace_ray(A, A.ray_begin + k, s_sun, slot, id);
+    __syncwarp();
+    const uint64_t warp_first = (uint64_t)blockIdx.x * kTraceBlock + (uint64_t)warp * 32;
+    if (warp_first >= A.count) return;
+    const uint64_t n_rec = min((uint64_t)32, A.count - warp_first) * kMaxDepth;
+    float4* gh = A.hits + warp_first * kMaxDepth;
+#pragma unroll
+    for (int s = 0; s < kMaxDepth; ++s) {
+        const uint32_t e = (uint32_t)(s * 32 + lane);
+        if (e < n_rec) __stcs(gh + e, wh[e]);
+    }
+    if (A.ids) {
+        uint32_t* gi = A.ids + warp_first * kMaxDepth;
+#pragma unroll
+        for (int s = 0; s < kMaxDepth; ++s) {
+            const uint32_t e = (uint32_t)(s * 32 + lane);
+            if (e < n_rec) __stcs(gi + e, wi[e]);
+        }
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_prepare_sun(const Aabb* aabbs, int n, float sx, float sy, float sz, float tan_pad, int shape,
+                               float param, SunFrame* out, cudaStream_t stream) {
+    prepare_sun_kernel<<<1, kPrepBlock, 0, stream>>>(aabbs, n, make_float3(sx, sy, sz), tan_pad, shape, param, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace(const TraceArgs& args, cudaStream_t stream) {
+    if (args.count == 0) return cudaSuccess;
+    const uint64_t blocks = (args.count + kTraceBlock - 1) / kTraceBlock;
+    if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
+    trace_kernel<<<(unsigned)blocks, kTraceBlock, 0, stream>>>(args);
+    return cudaGetLastError();
+}
+
+}  // namespace csp

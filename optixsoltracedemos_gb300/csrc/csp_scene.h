@@ -1,0 +1,43 @@
+// csp_scene.h -- host scene model: elements -> device records, acceleration structure, refit.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "csp_c_api.h"
+#include "csp_types.cuh"
+
+namespace csp {
+
+struct HostScene {
+    std::vector<Prim> prims;      // per element, element order
+    std::vector<Optics> optics;   // per element
+    std::vector<Aabb> aabbs;      // exact element AABBs (float), element order
+    std::vector<Aabb> prune;      // boxes bounding each element's surface (sag, rounding margin)
+    std::vector<uint32_t> types;  // EntityType per element
+    std::vector<Node> nodes;      // traversal order
+    std::vector<int32_t> parent;  // parent node of each node (-1 for the root), for refits
+    std::vector<int32_t> leaf_of; // node index of each element's leaf
+    float sun[3] = {0, 0, 1};     // normalized sun vector, float
+};
+
+// Build prims, optics, AABBs, pruning boxes and entity types.  Returns CSP_OK or an error status
+// with `err` filled.  The geometry arithmetic is the reference's (lib/element.cpp, lib/math_util.h,
+// cuda/GeometryDataST.h constructors), in the same double/float operation order.
+int build_elements(const csp_element* el, uint32_t n, HostScene& s, std::string& err);
+
+// Build the stackless BVH over the pruning boxes (binned SAH, one element per leaf; scenes of up
+// to kFlatListMax elements get a plain list of leaves instead).
+constexpr uint32_t kFlatListMax = 8;
+void build_bvh(HostScene& s);
+
+// Recompute every node box of an existing topology from the current aabbs/prune boxes (children
+// are stored after their parents, so one reverse sweep is a bottom-up refit).
+void refit_bvh(HostScene& s);
+
+// normalized sun vector in double, cast to float (SolTraceSystem::initialize,
+// lib/soltrace_system.cpp:81-85)
+void sun_vector_f(const double d[3], float out[3]);
+
+}  // namespace csp

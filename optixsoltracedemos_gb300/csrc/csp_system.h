@@ -1,0 +1,66 @@
+// csp_system.h -- state behind one csp_handle.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "csp_c_api.h"
+#include "csp_kernels.cuh"
+#include "csp_scene.h"
+
+namespace csp {
+
+int set_error(int status, const std::string& msg);
+int cuda_status(cudaError_t e, const char* what);
+
+struct System {
+    int device = -1;
+    uint64_t num_rays = 0;
+    std::vector<csp_element> elements;
+    double sun_dir[3] = {0.0, 0.0, 1.0};
+    int sun_shape = CSP_SUN_PILLBOX;
+    double sun_param = 0.0;
+    uint64_t seed = 0;
+    uint32_t instance = 0;
+    bool record_ids = false;
+    bool initialized = false;
+
+    HostScene scene;
+
+    Node* d_nodes = nullptr;
+    Prim* d_prims = nullptr;
+    Optics* d_optics = nullptr;
+    Aabb* d_aabbs = nullptr;
+    SunFrame* d_sun = nullptr;
+    float4* d_hits = nullptr;
+    uint32_t* d_ids = nullptr;
+    size_t cap_nodes = 0, cap_prims = 0, cap_optics = 0, cap_aabbs = 0;
+    uint64_t cap_rays = 0;
+    bool ids_allocated = false;
+
+    cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    double time_setup = 0.0;
+    double time_trace = 0.0;
+
+    ~System();
+    void release();
+    int ensure_streams();
+    int upload_scene();
+    int prepare_sun();
+    float pad_angle() const;
+    int ensure_hit_buffers();
+    int initialize();
+    int update();
+    TraceArgs args(uint64_t begin, uint64_t count) const;
+    int trace_async(cudaStream_t st);
+    int run();
+    int run_to_host(float* dst, uint32_t* ids);
+};
+
+}  // namespace csp

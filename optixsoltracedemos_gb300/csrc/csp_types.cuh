@@ -1,0 +1,121 @@
+// csp_types.cuh -- device data layout shared by the host scene builder and the CUDA kernels.
+//
+// Layout in HBM (all arrays 16-byte aligned, read through the read-only path):
+//   Prim   [n]      64 B  geometry of one element in the form its intersection test consumes
+//   Optics [n]      16 B  reflectivity, slope error, specularity error (extension)
+//   Aabb   [n]      32 B  element AABB exactly as the reference hands it to OptiX (float)
+//   Node   [m]      32 B  stackless BVH node: box + hit link + miss link
+//   SunFrame        sun-plane parallelogram and cone frame, written on device by the prepare kernel
+//   hits   [N*5]    80 B/ray  float4 {stage, x, y, z}, the reference's hit_point_buffer
+//   ids    [N*5]    20 B/ray  uint32 element index per slot (optional)
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace csp {
+
+// OpticalEntityType of the reference (cuda/Soltrace.h:24-30).
+enum EntityType : uint32_t { kFlatMirror = 0, kParabolicMirror = 1, kFlatReceiver = 2, kCylReceiver = 3 };
+
+constexpr int kMaxDepth = 5;               // MAX_TRACE_DEPTH (cuda/Soltrace.h:11)
+constexpr float kTminSun = 0.001f;         // cuda/sun.cu:123
+constexpr float kTminBounce = 0.01f;       // cuda/materials.cu:76
+constexpr float kTmax = 1e16f;             // cuda/sun.cu:124
+constexpr uint32_t kLeafFlag = 0x80000000u;
+constexpr uint32_t kTypeShift = 28;
+constexpr uint32_t kPrimMask = 0x0FFFFFFFu;
+constexpr uint32_t kNoElement = 0xFFFFFFFFu;
+
+// Prim field layout by entity type (all values float, computed on the host with the same float
+// operations the reference's intersection programs perform per call, so hoisting them is exact):
+//  flat mirror / flat receiver (Rectangle_Flat, cuda/GeometryDataST.h:41-58):
+//    a = (plane normal n, plane w)   b = (center, width/2)   c = (x axis, height/2)   d = (y axis, 0)
+//  parabolic mirror (Rectangle_Parabolic, cuda/GeometryDataST.h:79-103, cuda/intersection.cu:335-352):
+//    a = (e1, L1/2)   b = (e2, L2/2)   c = (n = normalize(e2 x e1), curv_x)   d = (rect center, curv_y)
+//  cylinder receiver (Cylinder_Y, cuda/GeometryDataST.h:60-77, cuda/intersection.cu:188-194):
+//    a = (center, radius)   b = (local x, half height)   c = (local y = z x x, radius^2)   d = (local z, 0)
+struct alignas(16) Prim {
+    float4 a, b, c, d;
+};
+
+struct alignas(16) Optics {
+    float reflectivity, slope, spec, pad;
+};
+
+struct alignas(16) Aabb {
+    float4 lo;  // xyz, w unused
+    float4 hi;
+};
+
+// Stackless BVH node.  lo.w / hi.w carry int32 links (bit patterns):
+//   internal: hit = index of the first child, visited when the box is entered; miss = next node
+//             in traversal order once this subtree is done (-1 = end).
+//   leaf:     hit = kLeafFlag | type << kTypeShift | element index; miss as above.
+// Internal boxes bound every surface below them (sag-inflated for paraboloids); a leaf box is the
+// element's exact AABB, the box whose overlap decides whether the element is tested at all.
+struct alignas(16) Node {
+    float4 lo;
+    float4 hi;
+};
+
+struct alignas(16) SunFrame {
+    float4 s_d;    // normalized sun vector, plane distance d
+    float4 v0;     // parallelogram corner
+    float4 e1;     // v1 - v0
+    float4 e2;     // v3 - v0
+    float4 v1, v2, v3;
+    float4 w;      // cone axis = -sun
+    float4 u, v;   // cone frame
+    float cos_theta, sigma, tan_pad, pad;
+    int shape, n_prims, pad1, pad2;
+};
+
+// Halton base-3 digit weights: f_k = fl(f_{k-1} / 3), f_0 = 1 (the float sequence cuda/sun.cu:19
+// produces), k = 1..41 enough for 64-bit indices.
+#ifdef __CUDACC__
+__constant__ const float c_halton3_f[41] = {
+    0x1.5555560000000p-2f,
+    0x1.c71c720000000p-4f,
+    0x1.2f684c0000000p-5f,
+    0x1.948b100000000p-7f,
+    0x1.0db20a0000000p-8f,
+    0x1.67980e0000000p-10f,
+    0x1.df75680000000p-12f,
+    0x1.3fa39a0000000p-13f,
+    0x1.aa2f780000000p-15f,
+    0x1.1c1fa60000000p-16f,
+    0x1.7ad4de0000000p-18f,
+    0x1.f91bd20000000p-20f,
+    0x1.50bd360000000p-21f,
+    0x1.c0fc480000000p-23f,
+    0x1.2b52da0000000p-24f,
+    0x1.8f19220000000p-26f,
+    0x1.0a10c20000000p-27f,
+    0x1.62c1020000000p-29f,
+    0x1.d901580000000p-31f,
+    0x1.3b563a0000000p-32f,
+    0x1.a472f80000000p-34f,
+    0x1.184ca60000000p-35f,
+    0x1.75bb880000000p-37f,
+    0x1.f24f600000000p-39f,
+    0x1.4c34ea0000000p-40f,
+    0x1.baf1380000000p-42f,
+    0x1.274b7a0000000p-43f,
+    0x1.89b9f80000000p-45f,
+    0x1.067bfa0000000p-46f,
+    0x1.5dfaa20000000p-48f,
+    0x1.d2a3820000000p-50f,
+    0x1.3717ac0000000p-51f,
+    0x1.9eca3a0000000p-53f,
+    0x1.1486d20000000p-54f,
+    0x1.70b3c20000000p-56f,
+    0x1.eb9a580000000p-58f,
+    0x1.47bc3a0000000p-59f,
+    0x1.b4faf80000000p-61f,
+    0x1.2351fa0000000p-62f,
+    0x1.846d4e0000000p-64f,
+    0x1.02f38a0000000p-65f
+};
+#endif
+
+}  // namespace csp

@@ -1,0 +1,219 @@
+"""ctypes binding of libcsp_gb300.so (the C ABI declared in include/csp_c_api.h).
+
+There is no fallback: if the native library is missing or fails to load, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from .scenes import ELEMENT_DTYPE
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_lib", "libcsp_gb300.so")
+MAX_DEPTH = 5
+NO_ELEMENT = 0xFFFFFFFF
+
+STATUS = {
+    0: "CSP_OK",
+    -1: "CSP_ERR_INVALID_ARGUMENT",
+    -2: "CSP_ERR_CUDA",
+    -3: "CSP_ERR_OUT_OF_MEMORY",
+    -4: "CSP_ERR_BAD_SCENE",
+    -5: "CSP_ERR_TIMEOUT",
+    -6: "CSP_ERR_STATE",
+    -7: "CSP_ERR_IO",
+    -8: "CSP_ERR_PARSE",
+}
+
+# every entry point of include/csp_c_api.h: name -> (restype, argtypes)
+_H = ctypes.c_void_p
+_P = ctypes.c_void_p
+SIGNATURES = {
+    "csp_last_error": (ctypes.c_char_p, []),
+    "csp_abi_version": (ctypes.c_int, []),
+    "csp_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_uint64]),
+    "csp_destroy": (ctypes.c_int, [_H]),
+    "csp_set_num_rays": (ctypes.c_int, [_H, ctypes.c_uint64]),
+    "csp_add_element": (ctypes.c_int, [_H, _P]),
+    "csp_set_elements": (ctypes.c_int, [_H, _P, ctypes.c_uint32]),
+    "csp_get_num_elements": (ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_uint32)]),
+    "csp_get_elements": (ctypes.c_int, [_H, _P, ctypes.c_uint32]),
+    "csp_set_sun_vector": (ctypes.c_int, [_H, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
+    "csp_set_sun_shape": (ctypes.c_int, [_H, ctypes.c_int, ctypes.c_double]),
+    "csp_set_seed": (ctypes.c_int, [_H, ctypes.c_uint64, ctypes.c_uint32]),
+    "csp_set_record_ids": (ctypes.c_int, [_H, ctypes.c_int]),
+    "csp_initialize": (ctypes.c_int, [_H]),
+    "csp_run": (ctypes.c_int, [_H]),
+    "csp_trace_async": (ctypes.c_int, [_H, _P]),
+    "csp_update": (ctypes.c_int, [_H]),
+    "csp_copy_hits": (ctypes.c_int, [_H, _P, _P, ctypes.c_uint64, ctypes.c_uint64]),
+    "csp_run_to_host": (ctypes.c_int, [_H, _P, _P]),
+    "csp_get_device_buffers": (ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p)]),
+    "csp_get_timing": (ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    "csp_get_sun_plane": (ctypes.c_int, [_H, _P]),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+class CspError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+def load(path: str | None = None) -> ctypes.CDLL:
+    """Load the native library (no fallback)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise RuntimeError(f"native library {p} is missing: run optixsoltracedemos_gb300.build.build()")
+        lib = ctypes.CDLL(p)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+        return lib
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise CspError(rc, load().csp_last_error().decode(errors="replace"))
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Tracer:
+    """One csp_handle: scene, sun, device buffers."""
+
+    def __init__(self, device: int = 0, num_rays: int = 0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        _check(self.lib.csp_create(ctypes.byref(h), int(device), int(num_rays)))
+        self.h = h
+        self.num_rays = int(num_rays)
+        self.record_ids = False
+
+    # ---- configuration
+    def set_num_rays(self, n: int):
+        _check(self.lib.csp_set_num_rays(self.h, int(n)))
+        self.num_rays = int(n)
+
+    def set_elements(self, elements: np.ndarray):
+        e = np.ascontiguousarray(elements)
+        if e.dtype != ELEMENT_DTYPE:
+            raise TypeError("elements must use scenes.ELEMENT_DTYPE")
+        _check(self.lib.csp_set_elements(self.h, _ptr(e), len(e)))
+
+    def add_element(self, element: np.ndarray):
+        e = np.ascontiguousarray(element.reshape(1))
+        _check(self.lib.csp_add_element(self.h, _ptr(e)))
+
+    def get_elements(self) -> np.ndarray:
+        n = ctypes.c_uint32()
+        _check(self.lib.csp_get_num_elements(self.h, ctypes.byref(n)))
+        out = np.zeros(n.value, ELEMENT_DTYPE)
+        if n.value:
+            _check(self.lib.csp_get_elements(self.h, _ptr(out), n.value))
+        return out
+
+    def set_sun_vector(self, x, y=None, z=None):
+        if y is None:
+            x, y, z = x
+        _check(self.lib.csp_set_sun_vector(self.h, float(x), float(y), float(z)))
+
+    def set_sun_shape(self, shape: int, param: float):
+        _check(self.lib.csp_set_sun_shape(self.h, int(shape), float(param)))
+
+    def set_seed(self, seed: int, instance: int = 0):
+        _check(self.lib.csp_set_seed(self.h, int(seed), int(instance)))
+
+    def set_record_ids(self, enable: bool = True):
+        _check(self.lib.csp_set_record_ids(self.h, 1 if enable else 0))
+        self.record_ids = bool(enable)
+
+    # ---- lifecycle
+    def initialize(self):
+        _check(self.lib.csp_initialize(self.h))
+
+    def run(self):
+        _check(self.lib.csp_run(self.h))
+
+    def trace_async(self, stream: int | None = None):
+        _check(self.lib.csp_trace_async(self.h, ctypes.c_void_p(stream or 0)))
+
+    def update(self):
+        _check(self.lib.csp_update(self.h))
+
+    def copy_hits(self, first: int = 0, count: int | None = None, with_ids: bool | None = None):
+        count = self.num_rays - first if count is None else count
+        hits = np.empty((count, MAX_DEPTH, 4), np.float32)
+        with_ids = self.record_ids if with_ids is None else with_ids
+        ids = np.empty((count, MAX_DEPTH), np.uint32) if with_ids else None
+        _check(self.lib.csp_copy_hits(self.h, _ptr(hits), _ptr(ids), int(first), int(count)))
+        return hits, ids
+
+    def run_to_host(self, hits: np.ndarray, ids: np.ndarray | None = None):
+        """hits: float32 array with num_rays*5*4 elements (page-locked for full speed)."""
+        if hits.dtype != np.float32 or hits.size != self.num_rays * MAX_DEPTH * 4 or not hits.flags.c_contiguous:
+            raise ValueError("hits must be a contiguous float32 array of num_rays*5*4 elements")
+        _check(self.lib.csp_run_to_host(self.h, _ptr(hits), _ptr(ids)))
+
+    def run_to_host_ptr(self, hits_ptr: int, ids_ptr: int | None = None):
+        _check(self.lib.csp_run_to_host(self.h, ctypes.c_void_p(hits_ptr), ctypes.c_void_p(ids_ptr or 0)))
+
+    def device_buffers(self):
+        a, b = ctypes.c_void_p(), ctypes.c_void_p()
+        _check(self.lib.csp_get_device_buffers(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def timing(self):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        _check(self.lib.csp_get_timing(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def sun_plane(self) -> np.ndarray:
+        out = np.zeros(16, np.float32)
+        _check(self.lib.csp_get_sun_plane(self.h, _ptr(out)))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            _check(self.lib.csp_destroy(self.h))
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def tracer_for(scene, device: int = 0, seed: int = 0, instance: int = 0, record_ids: bool = True,
+               num_rays: int | None = None) -> Tracer:
+    """Tracer configured and initialized for a scenes.Scene."""
+    t = Tracer(device, scene.num_rays if num_rays is None else num_rays)
+    t.set_elements(scene.elements)
+    t.set_sun_vector(scene.sun_dir)
+    t.set_sun_shape(scene.sun_shape, scene.sun_param)
+    t.set_seed(seed, instance)
+    t.set_record_ids(record_ids)
+    t.initialize()
+    return t
