@@ -130,6 +130,20 @@ CSP_API int csp_run_to_host(csp_handle h, float* dst, uint32_t* ids);
 CSP_API int csp_get_device_buffers(csp_handle h, void** hits, void** ids);
 
 CSP_API int csp_get_timing(csp_handle h, double* setup_s, double* trace_s);
+
+/* ---- SolTrace .stinput input and hit-record CSV output ---- */
+/* Also apply each element's front optical surface (reflectivity, RMS slope / specularity error in
+ * mrad) -- the reference parses and discards these values; without the flag so does this reader. */
+#define CSP_STINPUT_APPLY_OPTICS 1
+/* Parse a .stinput file on the host (no GPU).  With out == NULL only *count is set. */
+CSP_API int csp_parse_stinput(const char* path, csp_element* out, uint32_t capacity, uint32_t* count,
+                              double* sun_dir, double* sun_angle, int flags);
+/* Append the file's elements to the handle and take its sun vector and angle (pillbox). */
+CSP_API int csp_read_stinput(csp_handle h, const char* path, int flags);
+/* Write num_rays x 5 hit records (host memory) as the reference's CSV (no GPU). */
+CSP_API int csp_write_hits_csv(const float* hits, uint64_t num_rays, const char* path);
+/* Copy the hit buffer to the host and write it as CSV (write_output). */
+CSP_API int csp_write_output(csp_handle h, const char* path);
 /* out[16]: sun vector (3), v0 (3), v1 (3), v2 (3), v3 (3), plane distance (1). */
 CSP_API int csp_get_sun_plane(csp_handle h, float* out);
 

@@ -24,6 +24,7 @@ SOURCES = [
     "csp_kernels.cu",
     "csp_scene.cpp",
     "csp_c_api.cpp",
+    "csp_io.cpp",
 ]
 COMMON = [
     "-O3",

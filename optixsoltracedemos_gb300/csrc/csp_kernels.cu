@@ -298,7 +298,7 @@ __device__ __forceinline__ int traverse(const Node* __restrict__ nodes, const Pr
         const float t0y = (lo.y - o.y) * inv.y, t1y = (hi.y - o.y) * inv.y;
         const float t0z = (lo.z - o.z) * inv.z, t1z = (hi.z - o.z) * inv.z;
         const float tn = fmaxf(tmin, fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z)));
-        const float tf = fminf(fmaxf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+        const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
         const uint32_t hitw = __float_as_uint(lo.w);
         const int miss = __float_as_int(hi.w);
         if (hitw & kLeafFlag) {

@@ -55,7 +55,13 @@ SIGNATURES = {
     "csp_get_device_buffers": (ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p)]),
     "csp_get_timing": (ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "csp_get_sun_plane": (ctypes.c_int, [_H, _P]),
+    "csp_parse_stinput": (ctypes.c_int, [ctypes.c_char_p, _P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32), _P, _P,
+                                         ctypes.c_int]),
+    "csp_read_stinput": (ctypes.c_int, [_H, ctypes.c_char_p, ctypes.c_int]),
+    "csp_write_hits_csv": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.c_char_p]),
+    "csp_write_output": (ctypes.c_int, [_H, ctypes.c_char_p]),
 }
+STINPUT_APPLY_OPTICS = 1
 
 _lib = None
 _lock = threading.Lock()
@@ -188,6 +194,12 @@ class Tracer:
         _check(self.lib.csp_get_sun_plane(self.h, _ptr(out)))
         return out
 
+    def read_stinput(self, path: str, apply_optics: bool = False):
+        _check(self.lib.csp_read_stinput(self.h, path.encode(), STINPUT_APPLY_OPTICS if apply_optics else 0))
+
+    def write_output(self, path: str):
+        _check(self.lib.csp_write_output(self.h, path.encode()))
+
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:
             _check(self.lib.csp_destroy(self.h))
@@ -204,6 +216,25 @@ class Tracer:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def parse_stinput(path: str, apply_optics: bool = False):
+    """Host-only .stinput parse: (elements, sun_dir, sun_angle)."""
+    lib = load()
+    n = ctypes.c_uint32()
+    sun = np.zeros(3, np.float64)
+    ang = np.zeros(1, np.float64)
+    fl = STINPUT_APPLY_OPTICS if apply_optics else 0
+    _check(lib.csp_parse_stinput(path.encode(), None, 0, ctypes.byref(n), _ptr(sun), _ptr(ang), fl))
+    out = np.zeros(n.value, ELEMENT_DTYPE)
+    _check(lib.csp_parse_stinput(path.encode(), _ptr(out), n.value, ctypes.byref(n), _ptr(sun), _ptr(ang), fl))
+    return out, sun, float(ang[0])
+
+
+def write_hits_csv(hits: np.ndarray, path: str) -> None:
+    """Host-only CSV writer of [N, 5, 4] float32 hit records (the reference's write_output format)."""
+    h = np.ascontiguousarray(hits, np.float32)
+    _check(load().csp_write_hits_csv(_ptr(h), h.shape[0], path.encode()))
 
 
 def tracer_for(scene, device: int = 0, seed: int = 0, instance: int = 0, record_ids: bool = True,
