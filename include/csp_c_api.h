@@ -131,6 +131,12 @@ CSP_API int csp_get_device_buffers(csp_handle h, void** hits, void** ids);
 
 CSP_API int csp_get_timing(csp_handle h, double* setup_s, double* trace_s);
 
+/* Host-only element geometry (no GPU): Euler angles (yaw, pitch, roll; rad), global-to-local
+ * matrix (row-major, rows = the element's local x, y, z axes in world space) and exact double AABB,
+ * as Element::update_euler_angles / get_rotation_matrix / compute_bounding_box compute them
+ * (lib/element.cpp:77-93,97-103,172-275, lib/math_util.h:21-59).  Any output may be NULL. */
+CSP_API int csp_element_frame(const csp_element* e, double* euler, double* g2l, double* aabb_lo, double* aabb_hi);
+
 /* ---- SolTrace .stinput input and hit-record CSV output ---- */
 /* Also apply each element's front optical surface (reflectivity, RMS slope / specularity error in
  * mrad) -- the reference parses and discards these values; without the flag so does this reader. */

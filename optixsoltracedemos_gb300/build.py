@@ -25,6 +25,7 @@ SOURCES = [
     "csp_scene.cpp",
     "csp_c_api.cpp",
     "csp_io.cpp",
+    "../cpp/src/dropin.cpp",
 ]
 COMMON = [
     "-O3",
@@ -37,6 +38,7 @@ COMMON = [
     "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden,-fno-fast-math",
     "-I", os.path.join(ROOT, "include"),
     "-I", CSRC,
+    "-I", os.path.join(PKG, "cpp", "include"),
 ]
 
 
@@ -64,8 +66,9 @@ def _stale() -> bool:
     if not os.path.exists(LIB_PATH):
         return True
     t = os.path.getmtime(LIB_PATH)
-    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", f)
-                                                                for f in os.listdir(os.path.join(ROOT, "include"))]
+    deps = []
+    for d in (CSRC, os.path.join(ROOT, "include"), os.path.join(PKG, "cpp", "include"), os.path.join(PKG, "cpp", "src")):
+        deps += [os.path.join(d, f) for f in os.listdir(d) if os.path.isfile(os.path.join(d, f))]
     return any(os.path.getmtime(d) > t for d in deps) or os.path.getmtime(__file__) > t
 
 

@@ -1,0 +1,2 @@
+// Case alias: the reference includes this header under both spellings.
+#include "Aperture.h"

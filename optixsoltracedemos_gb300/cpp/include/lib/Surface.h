@@ -1,0 +1,2 @@
+// Forwarding header: the reference addresses its headers as lib/<name>.
+#include "../Surface.h"

@@ -418,6 +418,17 @@ int csp_get_timing(csp_handle h, double* setup_s, double* trace_s) {
     return CSP_OK;
 }
 
+int csp_element_frame(const csp_element* e, double* euler, double* g2l, double* aabb_lo, double* aabb_hi) {
+    if (!e) return fail(CSP_ERR_INVALID_ARGUMENT, "null element");
+    double eu[3], G[9], lo[3], hi[3];
+    csp::element_frame(*e, eu, G, lo, hi);
+    if (euler) std::memcpy(euler, eu, sizeof eu);
+    if (g2l) std::memcpy(g2l, G, sizeof G);
+    if (aabb_lo) std::memcpy(aabb_lo, lo, sizeof lo);
+    if (aabb_hi) std::memcpy(aabb_hi, hi, sizeof hi);
+    return CSP_OK;
+}
+
 int csp_get_sun_plane(csp_handle h, float* out) {
     CSP_GUARD(h);
     System* s = reinterpret_cast<System*>(h);

@@ -11,6 +11,7 @@
 //                       elements whose AABB the ray overlaps (OptiX traversal + the intersection
 //                       programs of cuda/intersection.cu:47-85,177-296,318-448), shading
 //                       (cuda/materials.cu:26-231) and the hit_point_buffer write.
+#include <algorithm>
 #include <cfloat>
 
 #include "csp_kernels.cuh"
@@ -145,6 +146,25 @@ __device__ __forceinline__ float halton3(uint64_t i) {
     uint32_t j = (uint32_t)i;
     while (j > 0) {
         const uint32_t q = j / 3u;
+        r = r + c_halton3_f[k++] * (float)(j - 3u * q);
+        j = q;
+    }
+    return r;
+}
+
+// Same fold with its first six steps looked up: t6[m] = halton3(m) for m < 3^6.  For larger i the
+// reference loop continues from exactly that partial sum with the seventh digit (a zero digit adds
+// +0, which leaves the sum unchanged), so the result is identical bit for bit.
+constexpr uint32_t kH3TabDigits = 6, kH3Tab = 729;
+__device__ __forceinline__ float halton3_tab(uint64_t i, const float* __restrict__ t6) {
+    if (i >= (1ull << 32)) return halton3(i);
+    uint32_t j = (uint32_t)i;
+    uint32_t q = j / kH3Tab;
+    float r = t6[j - kH3Tab * q];
+    int k = kH3TabDigits;
+    j = q;
+    while (j > 0) {
+        q = j / 3u;
         r = r + c_halton3_f[k++] * (float)(j - 3u * q);
         j = q;
     }
@@ -323,11 +343,113 @@ __device__ __forceinline__ int traverse(const Node* __restrict__ nodes, const Pr
 }
 
 // ------------------------------------------------------------------------------ trace ---------
-// Records go straight into this thread's slots of the shared-memory staging area (slot index is
-// data dependent; a register array would be demoted to local memory).
-__device__ void trace_ray(const TraceArgs& A, uint64_t ray, const SunFrame& S, float4* slot, uint32_t* id) {
-    // ray generation, cuda/sun.cu:28-38 and :94-115
-    const float hu = halton2(ray), hv = halton3(ray);
+// Persistent kernel, wavefront inside each CTA.  A CTA walks tiles of kTraceBlock consecutive rays.
+//   phase A (one ray per thread): sun sample, closest hit of the first segment, its record.  A ray
+//     that hits a mirror is pushed, unshaded, into a shared-memory queue (warp ballot + one shared
+//     atomic per warp).
+//   phase B (only on full batches of kTraceBlock queued rays, and on the remainder at the end):
+//     shade the queued mirror hit (normal, slope/specularity error, reflection, absorption), then
+//     find and record the next hit; mirror hits go back into the queue.
+// In the heliostat workloads ~10% of rays reach a mirror; shading and tracing them on full warps
+// instead of inside warps where ~90% of lanes have already finished is the point of the queue.
+constexpr int kQueueCap = 2 * kTraceBlock;
+
+struct Segment {
+    float3 o, d;
+    float tmin;
+    int depth;
+};
+
+struct Record {
+    float4 rec;
+    uint32_t id;
+    int slot;
+};
+
+// A mirror hit waiting for its closest-hit program: the incoming segment, hit distance, element,
+// entity type and the depth of the hit (its record slot).
+struct Pending {
+    float3 o, d;
+    float t;
+    uint32_t prim;
+    uint32_t type;
+    int depth;
+};
+
+// optixTrace of one segment up to the choice of closest-hit program: closest hit, its record, and
+// for a mirror the pending shading.  Returns true when a mirror hit is pending.
+__device__ __forceinline__ bool find_hit(const TraceArgs& A, const Segment& g, Record& out, Pending& pend) {
+    out.slot = -1;
+    float t;
+    uint32_t type = 0;
+    const int best = traverse(A.nodes, A.prims, g.o, g.d, g.tmin, t, type);
+    if (best < 0) return false;  // __miss__ms, cuda/materials.cu:236-253
+    const int nd = g.depth + 1;
+    if (type == kFlatMirror || type == kParabolicMirror) {
+        // cuda/materials.cu:44-60,180-197: the record is written, and traced on, only below max depth
+        if (nd >= kMaxDepth) return false;
+        const float3 hit = add(g.o, scale(t, g.d));
+        out.rec = make_float4(1.0f, hit.x, hit.y, hit.z);
+        out.id = (uint32_t)best;
+        out.slot = nd;
+        pend = Pending{g.o, g.d, t, (uint32_t)best, type, nd};
+        return true;
+    }
+    const float3 hit = add(g.o, scale(t, g.d));
+    if (type == kFlatReceiver) {
+        // __closesthit__receiver, cuda/materials.cu:86-121: front face only
+        const Prim p = load_prim(A.prims, (uint32_t)best);
+        const float3 rn = cross(xyz(p.c), xyz(p.d));
+        if (dot(g.d, rn) < 0.0f && nd < kMaxDepth) {
+            out.rec = make_float4(2.0f, hit.x, hit.y, hit.z);
+            out.id = (uint32_t)best;
+            out.slot = nd;
+        }
+        return false;
+    }
+    // __closesthit__receiver__cylinder__y, cuda/materials.cu:123-163
+    if (nd < kMaxDepth) {
+        out.rec = make_float4(2.0f, hit.x, hit.y, hit.z);
+        out.id = (uint32_t)best;
+        out.slot = nd;
+    }
+    return false;
+}
+
+// __closesthit__mirror / __closesthit__mirror__parabolic (cuda/materials.cu:26-84,170-231): normal
+// as the intersection program reports it, faced against the ray, ideal reflection; plus the
+// extensions (Gaussian slope and specularity error, absorption with probability 1 - reflectivity).
+// Returns false when the ray is absorbed.
+__device__ __forceinline__ bool shade_mirror(const TraceArgs& A, uint64_t ray, const Pending& q, Segment& next) {
+    const Prim p = load_prim(A.prims, q.prim);
+    const float3 hit = add(q.o, scale(q.t, q.d));
+    const float3 wn = (q.type == kFlatMirror) ? normalize(xyz(p.a)) : normalize(parab_normal(p, q.o, q.d, q.t));
+    float3 ffn = (dot(neg(q.d), wn) >= 0.0f) ? wn : neg(wn);
+    const Optics op = A.optics[q.prim];
+    const bool need_rng = (op.slope > 0.0f) || (op.spec > 0.0f) || !(op.reflectivity >= 1.0f);
+    u32x4 ra = {0u, 0u, 0u, 0u};
+    if (need_rng) ra = draw_block(ray, (uint32_t)q.depth, 0, A.instance, A.seed);
+    if (op.slope > 0.0f) {
+        float g1, g2;
+        box_muller(u01(ra.y), u01(ra.z), g1, g2);
+        ffn = perturb(ffn, op.slope, g1, g2);
+    }
+    float3 rd = reflect(q.d, ffn);
+    if (op.spec > 0.0f) {
+        const u32x4 rb = draw_block(ray, (uint32_t)q.depth, 1, A.instance, A.seed);
+        float g1, g2;
+        box_muller(u01(rb.x), u01(rb.y), g1, g2);
+        rd = perturb(normalize(rd), op.spec, g1, g2);
+    }
+    if (need_rng && u01(ra.x) > op.reflectivity) return false;  // absorbed at the mirror
+    next = Segment{hit, rd, kTminBounce, q.depth};
+    return true;
+}
+
+// Ray generation: cuda/sun.cu:28-38 (Halton point on the sun parallelogram) and :72-91, :106
+// (direction in the sun cone; Gaussian sun as an extension).
+__device__ __forceinline__ Segment generate(const TraceArgs& A, const SunFrame& S, uint64_t ray, const float* t6) {
+    const float hu = halton2(ray), hv = halton3_tab(ray, t6);
     const float3 pos = add(add(xyz(S.v0), scale(hu, xyz(S.e1))), scale(hv, xyz(S.e2)));
     const u32x4 r0 = draw_block(ray, 0, 0, A.instance, A.seed);
     const float3 w = xyz(S.w), cu = xyz(S.u), cv = xyz(S.v);
@@ -345,114 +467,153 @@ __device__ void trace_ray(const TraceArgs& A, uint64_t ray, const SunFrame& S, f
         det_sincos(phi, sp, cp);
         dir = normalize(add(scale(r, add(scale(cp, cu), scale(sp, cv))), scale(z, w)));
     }
-    slot[0] = make_float4(0.0f, pos.x, pos.y, pos.z);
+    return Segment{pos, dir, kTminSun, 0};
+}
 
-    float3 o = pos, d = dir;
-    float tmin = kTminSun;
-    int depth = 0;
-    for (;;) {
-        float t;
-        uint32_t type = 0;
-        const int best = traverse(A.nodes, A.prims, o, d, tmin, t, type);
-        if (best < 0) break;  // __miss__ms, cuda/materials.cu:236-253
-        const int nd = depth + 1;
-        const float3 hit = add(o, scale(t, d));
-        if (type == kFlatMirror || type == kParabolicMirror) {
-            // __closesthit__mirror / __closesthit__mirror__parabolic, cuda/materials.cu:26-84,170-231
-            if (nd >= kMaxDepth) break;
-            const Prim p = load_prim(A.prims, (uint32_t)best);
-            float3 wn;
-            if (type == kFlatMirror) {
-                wn = normalize(xyz(p.a));
-            } else {
-                wn = normalize(parab_normal(p, o, d, t));
-            }
-            float3 ffn = (dot(neg(d), wn) >= 0.0f) ? wn : neg(wn);
-            slot[nd] = make_float4(1.0f, hit.x, hit.y, hit.z);
-            id[nd] = (uint32_t)best;
-            const Optics op = A.optics[best];
-            const bool need_rng = (op.slope > 0.0f) || (op.spec > 0.0f) || !(op.reflectivity >= 1.0f);
-            u32x4 ra = {0u, 0u, 0u, 0u};
-            if (need_rng) ra = draw_block(ray, (uint32_t)nd, 0, A.instance, A.seed);
-            if (op.slope > 0.0f) {
-                float g1, g2;
-                box_muller(u01(ra.y), u01(ra.z), g1, g2);
-                ffn = perturb(ffn, op.slope, g1, g2);
-            }
-            float3 rd = reflect(d, ffn);
-            if (op.spec > 0.0f) {
-                const u32x4 rb = draw_block(ray, (uint32_t)nd, 1, A.instance, A.seed);
-                float g1, g2;
-                box_muller(u01(rb.x), u01(rb.y), g1, g2);
-                rd = perturb(normalize(rd), op.spec, g1, g2);
-            }
-            if (need_rng && u01(ra.x) > op.reflectivity) break;  // absorbed at the mirror
-            depth = nd;
-            o = hit;
-            d = rd;
-            tmin = kTminBounce;
-            continue;
-        }
-        if (type == kFlatReceiver) {
-            // __closesthit__receiver, cuda/materials.cu:86-121: front face only
-            const Prim p = load_prim(A.prims, (uint32_t)best);
-            const float3 rn = cross(xyz(p.c), xyz(p.d));
-            if (dot(d, rn) < 0.0f && nd < kMaxDepth) {
-                slot[nd] = make_float4(2.0f, hit.x, hit.y, hit.z);
-                id[nd] = (uint32_t)best;
-            }
-            break;
-        }
-        // __closesthit__receiver__cylinder__y, cuda/materials.cu:123-163
-        if (nd < kMaxDepth) {
-            slot[nd] = make_float4(2.0f, hit.x, hit.y, hit.z);
-            id[nd] = (uint32_t)best;
-        }
-        break;
+struct TraceSmem {
+    float4 hits[kTraceBlock * kMaxDepth];  // phase A record staging, ray-major per warp
+    uint32_t ids[kTraceBlock * kMaxDepth];
+    float qo[3][kQueueCap], qd[3][kQueueCap], qt[kQueueCap];
+    uint32_t qprim[kQueueCap];
+    uint32_t qmeta[kQueueCap];  // type << 8 | depth
+    uint64_t qray[kQueueCap];
+    float t6[kH3Tab];
+    SunFrame sun;
+    int qsize;
+};
+
+// warp-aggregated append of the lanes with `want` set; every lane of the warp must call it
+__device__ __forceinline__ void push(TraceSmem& sm, bool want, uint64_t ray, const Pending& q) {
+    const unsigned mask = __ballot_sync(0xffffffffu, want);
+    if (mask == 0u) return;
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == __ffs(mask) - 1) base = atomicAdd(&sm.qsize, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
+    if (want) {
+        const int k = base + __popc(mask & ((1u << lane) - 1u));
+        sm.qo[0][k] = q.o.x;
+        sm.qo[1][k] = q.o.y;
+        sm.qo[2][k] = q.o.z;
+        sm.qd[0][k] = q.d.x;
+        sm.qd[1][k] = q.d.y;
+        sm.qd[2][k] = q.d.z;
+        sm.qt[k] = q.t;
+        sm.qprim[k] = q.prim;
+        sm.qmeta[k] = (q.type << 8) | (uint32_t)q.depth;
+        sm.qray[k] = ray;
     }
 }
 
-__global__ void __launch_bounds__(kTraceBlock) trace_kernel(const TraceArgs A) {
-    __shared__ float4 s_hits[kTraceBlock * kMaxDepth];
-    __shared__ uint32_t s_ids[kTraceBlock * kMaxDepth];
-    __shared__ SunFrame s_sun;
+// Phase B: pop up to kTraceBlock queued mirror hits, shade them, find and record the next hit
+// (records go straight to global memory: their rows were written by phase A of an earlier tile of
+// this CTA, ordered by the barriers in between), push new mirror hits back.
+__device__ void drain(const TraceArgs& A, TraceSmem& sm, bool all) {
+    __syncthreads();
+    int qs = sm.qsize;
+    while (qs >= kTraceBlock || (all && qs > 0)) {
+        const int n = min(qs, kTraceBlock);
+        const int base = qs - n;
+        const bool have = (int)threadIdx.x < n;
+        Pending q;
+        uint64_t ray = 0;
+        if (have) {
+            const int k = base + threadIdx.x;
+            q.o = f3(sm.qo[0][k], sm.qo[1][k], sm.qo[2][k]);
+            q.d = f3(sm.qd[0][k], sm.qd[1][k], sm.qd[2][k]);
+            q.t = sm.qt[k];
+            q.prim = sm.qprim[k];
+            q.type = sm.qmeta[k] >> 8;
+            q.depth = (int)(sm.qmeta[k] & 0xffu);
+            ray = sm.qray[k];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) sm.qsize = base;
+        __syncthreads();
+        bool again = false;
+        Pending nq;
+        if (have) {
+            Segment g;
+            if (shade_mirror(A, ray, q, g)) {
+                Record r;
+                again = find_hit(A, g, r, nq);
+                if (r.slot >= 0) {
+                    const uint64_t row = (ray - A.ray_begin) * kMaxDepth + (uint64_t)r.slot;
+                    A.hits[row] = r.rec;
+                    if (A.ids) A.ids[row] = r.id;
+                }
+            }
+        }
+        __syncwarp();
+        push(sm, again, ray, nq);
+        __syncthreads();
+        qs = sm.qsize;
+    }
+}
+
+__global__ void __launch_bounds__(kTraceBlock, 3) trace_kernel(const TraceArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TraceSmem& sm = *reinterpret_cast<TraceSmem*>(smem_raw);
     if (threadIdx.x < sizeof(SunFrame) / 4)
-        reinterpret_cast<uint32_t*>(&s_sun)[threadIdx.x] = reinterpret_cast<const uint32_t*>(A.sun)[threadIdx.x];
+        reinterpret_cast<uint32_t*>(&sm.sun)[threadIdx.x] = reinterpret_cast<const uint32_t*>(A.sun)[threadIdx.x];
+    for (uint32_t m = threadIdx.x; m < kH3Tab; m += kTraceBlock) sm.t6[m] = halton3(m);
+    if (threadIdx.x == 0) sm.qsize = 0;
     __syncthreads();
 
-    const uint64_t k = (uint64_t)blockIdx.x * kTraceBlock + threadIdx.x;
-    // the warp's 32 x 80 B of records are staged in shared memory (stride 80 B per lane: the
-    // 16-byte stores of each quarter warp hit distinct banks), then written as 5 fully coalesced
-    // 512-byte rows in the ray-major layout of the reference's hit_point_buffer
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float4* wh = s_hits + warp * 32 * kMaxDepth;
-    uint32_t* wi = s_ids + warp * 32 * kMaxDepth;
+    float4* wh = sm.hits + warp * 32 * kMaxDepth;
+    uint32_t* wi = sm.ids + warp * 32 * kMaxDepth;
     float4* slot = wh + lane * kMaxDepth;
     uint32_t* id = wi + lane * kMaxDepth;
-#pragma unroll
-    for (int s = 0; s < kMaxDepth; ++s) {
-        slot[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-        id[s] = kNoElement;
-    }
-    if (k < A.count) trace_ray(A, A.ray_begin + k, s_sun, slot, id);
-    __syncwarp();
-    const uint64_t warp_first = (uint64_t)blockIdx.x * kTraceBlock + (uint64_t)warp * 32;
-    if (warp_first >= A.count) return;
-    const uint64_t n_rec = min((uint64_t)32, A.count - warp_first) * kMaxDepth;
-    float4* gh = A.hits + warp_first * kMaxDepth;
-#pragma unroll
-    for (int s = 0; s < kMaxDepth; ++s) {
-        const uint32_t e = (uint32_t)(s * 32 + lane);
-        if (e < n_rec) __stcs(gh + e, wh[e]);
-    }
-    if (A.ids) {
-        uint32_t* gi = A.ids + warp_first * kMaxDepth;
+    const uint64_t tiles = (A.count + kTraceBlock - 1) / kTraceBlock;
+
+    for (uint64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        // ---- phase A: generation and first hit, one ray per thread
+        const uint64_t k = tile * kTraceBlock + threadIdx.x;
+        const uint64_t ray = A.ray_begin + k;
 #pragma unroll
         for (int s = 0; s < kMaxDepth; ++s) {
-            const uint32_t e = (uint32_t)(s * 32 + lane);
-            if (e < n_rec) __stcs(gi + e, wi[e]);
+            slot[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+            id[s] = kNoElement;
         }
+        bool pending = false;
+        Pending q;
+        if (k < A.count) {
+            const Segment g = generate(A, sm.sun, ray, sm.t6);
+            slot[0] = make_float4(0.0f, g.o.x, g.o.y, g.o.z);
+            Record r;
+            pending = find_hit(A, g, r, q);
+            if (r.slot >= 0) {
+                slot[r.slot] = r.rec;
+                id[r.slot] = r.id;
+            }
+        }
+        __syncwarp();
+        push(sm, pending, ray, q);
+        // the warp's 32 x 80 B of records leave as 5 fully coalesced 512-byte rows (stride 80 B per
+        // lane in shared memory: the 16-byte stores of each quarter warp hit distinct banks)
+        const uint64_t warp_first = tile * kTraceBlock + (uint64_t)warp * 32;
+        if (warp_first < A.count) {
+            const uint64_t n_rec = min((uint64_t)32, A.count - warp_first) * kMaxDepth;
+            float4* gh = A.hits + warp_first * kMaxDepth;
+#pragma unroll
+            for (int s = 0; s < kMaxDepth; ++s) {
+                const uint32_t e = (uint32_t)(s * 32 + lane);
+                if (e < n_rec) gh[e] = wh[e];
+            }
+            if (A.ids) {
+                uint32_t* gi = A.ids + warp_first * kMaxDepth;
+#pragma unroll
+                for (int s = 0; s < kMaxDepth; ++s) {
+                    const uint32_t e = (uint32_t)(s * 32 + lane);
+                    if (e < n_rec) gi[e] = wi[e];
+                }
+            }
+        }
+        // ---- phase B on full batches
+        drain(A, sm, false);
     }
+    drain(A, sm, true);
 }
 
 }  // namespace
@@ -465,9 +626,21 @@ cudaError_t launch_prepare_sun(const Aabb* aabbs, int n, float sx, float sy, flo
 
 cudaError_t launch_trace(const TraceArgs& args, cudaStream_t stream) {
     if (args.count == 0) return cudaSuccess;
-    const uint64_t blocks = (args.count + kTraceBlock - 1) / kTraceBlock;
-    if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
-    trace_kernel<<<(unsigned)blocks, kTraceBlock, 0, stream>>>(args);
+    // persistent grid: every resident CTA slot of the device, never more CTAs than tiles
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    static bool attr_set = false;  // per process; the attribute is per function, not per device
+    if (e == cudaSuccess && !attr_set) {
+        e = cudaFuncSetAttribute(trace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TraceSmem));
+        attr_set = (e == cudaSuccess);
+    }
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel, kTraceBlock, sizeof(TraceSmem));
+    if (e != cudaSuccess) return e;
+    const uint64_t tiles = (args.count + kTraceBlock - 1) / kTraceBlock;
+    const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)std::max(1, sms * std::max(1, per_sm)));
+    trace_kernel<<<(unsigned)grid, kTraceBlock, sizeof(TraceSmem), stream>>>(args);
     return cudaGetLastError();
 }
 

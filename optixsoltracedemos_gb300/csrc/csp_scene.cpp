@@ -23,7 +23,7 @@ inline float3 tof3(const D3& v) { return make_float3((float)v.x, (float)v.y, (fl
 // (yaw = atan2(nx, nz), pitch = asin(ny), roll = zrot in radians) and lib/math_util.h:41-59
 // (global-to-local matrix, Spencer & Murty).  Returns G2L row-major; the local x, y, z axes in
 // world space are its rows (the columns of L2G = G2L^T, lib/vector3d.h:151-159).
-void global_to_local(const csp_element& e, double G[9]) {
+void global_to_local(const csp_element& e, double G[9], double* euler = nullptr) {
     double n[3] = {e.aim_point[0] - e.origin[0], e.aim_point[1] - e.origin[1], e.aim_point[2] - e.origin[2]};
     const double len = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
     if (len > 0) {
@@ -36,6 +36,11 @@ void global_to_local(const csp_element& e, double G[9]) {
     const double alpha = std::atan2(n[0], n[2]);
     const double beta = std::asin(n[1]);
     const double gamma = e.zrot_deg * M_PI / 180.0;
+    if (euler) {
+        euler[0] = alpha;
+        euler[1] = beta;
+        euler[2] = gamma;
+    }
     const double ca = std::cos(alpha), sa = std::sin(alpha);
     const double cb = std::cos(beta), sb = std::sin(beta);
     const double cg = std::cos(gamma), sg = std::sin(gamma);
@@ -84,6 +89,35 @@ Aabb outward(const double lo[3], const double hi[3]) {
 }
 
 }  // namespace
+
+void element_frame(const csp_element& e, double euler[3], double G[9], double lo[3], double hi[3]) {
+    global_to_local(e, G, euler);
+    const double w = e.width, h = e.height;
+    if (e.surface != CSP_SURFACE_CYLINDER) {
+        const double c[4][3] = {{-w / 2, -h / 2, 0.0}, {w / 2, -h / 2, 0.0}, {w / 2, h / 2, 0.0}, {-w / 2, h / 2, 0.0}};
+        D3 g[4];
+        for (int k = 0; k < 4; ++k) g[k] = to_world(G, c[k], e.origin);
+        lo[0] = std::fmin(std::fmin(g[0].x, g[1].x), std::fmin(g[2].x, g[3].x));
+        lo[1] = std::fmin(std::fmin(g[0].y, g[1].y), std::fmin(g[2].y, g[3].y));
+        lo[2] = std::fmin(std::fmin(g[0].z, g[1].z), std::fmin(g[2].z, g[3].z));
+        hi[0] = std::fmax(std::fmax(g[0].x, g[1].x), std::fmax(g[2].x, g[3].x));
+        hi[1] = std::fmax(std::fmax(g[0].y, g[1].y), std::fmax(g[2].y, g[3].y));
+        hi[2] = std::fmax(std::fmax(g[0].z, g[1].z), std::fmax(g[2].z, g[3].z));
+    } else {
+        lo[0] = lo[1] = lo[2] = DBL_MAX;
+        hi[0] = hi[1] = hi[2] = -DBL_MAX;
+        for (int k = 0; k < 8; ++k) {
+            const double c[3] = {(k & 1) ? w / 2 : -w / 2, (k & 2) ? h / 2 : -h / 2, (k & 4) ? w / 2 : -w / 2};
+            const D3 g = to_world(G, c, e.origin);
+            lo[0] = std::fmin(lo[0], g.x);
+            lo[1] = std::fmin(lo[1], g.y);
+            lo[2] = std::fmin(lo[2], g.z);
+            hi[0] = std::fmax(hi[0], g.x);
+            hi[1] = std::fmax(hi[1], g.y);
+            hi[2] = std::fmax(hi[2], g.z);
+        }
+    }
+}
 
 void sun_vector_f(const double d[3], float out[3]) {
     const double len = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
@@ -139,36 +173,9 @@ int build_elements(const csp_element* el, uint32_t n, HostScene& s, std::string&
         }
         s.types[i] = type;
 
-        double G[9];
-        global_to_local(e, G);
+        double G[9], euler[3], lo[3], hi[3];
+        element_frame(e, euler, G, lo, hi);
         const double w = e.width, h = e.height;
-
-        // exact AABB: lib/element.cpp:172-275
-        double lo[3], hi[3];
-        if (e.surface != CSP_SURFACE_CYLINDER) {
-            const double c[4][3] = {{-w / 2, -h / 2, 0.0}, {w / 2, -h / 2, 0.0}, {w / 2, h / 2, 0.0}, {-w / 2, h / 2, 0.0}};
-            D3 g[4];
-            for (int k = 0; k < 4; ++k) g[k] = to_world(G, c[k], e.origin);
-            lo[0] = std::fmin(std::fmin(g[0].x, g[1].x), std::fmin(g[2].x, g[3].x));
-            lo[1] = std::fmin(std::fmin(g[0].y, g[1].y), std::fmin(g[2].y, g[3].y));
-            lo[2] = std::fmin(std::fmin(g[0].z, g[1].z), std::fmin(g[2].z, g[3].z));
-            hi[0] = std::fmax(std::fmax(g[0].x, g[1].x), std::fmax(g[2].x, g[3].x));
-            hi[1] = std::fmax(std::fmax(g[0].y, g[1].y), std::fmax(g[2].y, g[3].y));
-            hi[2] = std::fmax(std::fmax(g[0].z, g[1].z), std::fmax(g[2].z, g[3].z));
-        } else {
-            lo[0] = lo[1] = lo[2] = DBL_MAX;
-            hi[0] = hi[1] = hi[2] = -DBL_MAX;
-            for (int k = 0; k < 8; ++k) {
-                const double c[3] = {(k & 1) ? w / 2 : -w / 2, (k & 2) ? h / 2 : -h / 2, (k & 4) ? w / 2 : -w / 2};
-                const D3 g = to_world(G, c, e.origin);
-                lo[0] = std::fmin(lo[0], g.x);
-                lo[1] = std::fmin(lo[1], g.y);
-                lo[2] = std::fmin(lo[2], g.z);
-                hi[0] = std::fmax(hi[0], g.x);
-                hi[1] = std::fmax(hi[1], g.y);
-                hi[2] = std::fmax(hi[2], g.z);
-            }
-        }
         Aabb& box = s.aabbs[i];
         box.lo = make_float4((float)lo[0], (float)lo[1], (float)lo[2], 0.f);
         box.hi = make_float4((float)hi[0], (float)hi[1], (float)hi[2], 0.f);

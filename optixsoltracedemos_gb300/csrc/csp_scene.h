@@ -36,6 +36,10 @@ void build_bvh(HostScene& s);
 // are stored after their parents, so one reverse sweep is a bottom-up refit).
 void refit_bvh(HostScene& s);
 
+// Euler angles (yaw, pitch, roll in radians), global-to-local matrix (row-major; rows = local x,
+// y, z axes in world space) and exact double AABB of one element.
+void element_frame(const csp_element& e, double euler[3], double G[9], double lo[3], double hi[3]);
+
 // normalized sun vector in double, cast to float (SolTraceSystem::initialize,
 // lib/soltrace_system.cpp:81-85)
 void sun_vector_f(const double d[3], float out[3]);

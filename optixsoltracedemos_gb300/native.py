@@ -60,6 +60,7 @@ SIGNATURES = {
     "csp_read_stinput": (ctypes.c_int, [_H, ctypes.c_char_p, ctypes.c_int]),
     "csp_write_hits_csv": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.c_char_p]),
     "csp_write_output": (ctypes.c_int, [_H, ctypes.c_char_p]),
+    "csp_element_frame": (ctypes.c_int, [_P, _P, _P, _P, _P]),
 }
 STINPUT_APPLY_OPTICS = 1
 

@@ -124,6 +124,25 @@ def single_parabolic(sun_sigma=2.5e-3, slope_error=1.5e-3, num_rays=1 << 24, sun
     return Scene("single_parabolic", e, sun, sun_shape, sun_sigma, num_rays, {"focal_length": f})
 
 
+def corridor(num_rays=1 << 20, sun=(0.8, 0.0, 1.0), sun_angle=4.65e-3, slope_error=0.0) -> Scene:
+    """Two tall flat mirrors facing each other (x = -2 and x = +2, 20 m along z, 4 m along y) above
+    a flat 4 x 4 m receiver facing up at z = -10.5: rays entering between the mirrors bounce back and
+    forth several times, so paths reach the five-slot limit of the hit record."""
+    e = make_elements(3)
+    e["origin"][0] = [-2.0, 0.0, 0.0]
+    e["aim_point"][0] = [1.0, 0.0, 0.0]
+    e["origin"][1] = [2.0, 0.0, 0.0]
+    e["aim_point"][1] = [-1.0, 0.0, 0.0]
+    e["width"][:2] = 20.0
+    e["height"][:2] = 4.0
+    e["slope_error"][:2] = slope_error
+    e["origin"][2] = [0.0, 0.0, -10.5]
+    e["aim_point"][2] = [0.0, 0.0, 0.0]
+    e["width"][2] = 4.0
+    e["height"][2] = 4.0
+    return Scene("corridor", e, np.asarray(sun, np.float64), SUN_PILLBOX, sun_angle, num_rays)
+
+
 def radial_stagger(n=10000, r_min=100.0, r_max=800.0, mirror=10.0, seed=1) -> np.ndarray:
     """Heliostat base positions (z = 0) on a radial-stagger layout, truncated in ring order."""
     pitch = 1.2 * mirror * math.sqrt(2.0)

@@ -41,6 +41,7 @@ def _configs():
         "single_parabolic_pillbox_spec": scenes.single_parabolic(sun_shape=0, sun_sigma=4.65e-3),
         "field_300": scenes.large_field(n_heliostats=300, sun=scenes.sun_vector(40.0, 30.0)),
         "field_2000_parabolic": scenes.large_field(n_heliostats=2000, parabolic=True, sun=scenes.sun_vector(60.0, -45.0)),
+        "corridor_multibounce": scenes.corridor(slope_error=1e-3),
     }
 
 
