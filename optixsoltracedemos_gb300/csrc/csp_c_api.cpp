@@ -195,7 +195,7 @@ int System::trace_async(cudaStream_t st) {
     if (!initialized) return fail(CSP_ERR_STATE, "trace before initialize()");
     int rc = ensure_hit_buffers();
     if (rc) return rc;
-    return cuda_status(launch_trace(args(0, num_rays), st ? st : stream), "trace_kernel");
+    return cuda_status(launch_trace(args(0, num_rays), (int)scene.prims.size(), st ? st : stream), "trace_kernel");
 }
 
 int System::run() {
@@ -203,7 +203,7 @@ int System::run() {
     int rc = ensure_hit_buffers();
     if (rc) return rc;
     if ((rc = cuda_status(cudaEventRecord(ev0, stream), "cudaEventRecord"))) return rc;
-    if ((rc = cuda_status(launch_trace(args(0, num_rays), stream), "trace_kernel"))) return rc;
+    if ((rc = cuda_status(launch_trace(args(0, num_rays), (int)scene.prims.size(), stream), "trace_kernel"))) return rc;
     if ((rc = cuda_status(cudaEventRecord(ev1, stream), "cudaEventRecord"))) return rc;
     if ((rc = cuda_status(cudaEventSynchronize(ev1), "trace"))) return rc;
     float ms = 0.f;
@@ -221,7 +221,7 @@ int System::run_to_host(float* dst, uint32_t* ids_dst) {
     const auto t0 = std::chrono::steady_clock::now();
     for (uint64_t b = 0; b < num_rays; b += chunk) {
         const uint64_t c = std::min(chunk, num_rays - b);
-        if ((rc = cuda_status(launch_trace(args(b, c), stream), "trace_kernel"))) break;
+        if ((rc = cuda_status(launch_trace(args(b, c), (int)scene.prims.size(), stream), "trace_kernel"))) break;
         cudaEvent_t ev;
         if ((rc = cuda_status(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate"))) break;
         done.push_back(ev);

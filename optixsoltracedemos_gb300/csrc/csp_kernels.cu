@@ -344,15 +344,20 @@ __device__ __forceinline__ int traverse(const Node* __restrict__ nodes, const Pr
 
 // ------------------------------------------------------------------------------ trace ---------
 // Persistent kernel, wavefront inside each CTA.  A CTA walks tiles of kTraceBlock consecutive rays.
-//   phase A (one ray per thread): sun sample, closest hit of the first segment, its record.  A ray
-//     that hits a mirror is pushed, unshaded, into a shared-memory queue (warp ballot + one shared
-//     atomic per warp).
-//   phase B (only on full batches of kTraceBlock queued rays, and on the remainder at the end):
-//     shade the queued mirror hit (normal, slope/specularity error, reflection, absorption), then
-//     find and record the next hit; mirror hits go back into the queue.
-// In the heliostat workloads ~10% of rays reach a mirror; shading and tracing them on full warps
-// instead of inside warps where ~90% of lanes have already finished is the point of the queue.
+//   phase A (one ray per thread, every ray): sun sample and the cheap, branch-free part of the first
+//     segment; the warp's records (sun point + empty slots) leave as coalesced rows.  Rays with
+//     more to do are pushed into a shared-memory queue (warp ballot + one shared atomic per warp):
+//       small scenes (kFlat, <= kFlatMax elements, all in shared memory): phase A only runs the AABB
+//         slab tests; rays whose segment overlaps some element box are queued with that mask;
+//       BVH scenes: phase A traverses and records the first hit; mirror hits are queued unshaded.
+//   phase B (only on full batches of kTraceBlock queued rays, and on the remainder at the end): the
+//     rest of each queued path -- intersection programs, shading, further segments -- with records
+//     written straight to global memory (their rows were written by phase A of an earlier tile of
+//     this CTA, ordered by the barriers in between).
+// In the heliostat workloads ~10% of rays meet an element; running their intersection programs and
+// shading on full warps instead of inside warps where ~90% of lanes have finished is the point.
 constexpr int kQueueCap = 2 * kTraceBlock;
+constexpr int kFlatMax = 8;
 
 struct Segment {
     float3 o, d;
@@ -360,59 +365,75 @@ struct Segment {
     int depth;
 };
 
-struct Record {
-    float4 rec;
-    uint32_t id;
-    int slot;
+// Scene copy in shared memory for kFlat launches.
+struct FlatScene {
+    Prim prim[kFlatMax];
+    Aabb box[kFlatMax];
+    Optics optics[kFlatMax];
+    uint32_t type[kFlatMax];
+    int n;
 };
 
-// A mirror hit waiting for its closest-hit program: the incoming segment, hit distance, element,
-// entity type and the depth of the hit (its record slot).
-struct Pending {
-    float3 o, d;
+// AABB culling of the intersection programs (segment [tmin, kTmax] against each element box) for a
+// kFlat scene: bit k set when element k's program has to run.
+__device__ __forceinline__ uint32_t candidates(const FlatScene& fs, float3 o, float3 d, float tmin) {
+    const float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    uint32_t mask = 0;
+    for (int k = 0; k < fs.n; ++k) {
+        const float4 lo = fs.box[k].lo, hi = fs.box[k].hi;
+        const float t0x = (lo.x - o.x) * inv.x, t1x = (hi.x - o.x) * inv.x;
+        const float t0y = (lo.y - o.y) * inv.y, t1y = (hi.y - o.y) * inv.y;
+        const float t0z = (lo.z - o.z) * inv.z, t1z = (hi.z - o.z) * inv.z;
+        const float tn = fmaxf(tmin, fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z)));
+        const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+        if (tn <= fminf(kTmax, tf)) mask |= 1u << k;
+    }
+    return mask;
+}
+
+// Closest hit among the candidate elements, in ascending index (equal t keeps the lower index).
+__device__ __forceinline__ int closest_in(const FlatScene& fs, uint32_t mask, float3 o, float3 d, float tmin,
+                                          float& best_t, uint32_t& best_type) {
+    int best = -1;
+    best_t = __int_as_float(0x7f800000);
+    while (mask) {
+        const int k = __ffs(mask) - 1;
+        mask &= mask - 1u;
+        float t;
+        if (hit_prim(fs.type[k], fs.prim[k], o, d, tmin, t) && t < best_t) {
+            best = k;
+            best_t = t;
+            best_type = fs.type[k];
+        }
+    }
+    return best;
+}
+
+struct Hit {
+    int best;  // element index, -1 on a miss
     float t;
-    uint32_t prim;
     uint32_t type;
-    int depth;
 };
 
-// optixTrace of one segment up to the choice of closest-hit program: closest hit, its record, and
-// for a mirror the pending shading.  Returns true when a mirror hit is pending.
-__device__ __forceinline__ bool find_hit(const TraceArgs& A, const Segment& g, Record& out, Pending& pend) {
-    out.slot = -1;
-    float t;
-    uint32_t type = 0;
-    const int best = traverse(A.nodes, A.prims, g.o, g.d, g.tmin, t, type);
-    if (best < 0) return false;  // __miss__ms, cuda/materials.cu:236-253
+// What the closest-hit program of a hit records: slot depth+1 (mirrors and the cylinder always,
+// below max depth; the flat receiver only from the front, cuda/materials.cu:86-163), and whether a
+// mirror has to be shaded next (cuda/materials.cu:44-60,180-197: only below max depth).
+__device__ __forceinline__ bool classify(const Prim& p, const Segment& g, const Hit& h, float4& rec, int& slot) {
+    slot = -1;
     const int nd = g.depth + 1;
-    if (type == kFlatMirror || type == kParabolicMirror) {
-        // cuda/materials.cu:44-60,180-197: the record is written, and traced on, only below max depth
-        if (nd >= kMaxDepth) return false;
-        const float3 hit = add(g.o, scale(t, g.d));
-        out.rec = make_float4(1.0f, hit.x, hit.y, hit.z);
-        out.id = (uint32_t)best;
-        out.slot = nd;
-        pend = Pending{g.o, g.d, t, (uint32_t)best, type, nd};
+    if (nd >= kMaxDepth) return false;
+    const float3 hit = add(g.o, scale(h.t, g.d));
+    if (h.type == kFlatMirror || h.type == kParabolicMirror) {
+        rec = make_float4(1.0f, hit.x, hit.y, hit.z);
+        slot = nd;
         return true;
     }
-    const float3 hit = add(g.o, scale(t, g.d));
-    if (type == kFlatReceiver) {
-        // __closesthit__receiver, cuda/materials.cu:86-121: front face only
-        const Prim p = load_prim(A.prims, (uint32_t)best);
+    if (h.type == kFlatReceiver) {
         const float3 rn = cross(xyz(p.c), xyz(p.d));
-        if (dot(g.d, rn) < 0.0f && nd < kMaxDepth) {
-            out.rec = make_float4(2.0f, hit.x, hit.y, hit.z);
-            out.id = (uint32_t)best;
-            out.slot = nd;
-        }
-        return false;
+        if (!(dot(g.d, rn) < 0.0f)) return false;
     }
-    // __closesthit__receiver__cylinder__y, cuda/materials.cu:123-163
-    if (nd < kMaxDepth) {
-        out.rec = make_float4(2.0f, hit.x, hit.y, hit.z);
-        out.id = (uint32_t)best;
-        out.slot = nd;
-    }
+    rec = make_float4(2.0f, hit.x, hit.y, hit.z);
+    slot = nd;
     return false;
 }
 
@@ -420,29 +441,29 @@ __device__ __forceinline__ bool find_hit(const TraceArgs& A, const Segment& g, R
 // as the intersection program reports it, faced against the ray, ideal reflection; plus the
 // extensions (Gaussian slope and specularity error, absorption with probability 1 - reflectivity).
 // Returns false when the ray is absorbed.
-__device__ __forceinline__ bool shade_mirror(const TraceArgs& A, uint64_t ray, const Pending& q, Segment& next) {
-    const Prim p = load_prim(A.prims, q.prim);
-    const float3 hit = add(q.o, scale(q.t, q.d));
-    const float3 wn = (q.type == kFlatMirror) ? normalize(xyz(p.a)) : normalize(parab_normal(p, q.o, q.d, q.t));
-    float3 ffn = (dot(neg(q.d), wn) >= 0.0f) ? wn : neg(wn);
-    const Optics op = A.optics[q.prim];
+__device__ __forceinline__ bool shade_mirror(const TraceArgs& A, uint64_t ray, const Prim& p, const Optics& op,
+                                             const Segment& g, const Hit& h, Segment& next) {
+    const int nd = g.depth + 1;
+    const float3 hit = add(g.o, scale(h.t, g.d));
+    const float3 wn = (h.type == kFlatMirror) ? normalize(xyz(p.a)) : normalize(parab_normal(p, g.o, g.d, h.t));
+    float3 ffn = (dot(neg(g.d), wn) >= 0.0f) ? wn : neg(wn);
     const bool need_rng = (op.slope > 0.0f) || (op.spec > 0.0f) || !(op.reflectivity >= 1.0f);
     u32x4 ra = {0u, 0u, 0u, 0u};
-    if (need_rng) ra = draw_block(ray, (uint32_t)q.depth, 0, A.instance, A.seed);
+    if (need_rng) ra = draw_block(ray, (uint32_t)nd, 0, A.instance, A.seed);
     if (op.slope > 0.0f) {
         float g1, g2;
         box_muller(u01(ra.y), u01(ra.z), g1, g2);
         ffn = perturb(ffn, op.slope, g1, g2);
     }
-    float3 rd = reflect(q.d, ffn);
+    float3 rd = reflect(g.d, ffn);
     if (op.spec > 0.0f) {
-        const u32x4 rb = draw_block(ray, (uint32_t)q.depth, 1, A.instance, A.seed);
+        const u32x4 rb = draw_block(ray, (uint32_t)nd, 1, A.instance, A.seed);
         float g1, g2;
         box_muller(u01(rb.x), u01(rb.y), g1, g2);
         rd = perturb(normalize(rd), op.spec, g1, g2);
     }
     if (need_rng && u01(ra.x) > op.reflectivity) return false;  // absorbed at the mirror
-    next = Segment{hit, rd, kTminBounce, q.depth};
+    next = Segment{hit, rd, kTminBounce, nd};
     return true;
 }
 
@@ -474,16 +495,16 @@ struct TraceSmem {
     float4 hits[kTraceBlock * kMaxDepth];  // phase A record staging, ray-major per warp
     uint32_t ids[kTraceBlock * kMaxDepth];
     float qo[3][kQueueCap], qd[3][kQueueCap], qt[kQueueCap];
-    uint32_t qprim[kQueueCap];
-    uint32_t qmeta[kQueueCap];  // type << 8 | depth
+    uint32_t qw[kQueueCap];  // kFlat: candidate mask; BVH: element | type << 28 of the pending mirror hit
     uint64_t qray[kQueueCap];
     float t6[kH3Tab];
+    FlatScene flat;
     SunFrame sun;
     int qsize;
 };
 
 // warp-aggregated append of the lanes with `want` set; every lane of the warp must call it
-__device__ __forceinline__ void push(TraceSmem& sm, bool want, uint64_t ray, const Pending& q) {
+__device__ __forceinline__ void push(TraceSmem& sm, bool want, uint64_t ray, float3 o, float3 d, float t, uint32_t w) {
     const unsigned mask = __ballot_sync(0xffffffffu, want);
     if (mask == 0u) return;
     const int lane = threadIdx.x & 31;
@@ -492,22 +513,50 @@ __device__ __forceinline__ void push(TraceSmem& sm, bool want, uint64_t ray, con
     base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
     if (want) {
         const int k = base + __popc(mask & ((1u << lane) - 1u));
-        sm.qo[0][k] = q.o.x;
-        sm.qo[1][k] = q.o.y;
-        sm.qo[2][k] = q.o.z;
-        sm.qd[0][k] = q.d.x;
-        sm.qd[1][k] = q.d.y;
-        sm.qd[2][k] = q.d.z;
-        sm.qt[k] = q.t;
-        sm.qprim[k] = q.prim;
-        sm.qmeta[k] = (q.type << 8) | (uint32_t)q.depth;
+        sm.qo[0][k] = o.x;
+        sm.qo[1][k] = o.y;
+        sm.qo[2][k] = o.z;
+        sm.qd[0][k] = d.x;
+        sm.qd[1][k] = d.y;
+        sm.qd[2][k] = d.z;
+        sm.qt[k] = t;
+        sm.qw[k] = w;
         sm.qray[k] = ray;
     }
 }
 
-// Phase B: pop up to kTraceBlock queued mirror hits, shade them, find and record the next hit
-// (records go straight to global memory: their rows were written by phase A of an earlier tile of
-// this CTA, ordered by the barriers in between), push new mirror hits back.
+__device__ __forceinline__ void store_record(const TraceArgs& A, uint64_t ray, int slot, float4 rec, uint32_t id) {
+    const uint64_t row = (ray - A.ray_begin) * kMaxDepth + (uint64_t)slot;
+    A.hits[row] = rec;
+    if (A.ids) A.ids[row] = id;
+}
+
+// Remainder of a path in phase B, from the closest hit `h` of segment `g`: record, shade, next
+// segment, until the ray misses, is absorbed, ends on the receiver or reaches the depth limit.
+template <bool kFlat>
+__device__ void finish_path(const TraceArgs& A, const TraceSmem& sm, uint64_t ray, Segment g, Hit h) {
+    for (;;) {
+        if (h.best < 0) return;  // __miss__ms, cuda/materials.cu:236-253
+        const Prim p = kFlat ? sm.flat.prim[h.best] : load_prim(A.prims, (uint32_t)h.best);
+        float4 rec;
+        int slot;
+        const bool mirror = classify(p, g, h, rec, slot);
+        if (slot >= 0) store_record(A, ray, slot, rec, (uint32_t)h.best);
+        if (!mirror) return;
+        const Optics op = kFlat ? sm.flat.optics[h.best] : A.optics[h.best];
+        Segment next;
+        if (!shade_mirror(A, ray, p, op, g, h, next)) return;
+        g = next;
+        if (kFlat) {
+            const uint32_t m = candidates(sm.flat, g.o, g.d, g.tmin);
+            h.best = closest_in(sm.flat, m, g.o, g.d, g.tmin, h.t, h.type);
+        } else {
+            h.best = traverse(A.nodes, A.prims, g.o, g.d, g.tmin, h.t, h.type);
+        }
+    }
+}
+
+template <bool kFlat>
 __device__ void drain(const TraceArgs& A, TraceSmem& sm, bool all) {
     __syncthreads();
     int qs = sm.qsize;
@@ -515,48 +564,67 @@ __device__ void drain(const TraceArgs& A, TraceSmem& sm, bool all) {
         const int n = min(qs, kTraceBlock);
         const int base = qs - n;
         const bool have = (int)threadIdx.x < n;
-        Pending q;
+        float3 o = f3(0.f, 0.f, 0.f), d = f3(0.f, 0.f, 1.f);
+        float t = 0.f;
+        uint32_t w = 0;
         uint64_t ray = 0;
         if (have) {
             const int k = base + threadIdx.x;
-            q.o = f3(sm.qo[0][k], sm.qo[1][k], sm.qo[2][k]);
-            q.d = f3(sm.qd[0][k], sm.qd[1][k], sm.qd[2][k]);
-            q.t = sm.qt[k];
-            q.prim = sm.qprim[k];
-            q.type = sm.qmeta[k] >> 8;
-            q.depth = (int)(sm.qmeta[k] & 0xffu);
+            o = f3(sm.qo[0][k], sm.qo[1][k], sm.qo[2][k]);
+            d = f3(sm.qd[0][k], sm.qd[1][k], sm.qd[2][k]);
+            t = sm.qt[k];
+            w = sm.qw[k];
             ray = sm.qray[k];
         }
         __syncthreads();
         if (threadIdx.x == 0) sm.qsize = base;
         __syncthreads();
-        bool again = false;
-        Pending nq;
         if (have) {
-            Segment g;
-            if (shade_mirror(A, ray, q, g)) {
-                Record r;
-                again = find_hit(A, g, r, nq);
-                if (r.slot >= 0) {
-                    const uint64_t row = (ray - A.ray_begin) * kMaxDepth + (uint64_t)r.slot;
-                    A.hits[row] = r.rec;
-                    if (A.ids) A.ids[row] = r.id;
+            if (kFlat) {
+                // first segment from the sun: intersection programs of the candidate elements
+                const Segment g{o, d, kTminSun, 0};
+                Hit h;
+                h.best = closest_in(sm.flat, w, o, d, kTminSun, h.t, h.type);
+                finish_path<kFlat>(A, sm, ray, g, h);
+            } else {
+                // pending mirror hit of the first segment: its record was written in phase A
+                const Segment g{o, d, kTminSun, 0};
+                const Hit h{(int)(w & kPrimMask), t, w >> kTypeShift};
+                const Prim p = load_prim(A.prims, (uint32_t)h.best);
+                Segment next;
+                if (shade_mirror(A, ray, p, A.optics[h.best], g, h, next)) {
+                    Hit h2;
+                    h2.best = traverse(A.nodes, A.prims, next.o, next.d, next.tmin, h2.t, h2.type);
+                    finish_path<kFlat>(A, sm, ray, next, h2);
                 }
             }
         }
-        __syncwarp();
-        push(sm, again, ray, nq);
         __syncthreads();
         qs = sm.qsize;
     }
 }
 
+template <bool kFlat>
 __global__ void __launch_bounds__(kTraceBlock, 3) trace_kernel(const TraceArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TraceSmem& sm = *reinterpret_cast<TraceSmem*>(smem_raw);
     if (threadIdx.x < sizeof(SunFrame) / 4)
         reinterpret_cast<uint32_t*>(&sm.sun)[threadIdx.x] = reinterpret_cast<const uint32_t*>(A.sun)[threadIdx.x];
     for (uint32_t m = threadIdx.x; m < kH3Tab; m += kTraceBlock) sm.t6[m] = halton3(m);
+    if (kFlat && threadIdx.x < kFlatMax) {
+        const int nprim = A.sun->n_prims;
+        const int k = threadIdx.x;
+        if (k < nprim) {
+            // a kFlat scene's nodes are its leaves in element order
+            const Node nd = A.nodes[k];
+            sm.flat.prim[k] = A.prims[k];
+            sm.flat.optics[k] = A.optics[k];
+            sm.flat.box[k].lo = nd.lo;
+            sm.flat.box[k].hi = nd.hi;
+            sm.flat.type[k] = (__float_as_uint(nd.lo.w) >> kTypeShift) & 7u;
+        }
+        if (k == 0) sm.flat.n = min(nprim, kFlatMax);
+    }
     if (threadIdx.x == 0) sm.qsize = 0;
     __syncthreads();
 
@@ -568,28 +636,44 @@ __global__ void __launch_bounds__(kTraceBlock, 3) trace_kernel(const TraceArgs A
     const uint64_t tiles = (A.count + kTraceBlock - 1) / kTraceBlock;
 
     for (uint64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        // ---- phase A: generation and first hit, one ray per thread
+        // ---- phase A
         const uint64_t k = tile * kTraceBlock + threadIdx.x;
         const uint64_t ray = A.ray_begin + k;
 #pragma unroll
-        for (int s = 0; s < kMaxDepth; ++s) {
-            slot[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-            id[s] = kNoElement;
+        for (int s = 0; s < kMaxDepth; ++s) slot[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (A.ids) {
+#pragma unroll
+            for (int s = 0; s < kMaxDepth; ++s) id[s] = kNoElement;
         }
-        bool pending = false;
-        Pending q;
+        bool want = false;
+        Segment g;
+        float qt = 0.f;
+        uint32_t qw = 0;
         if (k < A.count) {
-            const Segment g = generate(A, sm.sun, ray, sm.t6);
+            g = generate(A, sm.sun, ray, sm.t6);
             slot[0] = make_float4(0.0f, g.o.x, g.o.y, g.o.z);
-            Record r;
-            pending = find_hit(A, g, r, q);
-            if (r.slot >= 0) {
-                slot[r.slot] = r.rec;
-                id[r.slot] = r.id;
+            if (kFlat) {
+                qw = candidates(sm.flat, g.o, g.d, g.tmin);
+                want = qw != 0u;
+            } else {
+                Hit h;
+                h.best = traverse(A.nodes, A.prims, g.o, g.d, g.tmin, h.t, h.type);
+                if (h.best >= 0) {
+                    const Prim p = load_prim(A.prims, (uint32_t)h.best);
+                    float4 rec;
+                    int s;
+                    want = classify(p, g, h, rec, s);
+                    if (s >= 0) {
+                        slot[s] = rec;
+                        if (A.ids) id[s] = (uint32_t)h.best;
+                    }
+                    qt = h.t;
+                    qw = (uint32_t)h.best | (h.type << kTypeShift);
+                }
             }
         }
         __syncwarp();
-        push(sm, pending, ray, q);
+        push(sm, want, ray, g.o, g.d, qt, qw);
         // the warp's 32 x 80 B of records leave as 5 fully coalesced 512-byte rows (stride 80 B per
         // lane in shared memory: the 16-byte stores of each quarter warp hit distinct banks)
         const uint64_t warp_first = tile * kTraceBlock + (uint64_t)warp * 32;
@@ -611,9 +695,31 @@ __global__ void __launch_bounds__(kTraceBlock, 3) trace_kernel(const TraceArgs A
             }
         }
         // ---- phase B on full batches
-        drain(A, sm, false);
+        drain<kFlat>(A, sm, false);
     }
-    drain(A, sm, true);
+    drain<kFlat>(A, sm, true);
+}
+
+template <bool kFlat>
+cudaError_t launch_trace_t(const TraceArgs& args, int n_prims, cudaStream_t stream) {
+    (void)n_prims;
+    // persistent grid: every resident CTA slot of the device, never more CTAs than tiles
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    static bool attr_set = false;  // per process; the attribute belongs to the function
+    if (e == cudaSuccess && !attr_set) {
+        e = cudaFuncSetAttribute(trace_kernel<kFlat>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sizeof(TraceSmem));
+        attr_set = (e == cudaSuccess);
+    }
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel<kFlat>, kTraceBlock, sizeof(TraceSmem));
+    if (e != cudaSuccess) return e;
+    const uint64_t tiles = (args.count + kTraceBlock - 1) / kTraceBlock;
+    const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)std::max(1, sms * std::max(1, per_sm)));
+    trace_kernel<kFlat><<<(unsigned)grid, kTraceBlock, sizeof(TraceSmem), stream>>>(args);
+    return cudaGetLastError();
 }
 
 }  // namespace
@@ -624,24 +730,10 @@ cudaError_t launch_prepare_sun(const Aabb* aabbs, int n, float sx, float sy, flo
     return cudaGetLastError();
 }
 
-cudaError_t launch_trace(const TraceArgs& args, cudaStream_t stream) {
+cudaError_t launch_trace(const TraceArgs& args, int n_prims, cudaStream_t stream) {
     if (args.count == 0) return cudaSuccess;
-    // persistent grid: every resident CTA slot of the device, never more CTAs than tiles
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    static bool attr_set = false;  // per process; the attribute is per function, not per device
-    if (e == cudaSuccess && !attr_set) {
-        e = cudaFuncSetAttribute(trace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TraceSmem));
-        attr_set = (e == cudaSuccess);
-    }
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel, kTraceBlock, sizeof(TraceSmem));
-    if (e != cudaSuccess) return e;
-    const uint64_t tiles = (args.count + kTraceBlock - 1) / kTraceBlock;
-    const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)std::max(1, sms * std::max(1, per_sm)));
-    trace_kernel<<<(unsigned)grid, kTraceBlock, sizeof(TraceSmem), stream>>>(args);
-    return cudaGetLastError();
+    if (n_prims <= kFlatMax) return launch_trace_t<true>(args, n_prims, stream);
+    return launch_trace_t<false>(args, n_prims, stream);
 }
 
 }  // namespace csp

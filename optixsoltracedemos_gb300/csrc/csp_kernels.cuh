@@ -27,7 +27,8 @@ struct TraceArgs {
 cudaError_t launch_prepare_sun(const Aabb* aabbs, int n, float sx, float sy, float sz, float tan_pad, int shape,
                                float param, SunFrame* out, cudaStream_t stream);
 
-// One thread per ray: generation, traversal, shading and the dense hit-record write.
-cudaError_t launch_trace(const TraceArgs& args, cudaStream_t stream);
+// Trace rays [ray_begin, ray_begin + count): generation, closest-hit search, shading, the dense
+// hit-record write.  Scenes of up to 8 elements (n_prims) take the shared-memory element list path.
+cudaError_t launch_trace(const TraceArgs& args, int n_prims, cudaStream_t stream);
 
 }  // namespace csp

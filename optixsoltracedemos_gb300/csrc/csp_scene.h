@@ -29,7 +29,7 @@ int build_elements(const csp_element* el, uint32_t n, HostScene& s, std::string&
 
 // Build the stackless BVH over the pruning boxes (binned SAH, one element per leaf; scenes of up
 // to kFlatListMax elements get a plain list of leaves instead).
-constexpr uint32_t kFlatListMax = 8;
+constexpr uint32_t kFlatListMax = 8;  // = kFlatMax of the trace kernel
 void build_bvh(HostScene& s);
 
 // Recompute every node box of an existing topology from the current aabbs/prune boxes (children
