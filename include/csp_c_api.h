@@ -126,6 +126,11 @@ CSP_API int csp_copy_hits(csp_handle h, float* dst, uint32_t* ids, uint64_t firs
  * write_output), pipelining the copy of finished chunks behind the trace of later ones.  dst (and
  * ids when not NULL) should be page-locked for full speed. */
 CSP_API int csp_run_to_host(csp_handle h, float* dst, uint32_t* ids);
+/* Enqueue the trace of rays [first_ray, first_ray + count) on `stream` (NULL = the handle's own)
+ * into caller-provided buffers of count * 5 records: device memory, or page-locked host memory
+ * the device can address (the kernel then stores the records across the host link directly).
+ * ids may be NULL.  No host synchronisation; the handle's own hit buffer is not touched. */
+CSP_API int csp_trace_into(csp_handle h, void* hits, void* ids, uint64_t first_ray, uint64_t count, void* stream);
 /* Device pointers of the hit buffer ([num_rays*5] float4) and id buffer (NULL unless recorded). */
 CSP_API int csp_get_device_buffers(csp_handle h, void** hits, void** ids);
 

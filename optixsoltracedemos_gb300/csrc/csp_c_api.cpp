@@ -396,6 +396,20 @@ int csp_copy_hits(csp_handle h, float* dst, uint32_t* ids, uint64_t first, uint6
     return CSP_OK;
 }
 
+int csp_trace_into(csp_handle h, void* hits, void* ids, uint64_t first, uint64_t count, void* stream) {
+    CSP_GUARD(h);
+    System* s = reinterpret_cast<System*>(h);
+    if (!s->initialized) return fail(CSP_ERR_STATE, "trace before initialize()");
+    if (!hits && count) return fail(CSP_ERR_INVALID_ARGUMENT, "null hit buffer");
+    csp::TraceArgs a = s->args(0, 0);
+    a.hits = reinterpret_cast<float4*>(hits);
+    a.ids = reinterpret_cast<uint32_t*>(ids);
+    a.ray_begin = first;
+    a.count = count;
+    cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : s->stream;
+    return csp::cuda_status(csp::launch_trace(a, (int)s->scene.prims.size(), st), "trace_kernel");
+}
+
 int csp_run_to_host(csp_handle h, float* dst, uint32_t* ids) {
     CSP_GUARD(h);
     if (!dst) return fail(CSP_ERR_INVALID_ARGUMENT, "null destination");

@@ -20,7 +20,7 @@
 namespace csp {
 namespace {
 
-constexpr int kTraceBlock = 256;
+constexpr int kTraceBlock = 128;
 constexpr int kPrepBlock = 512;
 constexpr float kTwoPi = 2.0f * 3.14159265358979323846f;  // 2.0f * M_PIf, cuda/sun.cu:85
 
@@ -379,7 +379,10 @@ struct FlatScene {
 __device__ __forceinline__ uint32_t candidates(const FlatScene& fs, float3 o, float3 d, float tmin) {
     const float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
     uint32_t mask = 0;
-    for (int k = 0; k < fs.n; ++k) {
+    const int nb = fs.n;
+#pragma unroll
+    for (int k = 0; k < kFlatMax; ++k) {
+        if (k >= nb) break;
         const float4 lo = fs.box[k].lo, hi = fs.box[k].hi;
         const float t0x = (lo.x - o.x) * inv.x, t1x = (hi.x - o.x) * inv.x;
         const float t0y = (lo.y - o.y) * inv.y, t1y = (hi.y - o.y) * inv.y;
@@ -605,7 +608,7 @@ __device__ void drain(const TraceArgs& A, TraceSmem& sm, bool all) {
 }
 
 template <bool kFlat>
-__global__ void __launch_bounds__(kTraceBlock, 3) trace_kernel(const TraceArgs A) {
+__global__ void __launch_bounds__(kTraceBlock, 6) trace_kernel(const TraceArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TraceSmem& sm = *reinterpret_cast<TraceSmem*>(smem_raw);
     if (threadIdx.x < sizeof(SunFrame) / 4)

@@ -61,6 +61,7 @@ SIGNATURES = {
     "csp_write_hits_csv": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.c_char_p]),
     "csp_write_output": (ctypes.c_int, [_H, ctypes.c_char_p]),
     "csp_element_frame": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+    "csp_trace_into": (ctypes.c_int, [_H, _P, _P, ctypes.c_uint64, ctypes.c_uint64, _P]),
 }
 STINPUT_APPLY_OPTICS = 1
 
@@ -176,6 +177,12 @@ class Tracer:
         if hits.dtype != np.float32 or hits.size != self.num_rays * MAX_DEPTH * 4 or not hits.flags.c_contiguous:
             raise ValueError("hits must be a contiguous float32 array of num_rays*5*4 elements")
         _check(self.lib.csp_run_to_host(self.h, _ptr(hits), _ptr(ids)))
+
+    def trace_into(self, hits_ptr: int, ids_ptr: int | None = None, first: int = 0, count: int | None = None,
+                   stream: int | None = None):
+        count = self.num_rays - first if count is None else count
+        _check(self.lib.csp_trace_into(self.h, ctypes.c_void_p(hits_ptr), ctypes.c_void_p(ids_ptr or 0), int(first),
+                                       int(count), ctypes.c_void_p(stream or 0)))
 
     def run_to_host_ptr(self, hits_ptr: int, ids_ptr: int | None = None):
         _check(self.lib.csp_run_to_host(self.h, ctypes.c_void_p(hits_ptr), ctypes.c_void_p(ids_ptr or 0)))
