@@ -131,6 +131,20 @@ CSP_API int csp_run_to_host(csp_handle h, float* dst, uint32_t* ids);
  * the device can address (the kernel then stores the records across the host link directly).
  * ids may be NULL.  No host synchronisation; the handle's own hit buffer is not touched. */
 CSP_API int csp_trace_into(csp_handle h, void* hits, void* ids, uint64_t first_ray, uint64_t count, void* stream);
+/* One trace that allocates no memory (no counterpart in the reference).  For callers that cannot
+ * call cudaMalloc -- a framework whose allocator already holds the device memory, a real-time
+ * tracking loop that cannot take cudaMalloc's device-wide synchronisation: the caller passes the
+ * elements (at most 8), the sun, and its own output buffers (hits: num_rays * 5 float4, ids: NULL
+ * or num_rays * 5 uint32, device-addressable); rays [first_ray, first_ray + num_rays) are traced on
+ * `stream` of `device`, bit-identical to csp_trace_into on a handle with the same scene.  The only
+ * intermediate data live in a fixed 4 KB device array inside the library (held on every device that
+ * uses it until the library is unloaded); every call overwrites it fully, and calls whose work
+ * overlaps on the GPU (different streams or host threads) race on it.  The first call on a device
+ * looks up that array's address; make it before any stream capture.  More than 8 elements is
+ * rejected with CSP_ERR_INVALID_ARGUMENT.  No host synchronisation. */
+CSP_API int csp_trace_noalloc(int device, const csp_element* elements, uint32_t count, const double* sun_dir,
+                              int sun_shape, double sun_param, uint64_t seed, uint32_t instance, uint64_t first_ray,
+                              uint64_t num_rays, void* hits, void* ids, void* stream);
 /* Device pointers of the hit buffer ([num_rays*5] float4) and id buffer (NULL unless recorded). */
 CSP_API int csp_get_device_buffers(csp_handle h, void** hits, void** ids);
 

@@ -25,6 +25,7 @@ SOURCES = [
     "csp_scene.cpp",
     "csp_c_api.cpp",
     "csp_io.cpp",
+    "csp_noalloc.cu",
     "../cpp/src/dropin.cpp",
 ]
 COMMON = [

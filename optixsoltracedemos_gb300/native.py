@@ -62,6 +62,9 @@ SIGNATURES = {
     "csp_write_output": (ctypes.c_int, [_H, ctypes.c_char_p]),
     "csp_element_frame": (ctypes.c_int, [_P, _P, _P, _P, _P]),
     "csp_trace_into": (ctypes.c_int, [_H, _P, _P, ctypes.c_uint64, ctypes.c_uint64, _P]),
+    "csp_trace_noalloc": (ctypes.c_int, [ctypes.c_int, _P, ctypes.c_uint32, _P, ctypes.c_int, ctypes.c_double,
+                                         ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64, _P, _P,
+                                         _P]),
 }
 STINPUT_APPLY_OPTICS = 1
 
@@ -237,6 +240,20 @@ def parse_stinput(path: str, apply_optics: bool = False):
     out = np.zeros(n.value, ELEMENT_DTYPE)
     _check(lib.csp_parse_stinput(path.encode(), _ptr(out), n.value, ctypes.byref(n), _ptr(sun), _ptr(ang), fl))
     return out, sun, float(ang[0])
+
+
+def trace_noalloc(elements: np.ndarray, sun_dir, sun_shape: int, sun_param: float, hits_ptr: int,
+                  ids_ptr: int | None = None, first_ray: int = 0, num_rays: int = 0, seed: int = 0,
+                  instance: int = 0, device: int = 0, stream: int | None = None) -> None:
+    """csp_trace_noalloc: trace into caller-owned device buffers without any allocation (<= 8 elements)."""
+    e = np.ascontiguousarray(elements)
+    if e.dtype != ELEMENT_DTYPE:
+        raise TypeError("elements must use scenes.ELEMENT_DTYPE")
+    sd = np.ascontiguousarray(sun_dir, np.float64)
+    _check(load().csp_trace_noalloc(int(device), _ptr(e), len(e), _ptr(sd), int(sun_shape), float(sun_param),
+                                    int(seed), int(instance), int(first_ray), int(num_rays),
+                                    ctypes.c_void_p(hits_ptr), ctypes.c_void_p(ids_ptr or 0),
+                                    ctypes.c_void_p(stream or 0)))
 
 
 def write_hits_csv(hits: np.ndarray, path: str) -> None:
