@@ -39,9 +39,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "rays/s on 1 GB300 (batched/served vs plain trace) at flux L2<=1%; p50/p99 latency"
 BYTES_PER_RAY = 80  # 5 float4 hit records per ray, fully rewritten by every trace
-# dram__bytes_read.sum + dram__bytes_write.sum of one trace_kernel launch of this workload, from the
-# ncu capture summarised in profiles/trace_kernel_single_parabolic.md (None until captured)
-NCU_TRAFFIC_PER_LAUNCH = None
+# dram__bytes_read.sum + dram__bytes_write.sum of one full-size trace_kernel launch of this workload
+# (14,810,368 + 1,313,165,056 bytes), from the ncu capture summarised in
+# profiles/trace_kernel_single_parabolic.md
+NCU_TRAFFIC_PER_LAUNCH = 1327975424
 
 
 def parse():
@@ -272,7 +273,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": config(N),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": NCU_TRAFFIC_PER_LAUNCH, "peak_source": peak_kind,
+                     "traffic": NCU_TRAFFIC_PER_LAUNCH if N == 1 << 24 else None, "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": BYTES_PER_RAY * N, "launch_ms": launch_s * 1e3},
         "e2e": {"value": world * N / e2e_s, "unit": "rays/s",
                 "h2d_bytes_per_step": int(elements.nbytes + 3 * 8),
