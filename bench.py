@@ -51,7 +51,10 @@ def parse():
     p.add_argument("--steps", type=int, default=400)
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--rays", type=int, default=1 << 24)
+    p.add_argument("--rays", type=int, default=None, help="ray count (default: the workload's)")
+    p.add_argument("--workload", choices=["single_parabolic", "three_heliostats", "large_field"],
+                   default="single_parabolic",
+                   help="single_parabolic is the benchmark line; the others are for reporting only")
     p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -125,15 +128,14 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(seconds: float, rays: int):
+def cpu_baseline(seconds: float, sc):
     """Oracle port of the reference algorithm on all host cores over a bounded sample."""
     from oracle import oracle
-    from optixsoltracedemos_gb300 import scenes
     oracle.build(with_ref=False)
     o = oracle.Oracle("f32")
-    sc = scenes.single_parabolic(num_rays=rays)
+    rays = sc.num_rays
     cores = os.cpu_count() or 1
-    chunk = 1 << 20
+    chunk = 1 << 20 if len(sc.elements) < 64 else 1 << 12
     o.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, first_ray=0, count=chunk // 8, nthreads=cores,
             with_ids=False)
     done, first, t0 = 0, 0, time.perf_counter()
@@ -144,16 +146,38 @@ def cpu_baseline(seconds: float, rays: int):
         first = (first + chunk) % rays
     dt = time.perf_counter() - t0
     return {"value": done / dt, "unit": "rays/s", "cores": cores, "kind": "port",
-            "sample": f"{done} rays ({done // chunk} chunks of {chunk}) of the single_parabolic workload, "
+            "sample": f"{done} rays ({done // chunk} chunks of {chunk}) of the {sc.name} workload, "
                       f"{dt:.1f} s, OpenMP over {cores} threads"}
 
 
-def config(rays):
-    return {"workload": "single_parabolic_heliostat_cylinder_receiver", "rays": rays, "elements": 2,
-            "sun": "gaussian 2.5 mrad", "slope_error_rad": 1.5e-3, "focal_length_m": 100.0,
-            "hit_buffer_bytes": rays * BYTES_PER_RAY,
-            "l2_policy": "hit buffer (1.34 GB) larger than L2; no flush needed between steps",
+def make_scene(workload, rays):
+    from optixsoltracedemos_gb300 import scenes
+    if workload == "three_heliostats":
+        sc = scenes.three_heliostats()
+    elif workload == "large_field":
+        sc = scenes.large_field()
+    else:
+        sc = scenes.single_parabolic()
+    if rays:
+        sc.num_rays = rays
+    return sc
+
+
+def config(sc):
+    rays = sc.num_rays
+    base = {"rays": rays, "elements": int(len(sc.elements)), "hit_buffer_bytes": rays * BYTES_PER_RAY,
+            "l2_policy": f"hit buffer ({rays * BYTES_PER_RAY / 1e9:.2f} GB) larger than L2; no flush needed between steps",
             "parallelism": "replicas"}
+    if sc.name == "single_parabolic":
+        base.update({"workload": "single_parabolic_heliostat_cylinder_receiver", "sun": "gaussian 2.5 mrad",
+                     "slope_error_rad": 1.5e-3, "focal_length_m": 100.0})
+    elif sc.name == "three_heliostats":
+        base.update({"workload": "three_flat_heliostats_flat_receiver", "sun": "pillbox 4.65 mrad",
+                     "slope_error_rad": 1e-3, "reflectivity": 0.9})
+    else:
+        base.update({"workload": "large_field_10000_flat_heliostats_cylinder_receiver", "sun": "pillbox 4.65 mrad",
+                     "slope_error_rad": 1.5e-3})
+    return base
 
 
 def run_reference(args):
@@ -164,24 +188,24 @@ def run_reference(args):
     from optixsoltracedemos_gb300 import scenes
     oracle.build(with_ref=False)
     o = oracle.Oracle("f32")
-    sc = scenes.single_parabolic(num_rays=args.rays)
+    sc = make_scene(args.workload, args.rays)
     cores = os.cpu_count() or 1
-    sample = 1 << 20
+    sample = min(1 << 20, sc.num_rays) if args.workload != "large_field" else 1 << 14
     for w in range(args.warmup):
-        o.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, first_ray=w * sample % args.rays, count=sample,
-                nthreads=cores, with_ids=False)
+        o.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, first_ray=w * sample % sc.num_rays,
+                count=sample, nthreads=cores, with_ids=False)
     t0 = time.perf_counter()
     for k in range(args.steps):
-        o.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, first_ray=(k * sample) % args.rays,
+        o.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, first_ray=(k * sample) % sc.num_rays,
                 count=sample, nthreads=cores, with_ids=False)
     dt = time.perf_counter() - t0
     v = args.steps * sample / dt
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "rays/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config(args.rays),
+            "config": config(sc),
             "cpu_baseline": {"value": v, "unit": "rays/s", "cores": cores, "kind": "port",
-                             "sample": f"each step traces {sample} of the {args.rays} rays (oracle port of the "
+                             "sample": f"each step traces {sample} of the {sc.num_rays} rays (oracle port of the "
                                        f"reference algorithm, OpenMP over {cores} threads)"},
             "e2e": {"value": v, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -207,8 +231,8 @@ def run_ours(args):
     from optixsoltracedemos_gb300 import native, scenes
     from optixsoltracedemos_gb300.flux import flux_map_from_hits, flux_l2
 
-    sc = scenes.single_parabolic(num_rays=args.rays)
-    N = args.rays
+    sc = make_scene(args.workload, args.rays)
+    N = sc.num_rays
     tr = native.tracer_for(sc, device=local, record_ids=False)
     stream = torch.cuda.Stream(device=local)
     sp = stream.cuda_stream
@@ -271,9 +295,10 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": config(N),
+        "config": config(sc),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": NCU_TRAFFIC_PER_LAUNCH if N == 1 << 24 else None, "peak_source": peak_kind,
+                     "traffic": NCU_TRAFFIC_PER_LAUNCH if (N == 1 << 24 and sc.name == "single_parabolic") else None,
+                     "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": BYTES_PER_RAY * N, "launch_ms": launch_s * 1e3},
         "e2e": {"value": world * N / e2e_s, "unit": "rays/s",
                 "h2d_bytes_per_step": int(elements.nbytes + 3 * 8),
@@ -297,7 +322,7 @@ def run_ours(args):
         except Exception as exc:  # accuracy is reported, not required for the timing line
             line["flux_l2_vs_fp64"] = f"unavailable: {exc}"
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args.cpu_seconds, N)
+        line["cpu_baseline"] = cpu_baseline(args.cpu_seconds, sc)
     tr.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

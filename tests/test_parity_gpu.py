@@ -51,12 +51,27 @@ def test_gpu_matches_oracle_bit_exact(gpu, oracle32, name):
     if name == "single_parabolic_pillbox_spec":
         sc.elements["specularity_error"][0] = 0.5e-3
         sc.elements["reflectivity"][0] = 0.93
-    n = 60000 if "field" not in name else 20000
+    n = 60000  # above 2 x 27648: the BVH path's coherent ray order covers two whole blocks and a tail
     for seed, inst in ((0, 0), (987654321, 5)):
         hits, ids = gpu_trace(sc, n, seed=seed, instance=inst)
         oh, oi = oracle32.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, count=n, seed=seed, instance=inst)
         np.testing.assert_array_equal(ids, oi)
         np.testing.assert_array_equal(hits, oh.astype(np.float32))
+
+
+def test_gpu_large_field_bvh_bit_exact(gpu, oracle32):
+    """2000 flat heliostats, cylinder receiver (BVH path, coherent ray order): a window of 100k rays
+    starting mid-launch, against the oracle's brute-force closest hit."""
+    sc = scenes.large_field(n_heliostats=2000, sun=scenes.sun_vector(35.0, 70.0))
+    t = native.tracer_for(sc, seed=4, num_rays=400000)
+    t.run()
+    first, n = 150001, 100000
+    hits, ids = t.copy_hits(first, n)
+    t.close()
+    oh, oi = oracle32.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, first_ray=first, count=n, seed=4)
+    np.testing.assert_array_equal(ids, oi)
+    np.testing.assert_array_equal(hits, oh.astype(np.float32))
+    assert (hits[:, :, 0] == 2).sum() > 1000
 
 
 def test_gpu_sun_plane_matches_oracle(gpu, oracle32):
