@@ -172,6 +172,60 @@ CSP_API int csp_write_output(csp_handle h, const char* path);
 /* out[16]: sun vector (3), v0 (3), v1 (3), v2 (3), v3 (3), plane distance (1). */
 CSP_API int csp_get_sun_plane(csp_handle h, float* out);
 
+/* ---- Receiver flux maps ---- */
+/* Flux map of the last run on the receiver (last element), computed on the device from the hit
+ * buffer: stage-2 records binned nx x ny as scripts/post_processing/flux_map_calculator.py:135-179
+ * does (flat receiver: local x, y over the aperture; cylinder: angle about the axis in [0, 2 pi)
+ * from the local x axis, and the axial coordinate; cylinder cap hits are dropped), bin (i, j) at
+ * [i * ny + j].  counts (may be NULL) receives hit counts; flux (may be NULL) receives W/m^2 =
+ * counts * dni * sun-plane area / rays / bin area. */
+CSP_API int csp_flux_map(csp_handle h, uint32_t nx, uint32_t ny, uint32_t* counts, double dni, double* flux);
+/* Host-only (no GPU): the float binning parameters the device uses for a receiver element.
+ * out[20]: origin (3), local x, y, z axes (9), hx, hy, kx, ky, keep, kind (0 flat, 1 cylinder),
+ * bin area (m^2), 0.  A record at p lands in bx = floor((lx + hx) kx) (flat) or
+ * floor(atan2(lz, lx) mod 2 pi * kx) (cylinder, |ly| < keep only), by = floor((ly + hy) ky). */
+CSP_API int csp_flux_target(const csp_element* receiver, uint32_t nx, uint32_t ny, float* out);
+
+/* ---- Batched tracing: many scene instances in one persistent launch ----
+ * A batch holds scenes (element lists; a scene's BVH topology is built once) and instances (a
+ * scene with optional per-instance element poses -- same count and surfaces, new origins, aim
+ * points or rotations -- a sun vector and shape, a ray count, a seed and a Philox instance id).
+ * csp_batch_run uploads the instances, refits each instance's BVH on the device, computes every
+ * instance's sun plane and traces all instances in one persistent launch per scene class
+ * (<= 8 elements / larger), binning receiver records into per-instance flux maps on the fly; no
+ * per-ray records are kept.  The device work of a run is one CUDA graph, re-launched while the
+ * batch layout (instances, element and ray counts) is unchanged.  Instance i's flux map equals
+ * csp_flux_map of a plain run of the same scene, sun, rays, seed and instance id.
+ * Replaces the reference's per-scene loop of set_sun_vector / update / run
+ * (lib/soltrace_system.cpp:145-184, demos/demo_dynamic_scene.cpp:18-78) with one launch. */
+typedef struct csp_batch_s* csp_batch;
+CSP_API int csp_batch_create(csp_batch* out, int device);
+CSP_API int csp_batch_destroy(csp_batch b);
+/* Flux map grid of every instance (default 100 x 100); resets the instances' results. */
+CSP_API int csp_batch_set_flux_grid(csp_batch b, uint32_t nx, uint32_t ny);
+CSP_API int csp_batch_add_scene(csp_batch b, const csp_element* elements, uint32_t count, uint32_t* scene_id);
+/* poses: NULL (the scene's own elements) or count elements matching the scene's surfaces. */
+CSP_API int csp_batch_add_instance(csp_batch b, uint32_t scene_id, const csp_element* poses, const double* sun_dir,
+                                   int sun_shape, double sun_param, uint64_t num_rays, uint64_t seed,
+                                   uint32_t instance, uint32_t* index);
+CSP_API int csp_batch_clear_instances(csp_batch b);
+CSP_API int csp_batch_num_instances(csp_batch b, uint32_t* count);
+/* Launch parameters: CTA/tile size (128 or 256 rays), resident CTAs per SM (0 = occupancy limit),
+ * tiles per work grab.  block = 0 selects the autotuner (default), which times candidates on a
+ * sample of the batch at the first run of each scene class and keeps the fastest per device. */
+CSP_API int csp_batch_set_tuning(csp_batch b, int block, int ctas_per_sm, int chunk);
+/* The parameters used by the last run for small (flat != 0) or BVH scenes. */
+CSP_API int csp_batch_get_tuning(csp_batch b, int flat, int* block, int* ctas_per_sm, int* chunk);
+CSP_API int csp_batch_run(csp_batch b);
+/* Results of the last run: counts / flux as csp_flux_map; stats[4] = rays, mirror records,
+ * receiver records, binned receiver records. */
+CSP_API int csp_batch_get_flux(csp_batch b, uint32_t index, uint32_t* counts, double dni, double* flux);
+CSP_API int csp_batch_get_stats(csp_batch b, uint32_t index, uint64_t* stats);
+/* out[16] as csp_get_sun_plane, for one instance. */
+CSP_API int csp_batch_get_sun_plane(csp_batch b, uint32_t index, float* out);
+/* setup_s: host element builds and upload; trace_s: device time of refit + sun planes + trace. */
+CSP_API int csp_batch_get_timing(csp_batch b, double* setup_s, double* trace_s);
+
 #ifdef __cplusplus
 }
 #endif

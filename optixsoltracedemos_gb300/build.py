@@ -26,6 +26,8 @@ SOURCES = [
     "csp_c_api.cpp",
     "csp_io.cpp",
     "csp_noalloc.cu",
+    "csp_batch.cu",
+    "csp_batch.cpp",
     "../cpp/src/dropin.cpp",
 ]
 COMMON = [

@@ -1,0 +1,692 @@
+// csp_batch.cpp -- batched tracing behind csp_batch_* (include/csp_c_api.h).
+//
+// A run:
+//   host    per-instance element builds (the reference's geometry arithmetic, lib/element.cpp and
+//           the GeometryDataST constructors, exactly as the single-scene path does it), in
+//           parallel threads, written into one pinned staging image of the device arena
+//   device  one CUDA graph: upload the image, zero the flux maps and counters, refit every
+//           instance's BVH (refit_kernel), compute every instance's sun plane
+//           (prepare_sun_batch_kernel), trace the small-scene instances and the BVH instances
+//           (one persistent batch_kernel launch each), copy flux maps, counters and sun frames back
+// The graph is captured once per batch layout (instances, element counts, ray counts, tuning) and
+// re-launched while the layout is unchanged.
+//
+// Arena layout (one cudaMalloc, offsets 16-byte aligned):
+//   upload  [per instance: prims | optics | aabbs | prune] [descs flat | descs bvh]
+//           [tile_begin flat | tile_begin bvh] [refit jobs] [sun jobs]
+//   nodes   per-instance refitted BVH nodes
+//   zeroed  [work counters (2)] [stats, 4 x u64 per instance] [counts, nx*ny x u32 per instance]
+//   suns    per-instance SunFrame
+// The download region is [stats .. suns end), one copy.
+#include "csp_batch.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <tuple>
+
+#include "csp_system.h"
+
+namespace csp {
+namespace {
+
+size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+// tuned launch parameters, per (device, scene class, ray-count class)
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int>, BatchTuning> g_tune_cache;
+
+int ray_class(uint64_t mean_rays) {
+    int c = 0;
+    while (mean_rays > 1 && c < 63) {
+        mean_rays >>= 1;
+        ++c;
+    }
+    return c / 2;  // factors of 4
+}
+
+}  // namespace
+
+Batch::~Batch() { release(); }
+
+void Batch::release() {
+    if (device >= 0) cudaSetDevice(device);
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+    for (BScene& s : scenes) {
+        cudaFree(s.d_topo);
+        s.d_topo = nullptr;
+    }
+    cudaFree(d_arena);
+    d_arena = nullptr;
+    arena_cap = 0;
+    if (h_stage) cudaFreeHost(h_stage);
+    if (h_result) cudaFreeHost(h_result);
+    h_stage = h_result = nullptr;
+    stage_cap = result_cap = 0;
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) cudaStreamDestroy(stream);
+    ev0 = ev1 = nullptr;
+    stream = nullptr;
+}
+
+int Batch::ensure_stream() {
+    if (stream) return CSP_OK;
+    int rc = cuda_status(cudaSetDevice(device), "cudaSetDevice");
+    if (rc) return rc;
+    if ((rc = cuda_status(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate"))) return rc;
+    if ((rc = cuda_status(cudaEventCreate(&ev0), "cudaEventCreate"))) return rc;
+    return cuda_status(cudaEventCreate(&ev1), "cudaEventCreate");
+}
+
+int Batch::add_scene(const csp_element* el, uint32_t n, uint32_t* id) {
+    int rc = ensure_stream();
+    if (rc) return rc;
+    BScene s;
+    s.elements.assign(el, el + n);
+    std::string err;
+    if ((rc = build_elements(el, n, s.base, err))) return set_error(rc, err);
+    build_bvh(s.base);
+    s.flat = n <= kFlatListMax;
+    const size_t bytes = s.base.nodes.size() * sizeof(Node);
+    if ((rc = cuda_status(cudaMalloc((void**)&s.d_topo, bytes), "cudaMalloc topology"))) return rc;
+    if ((rc = cuda_status(cudaMemcpy(s.d_topo, s.base.nodes.data(), bytes, cudaMemcpyHostToDevice), "upload topology"))) {
+        cudaFree(s.d_topo);
+        return rc;
+    }
+    scenes.push_back(std::move(s));
+    if (id) *id = (uint32_t)(scenes.size() - 1);
+    return CSP_OK;
+}
+
+int Batch::add_instance(const BInst& bi, uint32_t* index) {
+    if (bi.scene >= scenes.size()) return set_error(CSP_ERR_INVALID_ARGUMENT, "no such scene");
+    const BScene& s = scenes[bi.scene];
+    if (!bi.poses.empty()) {
+        if (bi.poses.size() != s.elements.size())
+            return set_error(CSP_ERR_BAD_SCENE, "instance poses must have the scene's element count");
+        for (size_t k = 0; k < s.elements.size(); ++k)
+            if (bi.poses[k].surface != s.elements[k].surface || bi.poses[k].aperture != s.elements[k].aperture)
+                return set_error(CSP_ERR_BAD_SCENE, "instance pose " + std::to_string(k) + " changes the surface type");
+    }
+    if (bi.shape != CSP_SUN_PILLBOX && bi.shape != CSP_SUN_GAUSSIAN)
+        return set_error(CSP_ERR_INVALID_ARGUMENT, "unknown sun shape");
+    if (!(bi.param >= 0.0) || bi.param > 0.5) return set_error(CSP_ERR_INVALID_ARGUMENT, "sun shape parameter out of range");
+    if (bi.rays >= (1ull << 40)) return set_error(CSP_ERR_INVALID_ARGUMENT, "too many rays for one instance");
+    inst.push_back(bi);
+    if (index) *index = (uint32_t)(inst.size() - 1);
+    ran = false;
+    return CSP_OK;
+}
+
+const csp_element* Batch::elements_of(size_t i) const {
+    return inst[i].poses.empty() ? scenes[inst[i].scene].elements.data() : inst[i].poses.data();
+}
+
+uint32_t Batch::count_of(size_t i) const { return (uint32_t)scenes[inst[i].scene].elements.size(); }
+
+// Offsets of every region; grows the arena and the pinned buffers when needed.
+int Batch::layout() {
+    const size_t n = inst.size();
+    place.assign(n, Place{});
+    n_group[0] = n_group[1] = 0;
+    max_nodes = 0;
+    size_t off = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const BScene& s = scenes[inst[i].scene];
+        const size_t ne = s.elements.size();
+        Place& p = place[i];
+        p.group = s.flat ? 0 : 1;
+        p.slot = n_group[p.group]++;
+        p.prims = off;
+        off += align16(ne * sizeof(Prim));
+        p.optics = off;
+        off += align16(ne * sizeof(Optics));
+        p.aabbs = off;
+        off += align16(ne * sizeof(Aabb));
+        p.prune = off;
+        off += align16(ne * sizeof(Aabb));
+        max_nodes = std::max(max_nodes, (int)s.base.nodes.size());
+    }
+    for (int g = 0; g < 2; ++g) {
+        desc_off[g] = off;
+        off += align16(n_group[g] * sizeof(InstanceDesc));
+    }
+    for (int g = 0; g < 2; ++g) {
+        tb_off[g] = off;
+        off += align16((n_group[g] + 1) * sizeof(uint64_t));
+    }
+    refit_off = off;
+    off += align16(n * sizeof(RefitJob));
+    sunjob_off = off;
+    off += align16(n * sizeof(SunJob));
+    up_bytes = off;
+    for (size_t i = 0; i < n; ++i) {
+        place[i].nodes = off;
+        off += align16(scenes[inst[i].scene].base.nodes.size() * sizeof(Node));
+    }
+    zero_off = off;
+    counter_off = off;
+    off += 16;
+    res_off = off;
+    for (size_t i = 0; i < n; ++i) {
+        place[i].stats = off;
+        off += 4 * sizeof(unsigned long long);
+    }
+    const size_t nb = (size_t)nx * ny;
+    for (size_t i = 0; i < n; ++i) {
+        place[i].counts = off;
+        off += align16(nb * sizeof(uint32_t));
+    }
+    zero_bytes = off - zero_off;
+    for (size_t i = 0; i < n; ++i) {
+        place[i].sun = off;
+        off += align16(sizeof(SunFrame));
+    }
+    res_bytes = off - res_off;
+    const size_t total = std::max<size_t>(off, 16);
+
+    int rc;
+    if (total > arena_cap) {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        cudaFree(d_arena);
+        d_arena = nullptr;
+        arena_cap = 0;
+        size_t free_b = 0, total_b = 0;
+        cudaMemGetInfo(&free_b, &total_b);
+        if (total > free_b) return set_error(CSP_ERR_OUT_OF_MEMORY, "batch does not fit in free device memory");
+        if ((rc = cuda_status(cudaMalloc((void**)&d_arena, total), "cudaMalloc batch arena"))) return rc;
+        arena_cap = total;
+    }
+    if (up_bytes > stage_cap) {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        if (h_stage) cudaFreeHost(h_stage);
+        h_stage = nullptr;
+        stage_cap = 0;
+        if ((rc = cuda_status(cudaHostAlloc((void**)&h_stage, up_bytes, cudaHostAllocDefault), "cudaHostAlloc staging")))
+            return rc;
+        stage_cap = up_bytes;
+    }
+    if (res_bytes > result_cap) {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        if (h_result) cudaFreeHost(h_result);
+        h_result = nullptr;
+        result_cap = 0;
+        if ((rc = cuda_status(cudaHostAlloc((void**)&h_result, std::max<size_t>(res_bytes, 16), cudaHostAllocDefault),
+                              "cudaHostAlloc results")))
+            return rc;
+        result_cap = res_bytes;
+    }
+    return CSP_OK;
+}
+
+// Host build of instance i into the staging image: element records, refit job, sun job.
+int Batch::fill_instance(size_t i, HostScene& hs, std::string& err) {
+    const BInst& b = inst[i];
+    const Place& p = place[i];
+    const BScene& s = scenes[b.scene];
+    const uint32_t ne = count_of(i);
+    const HostScene* src = &s.base;
+    if (!b.poses.empty()) {
+        int rc = build_elements(b.poses.data(), ne, hs, err);
+        if (rc) return rc;
+        src = &hs;
+    }
+    std::memcpy(h_stage + p.prims, src->prims.data(), ne * sizeof(Prim));
+    std::memcpy(h_stage + p.optics, src->optics.data(), ne * sizeof(Optics));
+    std::memcpy(h_stage + p.aabbs, src->aabbs.data(), ne * sizeof(Aabb));
+    std::memcpy(h_stage + p.prune, src->prune.data(), ne * sizeof(Aabb));
+    RefitJob rj;
+    rj.topo = s.d_topo;
+    rj.aabbs = reinterpret_cast<const Aabb*>(d_arena + p.aabbs);
+    rj.prune = reinterpret_cast<const Aabb*>(d_arena + p.prune);
+    rj.out = reinterpret_cast<Node*>(d_arena + p.nodes);
+    rj.n_nodes = (int)s.base.nodes.size();
+    rj.pad = 0;
+    std::memcpy(h_stage + refit_off + i * sizeof(RefitJob), &rj, sizeof rj);
+    float sv[3];
+    sun_vector_f(b.sun, sv);
+    SunJob sj;
+    sj.aabbs = rj.aabbs;
+    sj.n = (int)ne;
+    sj.sx = sv[0];
+    sj.sy = sv[1];
+    sj.sz = sv[2];
+    sj.tan_pad = tanf((float)(b.shape == CSP_SUN_GAUSSIAN ? 5.0 * b.param : b.param));
+    sj.shape = b.shape;
+    sj.param = (float)b.param;
+    sj.out = reinterpret_cast<SunFrame*>(d_arena + p.sun);
+    std::memcpy(h_stage + sunjob_off + i * sizeof(SunJob), &sj, sizeof sj);
+    return CSP_OK;
+}
+
+// Instance descriptors and tile tables of both groups for the given tile sizes; `sample` > 0
+// limits every instance to its first rays (autotuner), 0 = all rays.
+void Batch::fill_descs(const int block[2], double sample, std::vector<InstanceDesc>* out_desc,
+                       std::vector<uint64_t>* out_tb) {
+    const size_t n = inst.size();
+    for (int g = 0; g < 2; ++g) {
+        out_desc[g].assign(n_group[g], InstanceDesc{});
+        out_tb[g].assign(n_group[g] + 1, 0);
+    }
+    uint64_t tiles[2] = {0, 0};
+    for (size_t i = 0; i < n; ++i) {
+        const BInst& b = inst[i];
+        const Place& p = place[i];
+        const int g = p.group;
+        uint64_t rays = b.rays;
+        if (sample > 0) rays = std::min<uint64_t>(rays, (uint64_t)std::ceil(rays * sample) + (uint64_t)block[g]);
+        InstanceDesc& d = out_desc[g][p.slot];
+        d.args.nodes = reinterpret_cast<const Node*>(d_arena + p.nodes);
+        d.args.prims = reinterpret_cast<const Prim*>(d_arena + p.prims);
+        d.args.optics = reinterpret_cast<const Optics*>(d_arena + p.optics);
+        d.args.sun = reinterpret_cast<const SunFrame*>(d_arena + p.sun);
+        d.args.hits = nullptr;
+        d.args.ids = nullptr;
+        d.args.ray_begin = 0;
+        d.args.count = rays;
+        d.args.seed = b.seed;
+        d.args.instance = b.instance;
+        d.args.pad = 0;
+        flux_target(elements_of(i)[count_of(i) - 1], nx, ny, d.flux);
+        d.flux.counts = reinterpret_cast<uint32_t*>(d_arena + p.counts);
+        d.flux.stats = reinterpret_cast<unsigned long long*>(d_arena + p.stats);
+        d.tile_begin = tiles[g];
+        d.n_prims = (int)count_of(i);
+        out_tb[g][p.slot] = tiles[g];
+        tiles[g] += (rays + block[g] - 1) / block[g];
+    }
+    for (int g = 0; g < 2; ++g) out_tb[g][n_group[g]] = tiles[g];
+}
+
+void Batch::write_descs(const std::vector<InstanceDesc>* desc, const std::vector<uint64_t>* tb, unsigned char* img) {
+    for (int g = 0; g < 2; ++g) {
+        if (!desc[g].empty()) std::memcpy(img + desc_off[g], desc[g].data(), desc[g].size() * sizeof(InstanceDesc));
+        std::memcpy(img + tb_off[g], tb[g].data(), tb[g].size() * sizeof(uint64_t));
+    }
+}
+
+BatchLaunch Batch::launch_of(int g, uint64_t total_tiles, int chunk) const {
+    BatchLaunch L;
+    L.inst = reinterpret_cast<const InstanceDesc*>(d_arena + desc_off[g]);
+    L.tile_begin = reinterpret_cast<const uint64_t*>(d_arena + tb_off[g]);
+    L.n_inst = n_group[g];
+    L.chunk = chunk;
+    L.total_tiles = total_tiles;
+    L.next_tile = reinterpret_cast<unsigned long long*>(d_arena + counter_off) + g;
+    return L;
+}
+
+// Device work of a run up to (not including) the trace launches.
+int Batch::enqueue_prefix(cudaStream_t st) {
+    int rc;
+    if ((rc = cuda_status(cudaMemcpyAsync(d_arena, h_stage, up_bytes, cudaMemcpyHostToDevice, st), "upload batch")))
+        return rc;
+    if ((rc = cuda_status(cudaMemsetAsync(d_arena + zero_off, 0, zero_bytes, st), "zero flux maps"))) return rc;
+    return CSP_OK;
+}
+
+int Batch::enqueue_scene_setup(cudaStream_t st) {
+    int rc;
+    if ((rc = cuda_status(launch_refit(reinterpret_cast<const RefitJob*>(d_arena + refit_off), (int)inst.size(),
+                                       max_nodes, st),
+                          "refit_kernel")))
+        return rc;
+    return cuda_status(launch_prepare_sun_batch(reinterpret_cast<const SunJob*>(d_arena + sunjob_off),
+                                                (int)inst.size(), st),
+                       "prepare_sun_batch_kernel");
+}
+
+// Time the candidate launch parameters of group g on a sample of its instances and keep the
+// fastest.  Needs the scene setup on the device (prefix + refit + sun frames) done.
+int Batch::autotune(int g, BatchTuning& best) {
+    std::vector<BatchTuning> cands;
+    for (int block : {128, 256}) {
+        const int occ = batch_occupancy(g == 0, block);
+        if (occ <= 0) continue;
+        std::vector<int> ctas = {occ};
+        if (occ > 1) ctas.push_back(std::max(1, occ * 2 / 3));
+        for (int c : ctas)
+            for (int chunk : {1, 4, 16}) cands.push_back(BatchTuning{block, c, chunk});
+    }
+    if (cands.empty()) return set_error(CSP_ERR_CUDA, "no launchable configuration of the batch kernel");
+    uint64_t total = 0;
+    for (size_t i = 0; i < inst.size(); ++i)
+        if (place[i].group == g) total += inst[i].rays;
+    const double budget = g == 0 ? 256e6 : 32e6;  // rays per candidate
+    const double sample = std::min(1.0, std::max(1e-4, budget / std::max<double>(1.0, (double)total)));
+    std::vector<unsigned char> img(up_bytes);
+    double best_ms = 1e30;
+    int rc = CSP_OK;
+    for (const BatchTuning& t : cands) {
+        const int block[2] = {t.block, t.block};
+        std::vector<InstanceDesc> desc[2];
+        std::vector<uint64_t> tb[2];
+        fill_descs(block, sample, desc, tb);
+        // descs and tile tables only: the element records already on the device stay
+        const size_t lo = desc_off[0], hi = refit_off;
+        write_descs(desc, tb, img.data());
+        if ((rc = cuda_status(cudaMemcpyAsync(d_arena + lo, img.data() + lo, hi - lo, cudaMemcpyHostToDevice, stream),
+                              "upload sample descs")))
+            break;
+        const BatchLaunch L = launch_of(g, tb[g][n_group[g]], t.chunk);
+        float ms_best = 1e30f;
+        for (int rep = 0; rep < 2 && rc == CSP_OK; ++rep) {
+            rc = cuda_status(cudaMemsetAsync(d_arena + counter_off, 0, 16, stream), "zero counters");
+            if (!rc) rc = cuda_status(cudaEventRecord(ev0, stream), "cudaEventRecord");
+            if (!rc) rc = cuda_status(launch_trace_batch(L, g == 0, t, stream), "batch_kernel");
+            if (!rc) rc = cuda_status(cudaEventRecord(ev1, stream), "cudaEventRecord");
+            if (!rc) rc = cuda_status(cudaEventSynchronize(ev1), "autotune");
+            float ms = 0.f;
+            if (!rc) cudaEventElapsedTime(&ms, ev0, ev1);
+            ms_best = std::min(ms_best, ms);
+        }
+        if (rc) break;
+        if (ms_best < best_ms) {
+            best_ms = ms_best;
+            best = t;
+        }
+    }
+    return rc;
+}
+
+int Batch::resolve_tuning() {
+    uint64_t rays[2] = {0, 0};
+    for (size_t i = 0; i < inst.size(); ++i) rays[place[i].group] += inst[i].rays;
+    bool need_setup = true;
+    for (int g = 0; g < 2; ++g) {
+        if (n_group[g] == 0) {
+            used[g] = BatchTuning{128, 0, 4};
+            continue;
+        }
+        if (user.block != 0) {
+            if (batch_occupancy(g == 0, user.block) <= 0)
+                return set_error(CSP_ERR_INVALID_ARGUMENT, "unsupported batch block size");
+            used[g] = user;
+            continue;
+        }
+        const auto key = std::make_tuple(device, g, ray_class(rays[g] / (uint64_t)n_group[g]));
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            auto it = g_tune_cache.find(key);
+            if (it != g_tune_cache.end()) {
+                used[g] = it->second;
+                continue;
+            }
+        }
+        int rc;
+        if (need_setup) {
+            if ((rc = enqueue_prefix(stream)) || (rc = enqueue_scene_setup(stream))) return rc;
+            need_setup = false;
+        }
+        BatchTuning best{128, 0, 4};
+        if ((rc = autotune(g, best))) return rc;
+        used[g] = best;
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = best;
+    }
+    return CSP_OK;
+}
+
+int Batch::run() {
+    if (inst.empty()) return set_error(CSP_ERR_STATE, "batch has no instances");
+    const auto t0 = std::chrono::steady_clock::now();
+    int rc = ensure_stream();
+    if (rc) return rc;
+    if ((rc = layout())) return rc;
+
+    // host element builds, parallel over instances
+    const size_t n = inst.size();
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t workers = std::min<size_t>(std::min<size_t>(hw, 64), n);
+    std::vector<int> wrc(workers, CSP_OK);
+    std::vector<std::string> werr(workers);
+    auto work = [&](size_t w) {
+        HostScene hs;
+        for (size_t i = w; i < n; i += workers) {
+            const int r = fill_instance(i, hs, werr[w]);
+            if (r) {
+                wrc[w] = r;
+                werr[w] = "instance " + std::to_string(i) + ": " + werr[w];
+                return;
+            }
+        }
+    };
+    if (workers <= 1) work(0);
+    else {
+        std::vector<std::thread> th;
+        for (size_t w = 0; w < workers; ++w) th.emplace_back(work, w);
+        for (auto& t : th) t.join();
+    }
+    for (size_t w = 0; w < workers; ++w)
+        if (wrc[w]) return set_error(wrc[w], werr[w]);
+
+    if ((rc = resolve_tuning())) return rc;
+    const int block[2] = {used[0].block, used[1].block};
+    std::vector<InstanceDesc> desc[2];
+    std::vector<uint64_t> tb[2];
+    fill_descs(block, 0.0, desc, tb);
+    write_descs(desc, tb, h_stage);
+    const uint64_t tiles[2] = {tb[0][n_group[0]], tb[1][n_group[1]]};
+
+    // graph signature: everything the captured launches depend on besides the staged contents
+    std::vector<uint64_t> sig = {(uint64_t)(uintptr_t)d_arena, (uint64_t)(uintptr_t)h_stage,
+                                 (uint64_t)(uintptr_t)h_result, up_bytes, zero_bytes, res_bytes, n, nx, ny,
+                                 tiles[0], tiles[1]};
+    for (int g = 0; g < 2; ++g) {
+        sig.push_back((uint64_t)used[g].block);
+        sig.push_back((uint64_t)used[g].ctas_per_sm);
+        sig.push_back((uint64_t)used[g].chunk);
+    }
+    if (!graph || sig != graph_sig) {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        cudaGraph_t g = nullptr;
+        if ((rc = cuda_status(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture")))
+            return rc;
+        int crc = enqueue_prefix(stream);
+        if (!crc) crc = cuda_status(cudaEventRecordWithFlags(ev0, stream, cudaEventRecordExternal), "event");
+        if (!crc) crc = enqueue_scene_setup(stream);
+        for (int gi = 0; gi < 2 && !crc; ++gi)
+            if (n_group[gi] > 0)
+                crc = cuda_status(launch_trace_batch(launch_of(gi, tiles[gi], used[gi].chunk), gi == 0, used[gi], stream),
+                                  "batch_kernel");
+        if (!crc) crc = cuda_status(cudaEventRecordWithFlags(ev1, stream, cudaEventRecordExternal), "event");
+        if (!crc)
+            crc = cuda_status(
+                cudaMemcpyAsync(h_result, d_arena + res_off, res_bytes, cudaMemcpyDeviceToHost, stream), "download");
+        const int erc = cuda_status(cudaStreamEndCapture(stream, &g), "end capture");
+        if (crc || erc) {
+            if (g) cudaGraphDestroy(g);
+            return crc ? crc : erc;
+        }
+        rc = cuda_status(cudaGraphInstantiate(&graph, g, 0), "cudaGraphInstantiate");
+        cudaGraphDestroy(g);
+        if (rc) return rc;
+        graph_sig = sig;
+    }
+    time_setup = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if ((rc = cuda_status(cudaGraphLaunch(graph, stream), "cudaGraphLaunch"))) return rc;
+    if ((rc = cuda_status(cudaStreamSynchronize(stream), "batch run"))) return rc;
+    float ms = 0.f;
+    if ((rc = cuda_status(cudaEventElapsedTime(&ms, ev0, ev1), "batch timing"))) return rc;
+    time_trace = ms * 1e-3;
+    ran = true;
+    return CSP_OK;
+}
+
+int Batch::result(uint32_t index, const uint32_t** counts, const unsigned long long** stats, const SunFrame** sun) const {
+    if (!ran) return set_error(CSP_ERR_STATE, "no results: run the batch first");
+    if (index >= inst.size()) return set_error(CSP_ERR_INVALID_ARGUMENT, "no such instance");
+    const Place& p = place[index];
+    if (counts) *counts = reinterpret_cast<const uint32_t*>(h_result + (p.counts - res_off));
+    if (stats) *stats = reinterpret_cast<const unsigned long long*>(h_result + (p.stats - res_off));
+    if (sun) *sun = reinterpret_cast<const SunFrame*>(h_result + (p.sun - res_off));
+    return CSP_OK;
+}
+
+}  // namespace csp
+
+using csp::Batch;
+
+#define CSP_BGUARD(b)                                                                      \
+    do {                                                                                   \
+        if (!(b)) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "null batch handle");     \
+    } while (0)
+
+extern "C" {
+
+int csp_batch_create(csp_batch* out, int device) {
+    if (!out) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "null output handle");
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess) return csp::cuda_status(e, "cudaGetDeviceCount");
+    if (device < 0 || device >= count) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "no such CUDA device");
+    Batch* b = new (std::nothrow) Batch();
+    if (!b) return csp::set_error(CSP_ERR_OUT_OF_MEMORY, "host allocation failed");
+    b->device = device;
+    *out = reinterpret_cast<csp_batch>(b);
+    return CSP_OK;
+}
+
+int csp_batch_destroy(csp_batch b) {
+    CSP_BGUARD(b);
+    delete reinterpret_cast<Batch*>(b);
+    return CSP_OK;
+}
+
+int csp_batch_set_flux_grid(csp_batch bh, uint32_t nx, uint32_t ny) {
+    CSP_BGUARD(bh);
+    if (nx == 0 || ny == 0 || (uint64_t)nx * ny > (1u << 24)) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "bad flux grid");
+    Batch* b = reinterpret_cast<Batch*>(bh);
+    b->nx = nx;
+    b->ny = ny;
+    b->ran = false;
+    return CSP_OK;
+}
+
+int csp_batch_add_scene(csp_batch bh, const csp_element* el, uint32_t n, uint32_t* id) {
+    CSP_BGUARD(bh);
+    if (!el || n == 0) return csp::set_error(CSP_ERR_BAD_SCENE, "scene has no elements");
+    return reinterpret_cast<Batch*>(bh)->add_scene(el, n, id);
+}
+
+int csp_batch_add_instance(csp_batch bh, uint32_t scene, const csp_element* poses, const double* sun, int shape,
+                           double param, uint64_t rays, uint64_t seed, uint32_t instance, uint32_t* index) {
+    CSP_BGUARD(bh);
+    if (!sun) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "null sun vector");
+    Batch* b = reinterpret_cast<Batch*>(bh);
+    csp::BInst bi;
+    bi.scene = scene;
+    if (poses && scene < b->scenes.size()) bi.poses.assign(poses, poses + b->scenes[scene].elements.size());
+    bi.sun[0] = sun[0];
+    bi.sun[1] = sun[1];
+    bi.sun[2] = sun[2];
+    bi.shape = shape;
+    bi.param = param;
+    bi.rays = rays;
+    bi.seed = seed;
+    bi.instance = instance;
+    return b->add_instance(bi, index);
+}
+
+int csp_batch_clear_instances(csp_batch bh) {
+    CSP_BGUARD(bh);
+    Batch* b = reinterpret_cast<Batch*>(bh);
+    b->inst.clear();
+    b->ran = false;
+    return CSP_OK;
+}
+
+int csp_batch_num_instances(csp_batch bh, uint32_t* count) {
+    CSP_BGUARD(bh);
+    if (!count) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "null output");
+    *count = (uint32_t)reinterpret_cast<Batch*>(bh)->inst.size();
+    return CSP_OK;
+}
+
+int csp_batch_set_tuning(csp_batch bh, int block, int ctas_per_sm, int chunk) {
+    CSP_BGUARD(bh);
+    if (block != 0 && block != 128 && block != 256)
+        return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "block must be 0 (autotune), 128 or 256");
+    if (block != 0 && (ctas_per_sm < 0 || chunk <= 0))
+        return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "bad tuning parameters");
+    reinterpret_cast<Batch*>(bh)->user = csp::BatchTuning{block, ctas_per_sm, block ? chunk : 0};
+    return CSP_OK;
+}
+
+int csp_batch_get_tuning(csp_batch bh, int flat, int* block, int* ctas_per_sm, int* chunk) {
+    CSP_BGUARD(bh);
+    const csp::BatchTuning& t = reinterpret_cast<Batch*>(bh)->used[flat ? 0 : 1];
+    if (block) *block = t.block;
+    if (ctas_per_sm) *ctas_per_sm = t.ctas_per_sm;
+    if (chunk) *chunk = t.chunk;
+    return CSP_OK;
+}
+
+int csp_batch_run(csp_batch bh) {
+    CSP_BGUARD(bh);
+    return reinterpret_cast<Batch*>(bh)->run();
+}
+
+int csp_batch_get_flux(csp_batch bh, uint32_t index, uint32_t* counts, double dni, double* flux) {
+    CSP_BGUARD(bh);
+    const Batch* b = reinterpret_cast<Batch*>(bh);
+    const uint32_t* c = nullptr;
+    const csp::SunFrame* f = nullptr;
+    int rc = b->result(index, &c, nullptr, &f);
+    if (rc) return rc;
+    const size_t nb = (size_t)b->nx * b->ny;
+    if (counts) std::memcpy(counts, c, nb * sizeof(uint32_t));
+    if (flux) {
+        const csp_element& rcv = b->elements_of(index)[b->count_of(index) - 1];
+        csp::counts_to_flux(c, nb, dni, csp::sun_plane_area(*f), b->inst[index].rays,
+                            csp::flux_bin_area(rcv, b->nx, b->ny), flux);
+    }
+    return CSP_OK;
+}
+
+int csp_batch_get_stats(csp_batch bh, uint32_t index, uint64_t* stats) {
+    CSP_BGUARD(bh);
+    if (!stats) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "null output");
+    const Batch* b = reinterpret_cast<Batch*>(bh);
+    const unsigned long long* s = nullptr;
+    int rc = b->result(index, nullptr, &s, nullptr);
+    if (rc) return rc;
+    stats[0] = b->inst[index].rays;
+    for (int k = 1; k < 4; ++k) stats[k] = s[k];
+    return CSP_OK;
+}
+
+int csp_batch_get_sun_plane(csp_batch bh, uint32_t index, float* out) {
+    CSP_BGUARD(bh);
+    if (!out) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "null output");
+    const Batch* b = reinterpret_cast<Batch*>(bh);
+    const csp::SunFrame* f = nullptr;
+    int rc = b->result(index, nullptr, nullptr, &f);
+    if (rc) return rc;
+    const float v[16] = {f->s_d.x, f->s_d.y, f->s_d.z, f->v0.x, f->v0.y, f->v0.z, f->v1.x, f->v1.y,
+                         f->v1.z,  f->v2.x,  f->v2.y,  f->v2.z, f->v3.x, f->v3.y, f->v3.z, f->s_d.w};
+    std::memcpy(out, v, sizeof(v));
+    return CSP_OK;
+}
+
+int csp_batch_get_timing(csp_batch bh, double* setup_s, double* trace_s) {
+    CSP_BGUARD(bh);
+    const Batch* b = reinterpret_cast<Batch*>(bh);
+    if (setup_s) *setup_s = b->time_setup;
+    if (trace_s) *trace_s = b->time_trace;
+    return CSP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,88 @@
+// csp_batch.h -- state behind one csp_batch handle (batched multi-instance tracing).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "csp_c_api.h"
+#include "csp_kernels.cuh"
+#include "csp_scene.h"
+
+namespace csp {
+
+struct BScene {
+    std::vector<csp_element> elements;
+    HostScene base;         // element records + BVH topology of the scene's own poses
+    Node* d_topo = nullptr; // topology on the device (links; boxes of the scene's own poses)
+    bool flat = false;      // <= kFlatListMax elements: shared-memory element list kernel
+};
+
+struct BInst {
+    uint32_t scene = 0;
+    std::vector<csp_element> poses;  // empty: the scene's own elements
+    double sun[3] = {0, 0, 1};
+    int shape = CSP_SUN_PILLBOX;
+    double param = 0.0;
+    uint64_t rays = 0, seed = 0;
+    uint32_t instance = 0;
+};
+
+// Byte offsets of one instance's arrays in the device arena (and the staging image).
+struct Place {
+    size_t prims = 0, optics = 0, aabbs = 0, prune = 0, nodes = 0, sun = 0, counts = 0, stats = 0;
+    int group = 0;  // 0 small-scene kernel, 1 BVH kernel
+    int slot = 0;   // index within the group
+};
+
+struct Batch {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    uint32_t nx = 100, ny = 100;
+    std::vector<BScene> scenes;
+    std::vector<BInst> inst;
+    BatchTuning user{0, 0, 0};  // block 0: autotune
+    BatchTuning used[2] = {{128, 0, 4}, {128, 0, 4}};
+
+    unsigned char* d_arena = nullptr;
+    size_t arena_cap = 0;
+    unsigned char* h_stage = nullptr;  // pinned image of the upload region
+    size_t stage_cap = 0;
+    unsigned char* h_result = nullptr;  // pinned copy of the download region
+    size_t result_cap = 0;
+
+    std::vector<Place> place;
+    size_t up_bytes = 0, zero_off = 0, zero_bytes = 0, res_off = 0, res_bytes = 0;
+    size_t desc_off[2] = {0, 0}, tb_off[2] = {0, 0}, refit_off = 0, sunjob_off = 0, counter_off = 0;
+    int n_group[2] = {0, 0};
+    int max_nodes = 0;
+
+    cudaGraphExec_t graph = nullptr;
+    std::vector<uint64_t> graph_sig;
+    bool ran = false;
+    double time_setup = 0.0, time_trace = 0.0;
+
+    ~Batch();
+    void release();
+    int ensure_stream();
+    int add_scene(const csp_element* el, uint32_t n, uint32_t* id);
+    int add_instance(const BInst& bi, uint32_t* index);
+    const csp_element* elements_of(size_t i) const;
+    uint32_t count_of(size_t i) const;
+    int layout();
+    int fill_instance(size_t i, HostScene& scratch, std::string& err);
+    void fill_descs(const int block[2], double sample, std::vector<InstanceDesc>* desc, std::vector<uint64_t>* tb);
+    void write_descs(const std::vector<InstanceDesc>* desc, const std::vector<uint64_t>* tb, unsigned char* img);
+    BatchLaunch launch_of(int g, uint64_t total_tiles, int chunk) const;
+    int enqueue_prefix(cudaStream_t st);
+    int enqueue_scene_setup(cudaStream_t st);
+    int autotune(int g, BatchTuning& best);
+    int resolve_tuning();
+    int run();
+    int result(uint32_t index, const uint32_t** counts, const unsigned long long** stats, const SunFrame** sun) const;
+};
+
+}  // namespace csp

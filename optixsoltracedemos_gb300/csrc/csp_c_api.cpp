@@ -64,6 +64,11 @@ void System::release() {
     cudaFree(d_sun);
     cudaFree(d_hits);
     cudaFree(d_ids);
+    cudaFree(d_flux);
+    cudaFree(d_fstats);
+    d_flux = nullptr;
+    d_fstats = nullptr;
+    cap_flux = 0;
     d_nodes = nullptr;
     d_prims = nullptr;
     d_optics = nullptr;
@@ -245,6 +250,55 @@ int System::run_to_host(float* dst, uint32_t* ids_dst) {
     if (sync_rc) return sync_rc;
     if (sync_rc2) return sync_rc2;
     time_trace = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return CSP_OK;
+}
+
+double sun_plane_area(const SunFrame& f) {
+    const double a[3] = {(double)f.v1.x - f.v0.x, (double)f.v1.y - f.v0.y, (double)f.v1.z - f.v0.z};
+    const double b[3] = {(double)f.v3.x - f.v0.x, (double)f.v3.y - f.v0.y, (double)f.v3.z - f.v0.z};
+    const double c[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+    return std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+}
+
+void counts_to_flux(const uint32_t* counts, size_t n, double dni, double sun_area, uint64_t rays, double bin_area,
+                    double* flux) {
+    const double per = (rays > 0 && bin_area > 0) ? dni * sun_area / (double)rays / bin_area : 0.0;
+    for (size_t i = 0; i < n; ++i) flux[i] = counts[i] * per;
+}
+
+int System::flux_map(uint32_t nx, uint32_t ny, uint32_t* counts, double dni, double* flux) {
+    if (!initialized || !d_hits) return fail(CSP_ERR_STATE, "flux map before initialize()/run()");
+    if (nx == 0 || ny == 0 || (uint64_t)nx * ny > (1u << 26)) return fail(CSP_ERR_INVALID_ARGUMENT, "bad flux grid");
+    const size_t nb = (size_t)nx * ny;
+    int rc;
+    if (nb > cap_flux) {
+        cudaFree(d_flux);
+        d_flux = nullptr;
+        cap_flux = 0;
+        if ((rc = cuda_status(cudaMalloc((void**)&d_flux, nb * sizeof(uint32_t)), "cudaMalloc flux map"))) return rc;
+        cap_flux = nb;
+    }
+    if (!d_fstats && (rc = cuda_status(cudaMalloc((void**)&d_fstats, 4 * sizeof(unsigned long long)), "cudaMalloc")))
+        return rc;
+    FluxTarget F;
+    flux_target(elements.back(), nx, ny, F);
+    F.counts = d_flux;
+    F.stats = d_fstats;
+    if ((rc = cuda_status(cudaMemsetAsync(d_flux, 0, nb * sizeof(uint32_t), stream), "memset flux"))) return rc;
+    if ((rc = cuda_status(cudaMemsetAsync(d_fstats, 0, 4 * sizeof(unsigned long long), stream), "memset"))) return rc;
+    if ((rc = cuda_status(launch_flux_records(d_hits, num_rays * kMaxDepth, F, stream), "flux_records_kernel")))
+        return rc;
+    std::vector<uint32_t> host(nb);
+    if ((rc = cuda_status(cudaMemcpyAsync(host.data(), d_flux, nb * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream),
+                          "D2H flux map")))
+        return rc;
+    SunFrame f;
+    if ((rc = cuda_status(cudaMemcpyAsync(&f, d_sun, sizeof(f), cudaMemcpyDeviceToHost, stream), "D2H sun frame")))
+        return rc;
+    if ((rc = cuda_status(cudaStreamSynchronize(stream), "flux map"))) return rc;
+    if (counts) std::copy(host.begin(), host.end(), counts);
+    if (flux)
+        counts_to_flux(host.data(), nb, dni, sun_plane_area(f), num_rays, flux_bin_area(elements.back(), nx, ny), flux);
     return CSP_OK;
 }
 
@@ -440,6 +494,23 @@ int csp_element_frame(const csp_element* e, double* euler, double* g2l, double* 
     if (g2l) std::memcpy(g2l, G, sizeof G);
     if (aabb_lo) std::memcpy(aabb_lo, lo, sizeof lo);
     if (aabb_hi) std::memcpy(aabb_hi, hi, sizeof hi);
+    return CSP_OK;
+}
+
+int csp_flux_map(csp_handle h, uint32_t nx, uint32_t ny, uint32_t* counts, double dni, double* flux) {
+    CSP_GUARD(h);
+    return reinterpret_cast<System*>(h)->flux_map(nx, ny, counts, dni, flux);
+}
+
+int csp_flux_target(const csp_element* rcv, uint32_t nx, uint32_t ny, float* out) {
+    if (!rcv || !out) return fail(CSP_ERR_INVALID_ARGUMENT, "null argument");
+    if (nx == 0 || ny == 0) return fail(CSP_ERR_INVALID_ARGUMENT, "bad flux grid");
+    csp::FluxTarget F;
+    csp::flux_target(*rcv, nx, ny, F);
+    const float v[20] = {F.o.x, F.o.y, F.o.z, F.x.x, F.x.y, F.x.z, F.y.x, F.y.y, F.y.z, F.z.x,
+                         F.z.y, F.z.z, F.hx,  F.hy,  F.kx,  F.ky,  F.keep, (float)F.kind,
+                         (float)csp::flux_bin_area(*rcv, nx, ny), 0.f};
+    std::memcpy(out, v, sizeof(v));
     return CSP_OK;
 }
 

@@ -1,711 +1,64 @@
-// csp_kernels.cu -- sm_103a kernels of the trace path.
+// csp_kernels.cu -- sm_103a kernels of the single-scene trace path.
 //
-// Built with -fmad=false (plus IEEE division and square root): every expression below rounds
-// exactly as written, which is what makes the hit records bit-identical to the host restatement of
-// the reference.  Fused multiply-adds appear only as explicit fmaf() calls in csp_math.cuh.
+// Built with -fmad=false (plus IEEE division and square root): every expression rounds exactly as
+// written, which is what makes the hit records bit-identical to the host restatement of the
+// reference.  Fused multiply-adds appear only as explicit fmaf() calls in csp_math.cuh.
 //
 // Kernel map (reference counterpart in parentheses, paths inside the reference project):
-//   prepare_sun_kernel  sun-plane distance, u/v bounds, parallelogram, cone frame
-//                       (lib/sun_utils.cu:53-179, lib/geometry_manager.cpp:97-148, cuda/sun.cu:76-79)
-//   trace_kernel        ray generation (cuda/sun.cu:16-38,72-134), closest-hit search over the
-//                       elements whose AABB the ray overlaps (OptiX traversal + the intersection
-//                       programs of cuda/intersection.cu:47-85,177-296,318-448), shading
-//                       (cuda/materials.cu:26-231) and the hit_point_buffer write.
+//   prepare_sun_kernel   sun-plane distance, u/v bounds, parallelogram, cone frame
+//                        (lib/sun_utils.cu:53-179, lib/geometry_manager.cpp:97-148, cuda/sun.cu:76-79)
+//   trace_kernel         ray generation (cuda/sun.cu:16-38,72-134), closest-hit search over the
+//                        elements whose AABB the ray overlaps (OptiX traversal + the intersection
+//                        programs of cuda/intersection.cu:47-85,177-296,318-448), shading
+//                        (cuda/materials.cu:26-231) and the hit_point_buffer write.
+//   flux_records_kernel  receiver flux map from a dense hit buffer
+//                        (scripts/post_processing/flux_map_calculator.py:135-179)
+// The device functions of the path live in csp_trace.cuh.
 #include <algorithm>
-#include <cfloat>
 
 #include "csp_kernels.cuh"
-#include "csp_math.cuh"
+#include "csp_trace.cuh"
 
 namespace csp {
 namespace {
 
 constexpr int kTraceBlock = 128;
 constexpr int kPrepBlock = 512;
-constexpr float kTwoPi = 2.0f * 3.14159265358979323846f;  // 2.0f * M_PIf, cuda/sun.cu:85
-
-// ------------------------------------------------------------------------------ sun plane -----
-__device__ __forceinline__ float3 corner(const Aabb& b, int k) {
-    return make_float3((k & 1) ? b.hi.x : b.lo.x, (k & 2) ? b.hi.y : b.lo.y, (k & 4) ? b.hi.z : b.lo.z);
-}
-
-template <bool kMax>
-__device__ float block_reduce(float v, float* scratch) {
-    for (int o = 16; o > 0; o >>= 1) {
-        const float w = __shfl_xor_sync(0xffffffffu, v, o);
-        v = kMax ? fmaxf(v, w) : fminf(v, w);
-    }
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __syncthreads();
-    if (lane == 0) scratch[warp] = v;
-    __syncthreads();
-    v = scratch[0];
-    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) v = kMax ? fmaxf(v, scratch[i]) : fminf(v, scratch[i]);
-    return v;
-}
+constexpr int kFluxBlock = 256;
 
 __global__ void __launch_bounds__(kPrepBlock) prepare_sun_kernel(const Aabb* __restrict__ aabbs, int n, float3 s,
                                                                    float tan_pad, int shape, float param,
                                                                    SunFrame* __restrict__ out) {
     __shared__ float scratch[kPrepBlock / 32];
-    // plane distance: max over every AABB corner of |c . s| (and 0), lib/sun_utils.cu:53-104
-    float md = 0.0f;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const Aabb b = aabbs[i];
-        for (int k = 0; k < 8; ++k) md = fmaxf(md, fabsf(dot(corner(b, k), s)));
-    }
-    const float d = block_reduce<true>(md, scratch);
-
-    const float3 axis = (fabsf(s.x) < 0.9f) ? f3(1.0f, 0.0f, 0.0f) : f3(0.0f, 1.0f, 0.0f);
-    const float3 su = normalize(cross(axis, s));
-    const float3 sv = normalize(cross(s, su));
-    const float3 pc = scale(d, s);
-    // u/v bounds padded by |c . s| tan(angle), lib/sun_utils.cu:106-179
-    float umin = FLT_MAX, umax = -FLT_MAX, vmin = FLT_MAX, vmax = -FLT_MAX;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const Aabb b = aabbs[i];
-        for (int k = 0; k < 8; ++k) {
-            const float3 pt = corner(b, k);
-            const float buf = fabsf(dot(pt, s)) * tan_pad;
-            const float3 proj = sub(pt, scale(dot(sub(pt, pc), s), s));
-            const float u = dot(proj, su), v = dot(proj, sv);
-            umin = fminf(umin, u - buf);
-            umax = fmaxf(umax, u + buf);
-            vmin = fminf(vmin, v - buf);
-            vmax = fmaxf(vmax, v + buf);
-        }
-    }
-    umin = block_reduce<false>(umin, scratch);
-    umax = block_reduce<true>(umax, scratch);
-    vmin = block_reduce<false>(vmin, scratch);
-    vmax = block_reduce<true>(vmax, scratch);
-    if (threadIdx.x != 0) return;
-    const float3 ds = scale(d, s);
-    const float3 v0 = add(add(scale(umin, su), scale(vmin, sv)), ds);
-    const float3 v1 = add(add(scale(umax, su), scale(vmin, sv)), ds);
-    const float3 v2 = add(add(scale(umax, su), scale(vmax, sv)), ds);
-    const float3 v3 = add(add(scale(umin, su), scale(vmax, sv)), ds);
-    // cone frame, cuda/sun.cu:76-79 with dir = -normalize(sun_vector) (cuda/sun.cu:106)
-    const float3 w = normalize(neg(normalize(s)));
-    const float3 cu = normalize(cross(fabsf(w.x) > 0.99f ? f3(0.0f, 1.0f, 0.0f) : f3(1.0f, 0.0f, 0.0f), w));
-    const float3 cv = cross(w, cu);
-    SunFrame f;
-    f.s_d = make_float4(s.x, s.y, s.z, d);
-    f.v0 = make_float4(v0.x, v0.y, v0.z, 0.f);
-    const float3 e1 = sub(v1, v0), e2 = sub(v3, v0);
-    f.e1 = make_float4(e1.x, e1.y, e1.z, 0.f);
-    f.e2 = make_float4(e2.x, e2.y, e2.z, 0.f);
-    f.v1 = make_float4(v1.x, v1.y, v1.z, 0.f);
-    f.v2 = make_float4(v2.x, v2.y, v2.z, 0.f);
-    f.v3 = make_float4(v3.x, v3.y, v3.z, 0.f);
-    f.w = make_float4(w.x, w.y, w.z, 0.f);
-    f.u = make_float4(cu.x, cu.y, cu.z, 0.f);
-    f.v = make_float4(cv.x, cv.y, cv.z, 0.f);
-    if (shape == 1) {
-        f.cos_theta = 1.0f;
-        f.sigma = param;
-    } else {
-        float sn, cs;
-        det_sincos(param, sn, cs);  // cosf(half_angle), cuda/sun.cu:82
-        f.cos_theta = cs;
-        f.sigma = 0.0f;
-    }
-    f.tan_pad = tan_pad;
-    f.pad = 0.f;
-    f.shape = shape;
-    f.n_prims = n;
-    f.pad1 = f.pad2 = 0;
-    *out = f;
+    sun_frame_block(aabbs, n, s, tan_pad, shape, param, out, scratch);
 }
 
-// ------------------------------------------------------------------------------ sampling ------
-// Halton radical inverse, cuda/sun.cu:16-24: f /= b; r += f * (i mod b); i /= b, in float.
-__device__ __forceinline__ float halton2(uint64_t i) {
-    if (i < (1ull << 24)) {
-        // every partial sum is a dyadic fraction of at most 24 bits, so the float loop is exact and
-        // equals the bit-reversed index scaled by 2^-32
-        return (float)__brev((uint32_t)i) * 0x1p-32f;
-    }
-    float f = 1.0f, r = 0.0f;
-    while (i > 0) {
-        f = f * 0.5f;  // f / 2 is exact
-        r = r + f * (float)(uint32_t)(i & 1u);
-        i >>= 1;
-    }
-    return r;
-}
-
-__device__ __forceinline__ float halton3(uint64_t i) {
-    float r = 0.0f;
-    int k = 0;
-    while (i >= (1ull << 32)) {
-        const uint64_t q = i / 3u;
-        r = r + c_halton3_f[k++] * (float)(uint32_t)(i - 3u * q);
-        i = q;
-    }
-    uint32_t j = (uint32_t)i;
-    while (j > 0) {
-        const uint32_t q = j / 3u;
-        r = r + c_halton3_f[k++] * (float)(j - 3u * q);
-        j = q;
-    }
-    return r;
-}
-
-// Same fold with its first six steps looked up: t6[m] = halton3(m) for m < 3^6.  For larger i the
-// reference loop continues from exactly that partial sum with the seventh digit (a zero digit adds
-// +0, which leaves the sum unchanged), so the result is identical bit for bit.
-constexpr uint32_t kH3TabDigits = 6, kH3Tab = 729;
-__device__ __forceinline__ float halton3_tab(uint64_t i, const float* __restrict__ t6) {
-    if (i >= (1ull << 32)) return halton3(i);
-    uint32_t j = (uint32_t)i;
-    uint32_t q = j / kH3Tab;
-    float r = t6[j - kH3Tab * q];
-    int k = kH3TabDigits;
-    j = q;
-    while (j > 0) {
-        q = j / 3u;
-        r = r + c_halton3_f[k++] * (float)(j - 3u * q);
-        j = q;
-    }
-    return r;
-}
-
-__device__ __forceinline__ float3 perturb(float3 n, float sigma, float g1, float g2) {
-    const float3 t1 = normalize(cross(fabsf(n.x) > 0.9f ? f3(0.0f, 1.0f, 0.0f) : f3(1.0f, 0.0f, 0.0f), n));
-    const float3 t2 = cross(n, t1);
-    return normalize(add(add(n, scale(sigma * g1, t1)), scale(sigma * g2, t2)));
-}
-
-// ------------------------------------------------------------------------------ intersection --
-// Rectangle_Flat, cuda/intersection.cu:47-85.
-__device__ __forceinline__ bool hit_flat(const Prim& p, float3 o, float3 d, float tmin, float& tout) {
-    const float3 n = xyz(p.a);
-    const float dt = dot(d, n);
-    const float t = (p.a.w - dot(n, o)) / dt;
-    if (!(t > tmin && t < kTmax)) return false;
-    const float3 v = sub(add(o, scale(t, d)), xyz(p.b));
-    const float x = dot(xyz(p.c), v), y = dot(xyz(p.d), v);
-    const float hw = p.b.w, hh = p.c.w;
-    if (x >= -hw && x <= hw && y >= -hh && y <= hh) {
-        tout = t;
-        return true;
-    }
-    return false;
-}
-
-
-// Rectangle_Parabolic, cuda/intersection.cu:318-419.  The reference's bounds test
-// a = x_hit / (L/2.) evaluated in double then rounded to float, |a| <= 1, is decided here as
-// |x_hit| <= L/2 in float: for floats x, h > 0, fl32(fl64(x/h)) > 1 exactly when x > h (if x > h
-// then x >= succ(h), so x/h >= 1 + 2^-24 + 2^-48 and both roundings stay above 1; if x <= h the
-// quotient is <= 1), and symmetrically for -1; NaN passes both forms.
-__device__ __forceinline__ bool hit_parab(const Prim& p, float3 o, float3 d, float tmin, float& tout) {
-    const float3 e1 = xyz(p.a), e2 = xyz(p.b), n = xyz(p.c), c = xyz(p.d);
-    const float cx = p.c.w, cy = p.d.w;
-    const float3 dd = sub(o, c);
-    const float ox = dot(dd, e1), oy = dot(dd, e2), oz = dot(dd, n);
-    const float dx = dot(d, e1), dy = dot(d, e2), dz = dot(d, n);
-    const float A = (cx * 0.5f) * (dx * dx) + (cy * 0.5f) * (dy * dy);
-    const float B = cx * (ox * dx) + cy * (oy * dy) - dz;
-    const float C = (cx * 0.5f) * (ox * ox) + (cy * 0.5f) * (oy * oy) - oz;
-    float t = 0.0f;
-    bool valid = false;
-    if (fabsf(A) < 1e-12f) {
-        t = -C / B;
-        valid = (t > 0.0f);
-    } else {
-        const float disc = B * B - 4.0f * A * C;
-        if (disc >= 0.0f) {
-            const float sq = sqrtf(disc);
-            const float t1 = (-B - sq) / (2.0f * A);
-            const float t2 = (-B + sq) / (2.0f * A);
-            if (t1 > 0.0f && t1 < t2) {
-                t = t1;
-                valid = true;
-            } else if (t2 > 0.0f) {
-                t = t2;
-                valid = true;
-            }
-        }
-    }
-    if (!valid || t < tmin || t > kTmax) return false;
-    const float xh = ox + t * dx, yh = oy + t * dy;
-    const float h1 = p.a.w, h2 = p.b.w;
-    if (xh > h1 || xh < -h1 || yh > h2 || yh < -h2) return false;
-    tout = t;
-    return true;
-}
-
-// World normal the parabolic intersection program reports for a hit at t (cuda/intersection.cu:
-// 354-361 local coordinates again, then :430-436).
-__device__ __forceinline__ float3 parab_normal(const Prim& p, float3 o, float3 d, float t) {
-    const float3 e1 = xyz(p.a), e2 = xyz(p.b), n = xyz(p.c);
-    const float3 dd = sub(o, xyz(p.d));
-    const float ox = dot(dd, e1), oy = dot(dd, e2);
-    const float dx = dot(d, e1), dy = dot(d, e2);
-    const float xh = ox + t * dx, yh = oy + t * dy;
-    const float3 nl = normalize(f3(-p.c.w * xh, -p.d.w * yh, 1.0f));
-    return normalize(add(add(scale(nl.x, e1), scale(nl.y, e2)), scale(nl.z, n)));
-}
-
-// Cylinder_Y with caps, cuda/intersection.cu:177-296.
-__device__ __forceinline__ bool hit_cyl(const Prim& p, float3 o, float3 draw, float tmin, float& tout) {
-    const float3 d = normalize(draw);
-    const float3 lo = sub(o, xyz(p.a));
-    const float3 lx = xyz(p.b), ly = xyz(p.c), lz = xyz(p.d);
-    const float Ox = dot(lo, lx), Oy = dot(lo, ly), Oz = dot(lo, lz);
-    const float Dx = dot(d, lx), Dy = dot(d, ly), Dz = dot(d, lz);
-    const float half = p.b.w, r2 = p.c.w;
-    const float A = Dx * Dx + Dz * Dz;
-    const float B = 2.0f * (Ox * Dx + Oz * Dz);
-    const float C = Ox * Ox + Oz * Oz - r2;
-    const float det = B * B - 4.0f * A * C;
-    const float inval = kTmax + 1.0f;
-    float tc = inval;
-    if (det >= 0.0f) {
-        const float sq = sqrtf(det);
-        const float t1 = (-B - sq) / (2.0f * A);
-        const float t2 = (-B + sq) / (2.0f * A);
-        if (t1 > tmin && t1 < kTmax && fabsf(Oy + t1 * Dy) <= half) tc = t1;
-        else if (t2 > tmin && t2 < kTmax && fabsf(Oy + t2 * Dy) <= half) tc = t2;
-    }
-    float tcap = inval;
-    if (fabsf(Dy) > 1e-6f) {
-        const float tb = (-half - Oy) / Dy;
-        const float bx = Ox + tb * Dx, bz = Oz + tb * Dz;
-        if (tb > tmin && tb < kTmax && bx * bx + bz * bz <= r2) tcap = tb;
-        const float tt = (half - Oy) / Dy;
-        const float tx = Ox + tt * Dx, tz = Oz + tt * Dz;
-        if (tt > tmin && tt < kTmax && tx * tx + tz * tz <= r2) tcap = fminf(tcap, tt);
-    }
-    const float t = fminf(tc, tcap);
-    if (t >= kTmax || t <= tmin) return false;
-    tout = t;
-    return true;
-}
-
-__device__ __forceinline__ bool hit_prim(uint32_t type, const Prim& p, float3 o, float3 d, float tmin, float& t) {
-    if (type == kParabolicMirror) return hit_parab(p, o, d, tmin, t);
-    if (type == kCylReceiver) return hit_cyl(p, o, d, tmin, t);
-    return hit_flat(p, o, d, tmin, t);
-}
-
-__device__ __forceinline__ Prim load_prim(const Prim* prims, uint32_t i) {
-    const float4* q = reinterpret_cast<const float4*>(prims + i);
-    Prim p;
-    p.a = __ldg(q);
-    p.b = __ldg(q + 1);
-    p.c = __ldg(q + 2);
-    p.d = __ldg(q + 3);
-    return p;
-}
-
-// Closest hit among the elements whose AABB the segment [tmin, kTmax] overlaps; equal t keeps the
-// lower element index.  Internal nodes are pruned against the closest hit so far with slack
-// (their boxes bound every surface below them with a margin); leaves test the exact AABB.
-__device__ __forceinline__ int traverse(const Node* __restrict__ nodes, const Prim* __restrict__ prims, float3 o,
-                                        float3 d, float tmin, float& best_t, uint32_t& best_type) {
-    const float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
-    int best = -1;
-    best_t = __int_as_float(0x7f800000);
-    float prune = kTmax;
-    int node = 0;
-    while (node >= 0) {
-        const float4* q = reinterpret_cast<const float4*>(nodes + node);
-        const float4 lo = __ldg(q), hi = __ldg(q + 1);
-        const float t0x = (lo.x - o.x) * inv.x, t1x = (hi.x - o.x) * inv.x;
-        const float t0y = (lo.y - o.y) * inv.y, t1y = (hi.y - o.y) * inv.y;
-        const float t0z = (lo.z - o.z) * inv.z, t1z = (hi.z - o.z) * inv.z;
-        const float tn = fmaxf(tmin, fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z)));
-        const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
-        const uint32_t hitw = __float_as_uint(lo.w);
-        const int miss = __float_as_int(hi.w);
-        if (hitw & kLeafFlag) {
-            if (tn <= fminf(kTmax, tf)) {
-                const uint32_t prim = hitw & kPrimMask;
-                const uint32_t type = (hitw >> kTypeShift) & 7u;
-                float t;
-                if (hit_prim(type, load_prim(prims, prim), o, d, tmin, t) &&
-                    (t < best_t || (t == best_t && (int)prim < best))) {
-                    best = (int)prim;
-                    best_t = t;
-                    best_type = type;
-                    prune = fminf(kTmax, best_t + best_t * 1e-3f + 1e-3f);
-                }
-            }
-            node = miss;
-        } else {
-            node = (tn <= fminf(prune, tf)) ? (int)hitw : miss;
-        }
-    }
-    return best;
-}
-
-// ------------------------------------------------------------------------------ trace ---------
-// Persistent kernel, wavefront inside each CTA.  A CTA walks tiles of kTraceBlock consecutive rays.
-//   phase A (one ray per thread, every ray): sun sample and the cheap, branch-free part of the first
-//     segment; the warp's records (sun point + empty slots) leave as coalesced rows.  Rays with
-//     more to do are pushed into a shared-memory queue (warp ballot + one shared atomic per warp):
-//       small scenes (kFlat, <= kFlatMax elements, all in shared memory): phase A only runs the AABB
-//         slab tests; rays whose segment overlaps some element box are queued with that mask;
-//       BVH scenes: phase A traverses and records the first hit; mirror hits are queued unshaded.
-//   phase B (only on full batches of kTraceBlock queued rays, and on the remainder at the end): the
-//     rest of each queued path -- intersection programs, shading, further segments -- with records
-//     written straight to global memory (their rows were written by phase A of an earlier tile of
-//     this CTA, ordered by the barriers in between).
-// In the heliostat workloads ~10% of rays meet an element; running their intersection programs and
-// shading on full warps instead of inside warps where ~90% of lanes have finished is the point.
-constexpr int kQueueCap = 2 * kTraceBlock;
-constexpr int kFlatMax = 8;
-
-struct Segment {
-    float3 o, d;
-    float tmin;
-    int depth;
-};
-
-// Scene copy in shared memory for kFlat launches.
-struct FlatScene {
-    Prim prim[kFlatMax];
-    Aabb box[kFlatMax];
-    Optics optics[kFlatMax];
-    uint32_t type[kFlatMax];
-    int n;
-};
-
-// AABB culling of the intersection programs (segment [tmin, kTmax] against each element box) for a
-// kFlat scene: bit k set when element k's program has to run.
-__device__ __forceinline__ uint32_t candidates(const FlatScene& fs, float3 o, float3 d, float tmin) {
-    const float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
-    uint32_t mask = 0;
-    const int nb = fs.n;
-#pragma unroll
-    for (int k = 0; k < kFlatMax; ++k) {
-        if (k >= nb) break;
-        const float4 lo = fs.box[k].lo, hi = fs.box[k].hi;
-        const float t0x = (lo.x - o.x) * inv.x, t1x = (hi.x - o.x) * inv.x;
-        const float t0y = (lo.y - o.y) * inv.y, t1y = (hi.y - o.y) * inv.y;
-        const float t0z = (lo.z - o.z) * inv.z, t1z = (hi.z - o.z) * inv.z;
-        const float tn = fmaxf(tmin, fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z)));
-        const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
-        if (tn <= fminf(kTmax, tf)) mask |= 1u << k;
-    }
-    return mask;
-}
-
-// Closest hit among the candidate elements, in ascending index (equal t keeps the lower index).
-__device__ __forceinline__ int closest_in(const FlatScene& fs, uint32_t mask, float3 o, float3 d, float tmin,
-                                          float& best_t, uint32_t& best_type) {
-    int best = -1;
-    best_t = __int_as_float(0x7f800000);
-    while (mask) {
-        const int k = __ffs(mask) - 1;
-        mask &= mask - 1u;
-        float t;
-        if (hit_prim(fs.type[k], fs.prim[k], o, d, tmin, t) && t < best_t) {
-            best = k;
-            best_t = t;
-            best_type = fs.type[k];
-        }
-    }
-    return best;
-}
-
-struct Hit {
-    int best;  // element index, -1 on a miss
-    float t;
-    uint32_t type;
-};
-
-// What the closest-hit program of a hit records: slot depth+1 (mirrors and the cylinder always,
-// below max depth; the flat receiver only from the front, cuda/materials.cu:86-163), and whether a
-// mirror has to be shaded next (cuda/materials.cu:44-60,180-197: only below max depth).
-__device__ __forceinline__ bool classify(const Prim& p, const Segment& g, const Hit& h, float4& rec, int& slot) {
-    slot = -1;
-    const int nd = g.depth + 1;
-    if (nd >= kMaxDepth) return false;
-    const float3 hit = add(g.o, scale(h.t, g.d));
-    if (h.type == kFlatMirror || h.type == kParabolicMirror) {
-        rec = make_float4(1.0f, hit.x, hit.y, hit.z);
-        slot = nd;
-        return true;
-    }
-    if (h.type == kFlatReceiver) {
-        const float3 rn = cross(xyz(p.c), xyz(p.d));
-        if (!(dot(g.d, rn) < 0.0f)) return false;
-    }
-    rec = make_float4(2.0f, hit.x, hit.y, hit.z);
-    slot = nd;
-    return false;
-}
-
-// __closesthit__mirror / __closesthit__mirror__parabolic (cuda/materials.cu:26-84,170-231): normal
-// as the intersection program reports it, faced against the ray, ideal reflection; plus the
-// extensions (Gaussian slope and specularity error, absorption with probability 1 - reflectivity).
-// Returns false when the ray is absorbed.
-__device__ __forceinline__ bool shade_mirror(const TraceArgs& A, uint64_t ray, const Prim& p, const Optics& op,
-                                             const Segment& g, const Hit& h, Segment& next) {
-    const int nd = g.depth + 1;
-    const float3 hit = add(g.o, scale(h.t, g.d));
-    const float3 wn = (h.type == kFlatMirror) ? normalize(xyz(p.a)) : normalize(parab_normal(p, g.o, g.d, h.t));
-    float3 ffn = (dot(neg(g.d), wn) >= 0.0f) ? wn : neg(wn);
-    const bool need_rng = (op.slope > 0.0f) || (op.spec > 0.0f) || !(op.reflectivity >= 1.0f);
-    u32x4 ra = {0u, 0u, 0u, 0u};
-    if (need_rng) ra = draw_block(ray, (uint32_t)nd, 0, A.instance, A.seed);
-    if (op.slope > 0.0f) {
-        float g1, g2;
-        box_muller(u01(ra.y), u01(ra.z), g1, g2);
-        ffn = perturb(ffn, op.slope, g1, g2);
-    }
-    float3 rd = reflect(g.d, ffn);
-    if (op.spec > 0.0f) {
-        const u32x4 rb = draw_block(ray, (uint32_t)nd, 1, A.instance, A.seed);
-        float g1, g2;
-        box_muller(u01(rb.x), u01(rb.y), g1, g2);
-        rd = perturb(normalize(rd), op.spec, g1, g2);
-    }
-    if (need_rng && u01(ra.x) > op.reflectivity) return false;  // absorbed at the mirror
-    next = Segment{hit, rd, kTminBounce, nd};
-    return true;
-}
-
-// Ray generation: cuda/sun.cu:28-38 (Halton point on the sun parallelogram) and :72-91, :106
-// (direction in the sun cone; Gaussian sun as an extension).
-__device__ __forceinline__ Segment generate(const TraceArgs& A, const SunFrame& S, uint64_t ray, const float* t6) {
-    const float hu = halton2(ray), hv = halton3_tab(ray, t6);
-    const float3 pos = add(add(xyz(S.v0), scale(hu, xyz(S.e1))), scale(hv, xyz(S.e2)));
-    const u32x4 r0 = draw_block(ray, 0, 0, A.instance, A.seed);
-    const float3 w = xyz(S.w), cu = xyz(S.u), cv = xyz(S.v);
-    float3 dir;
-    if (S.shape == 1) {
-        float g1, g2;
-        box_muller(u01(r0.x), u01(r0.y), g1, g2);
-        dir = normalize(add(add(w, scale(S.sigma * g1, cu)), scale(S.sigma * g2, cv)));
-    } else {
-        const float rand1 = u01(r0.x), rand2 = u01(r0.y);
-        const float phi = kTwoPi * rand1;
-        const float z = S.cos_theta + (1.0f - S.cos_theta) * rand2;
-        const float r = sqrtf(1.0f - z * z);
-        float sp, cp;
-        det_sincos(phi, sp, cp);
-        dir = normalize(add(scale(r, add(scale(cp, cu), scale(sp, cv))), scale(z, w)));
-    }
-    return Segment{pos, dir, kTminSun, 0};
-}
+template <bool kFlat>
+using PlainCfg = Cfg<kTraceBlock, kFlat, true, false>;
 
 struct TraceSmem {
-    float4 hits[kTraceBlock * kMaxDepth];  // phase A record staging, ray-major per warp
-    uint32_t ids[kTraceBlock * kMaxDepth];
-    float qo[3][kQueueCap], qd[3][kQueueCap], qt[kQueueCap];
-    uint32_t qw[kQueueCap];  // kFlat: candidate mask; BVH: element | type << 28 of the pending mirror hit
-    uint64_t qray[kQueueCap];
-    float t6[kH3Tab];
-    FlatScene flat;
-    SunFrame sun;
-    int qsize;
+    StageSmem<kTraceBlock> stage;
+    CoreSmem<kTraceBlock> core;
 };
 
-// warp-aggregated append of the lanes with `want` set; every lane of the warp must call it
-__device__ __forceinline__ void push(TraceSmem& sm, bool want, uint64_t ray, float3 o, float3 d, float t, uint32_t w) {
-    const unsigned mask = __ballot_sync(0xffffffffu, want);
-    if (mask == 0u) return;
-    const int lane = threadIdx.x & 31;
-    int base = 0;
-    if (lane == __ffs(mask) - 1) base = atomicAdd(&sm.qsize, __popc(mask));
-    base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
-    if (want) {
-        const int k = base + __popc(mask & ((1u << lane) - 1u));
-        sm.qo[0][k] = o.x;
-        sm.qo[1][k] = o.y;
-        sm.qo[2][k] = o.z;
-        sm.qd[0][k] = d.x;
-        sm.qd[1][k] = d.y;
-        sm.qd[2][k] = d.z;
-        sm.qt[k] = t;
-        sm.qw[k] = w;
-        sm.qray[k] = ray;
-    }
-}
-
-__device__ __forceinline__ void store_record(const TraceArgs& A, uint64_t ray, int slot, float4 rec, uint32_t id) {
-    const uint64_t row = (ray - A.ray_begin) * kMaxDepth + (uint64_t)slot;
-    A.hits[row] = rec;
-    if (A.ids) A.ids[row] = id;
-}
-
-// Remainder of a path in phase B, from the closest hit `h` of segment `g`: record, shade, next
-// segment, until the ray misses, is absorbed, ends on the receiver or reaches the depth limit.
-template <bool kFlat>
-__device__ void finish_path(const TraceArgs& A, const TraceSmem& sm, uint64_t ray, Segment g, Hit h) {
-    for (;;) {
-        if (h.best < 0) return;  // __miss__ms, cuda/materials.cu:236-253
-        const Prim p = kFlat ? sm.flat.prim[h.best] : load_prim(A.prims, (uint32_t)h.best);
-        float4 rec;
-        int slot;
-        const bool mirror = classify(p, g, h, rec, slot);
-        if (slot >= 0) store_record(A, ray, slot, rec, (uint32_t)h.best);
-        if (!mirror) return;
-        const Optics op = kFlat ? sm.flat.optics[h.best] : A.optics[h.best];
-        Segment next;
-        if (!shade_mirror(A, ray, p, op, g, h, next)) return;
-        g = next;
-        if (kFlat) {
-            const uint32_t m = candidates(sm.flat, g.o, g.d, g.tmin);
-            h.best = closest_in(sm.flat, m, g.o, g.d, g.tmin, h.t, h.type);
-        } else {
-            h.best = traverse(A.nodes, A.prims, g.o, g.d, g.tmin, h.t, h.type);
-        }
-    }
-}
-
-template <bool kFlat>
-__device__ void drain(const TraceArgs& A, TraceSmem& sm, bool all) {
-    __syncthreads();
-    int qs = sm.qsize;
-    while (qs >= kTraceBlock || (all && qs > 0)) {
-        const int n = min(qs, kTraceBlock);
-        const int base = qs - n;
-        const bool have = (int)threadIdx.x < n;
-        float3 o = f3(0.f, 0.f, 0.f), d = f3(0.f, 0.f, 1.f);
-        float t = 0.f;
-        uint32_t w = 0;
-        uint64_t ray = 0;
-        if (have) {
-            const int k = base + threadIdx.x;
-            o = f3(sm.qo[0][k], sm.qo[1][k], sm.qo[2][k]);
-            d = f3(sm.qd[0][k], sm.qd[1][k], sm.qd[2][k]);
-            t = sm.qt[k];
-            w = sm.qw[k];
-            ray = sm.qray[k];
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) sm.qsize = base;
-        __syncthreads();
-        if (have) {
-            if (kFlat) {
-                // first segment from the sun: intersection programs of the candidate elements
-                const Segment g{o, d, kTminSun, 0};
-                Hit h;
-                h.best = closest_in(sm.flat, w, o, d, kTminSun, h.t, h.type);
-                finish_path<kFlat>(A, sm, ray, g, h);
-            } else {
-                // pending mirror hit of the first segment: its record was written in phase A
-                const Segment g{o, d, kTminSun, 0};
-                const Hit h{(int)(w & kPrimMask), t, w >> kTypeShift};
-                const Prim p = load_prim(A.prims, (uint32_t)h.best);
-                Segment next;
-                if (shade_mirror(A, ray, p, A.optics[h.best], g, h, next)) {
-                    Hit h2;
-                    h2.best = traverse(A.nodes, A.prims, next.o, next.d, next.tmin, h2.t, h2.type);
-                    finish_path<kFlat>(A, sm, ray, next, h2);
-                }
-            }
-        }
-        __syncthreads();
-        qs = sm.qsize;
-    }
-}
-
+// Persistent kernel over the tiles of one launch (static round robin); dense records out.
 template <bool kFlat>
 __global__ void __launch_bounds__(kTraceBlock, 6) trace_kernel(const TraceArgs A) {
+    using C = PlainCfg<kFlat>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TraceSmem& sm = *reinterpret_cast<TraceSmem*>(smem_raw);
-    if (threadIdx.x < sizeof(SunFrame) / 4)
-        reinterpret_cast<uint32_t*>(&sm.sun)[threadIdx.x] = reinterpret_cast<const uint32_t*>(A.sun)[threadIdx.x];
-    for (uint32_t m = threadIdx.x; m < kH3Tab; m += kTraceBlock) sm.t6[m] = halton3(m);
-    if (kFlat && threadIdx.x < kFlatMax) {
-        const int nprim = A.sun->n_prims;
-        const int k = threadIdx.x;
-        if (k < nprim) {
-            // a kFlat scene's nodes are its leaves in element order
-            const Node nd = A.nodes[k];
-            sm.flat.prim[k] = A.prims[k];
-            sm.flat.optics[k] = A.optics[k];
-            sm.flat.box[k].lo = nd.lo;
-            sm.flat.box[k].hi = nd.hi;
-            sm.flat.type[k] = (__float_as_uint(nd.lo.w) >> kTypeShift) & 7u;
-        }
-        if (k == 0) sm.flat.n = min(nprim, kFlatMax);
-    }
-    if (threadIdx.x == 0) sm.qsize = 0;
+    load_instance_smem<C>(A, sm.core);
+    for (uint32_t m = threadIdx.x; m < kH3Tab; m += kTraceBlock) sm.core.t6[m] = halton3(m);
+    if (threadIdx.x == 0) sm.core.qsize = 0;
     __syncthreads();
-
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float4* wh = sm.hits + warp * 32 * kMaxDepth;
-    uint32_t* wi = sm.ids + warp * 32 * kMaxDepth;
-    float4* slot = wh + lane * kMaxDepth;
-    uint32_t* id = wi + lane * kMaxDepth;
+    const Sink none{nullptr, nullptr};
     const uint64_t tiles = (A.count + kTraceBlock - 1) / kTraceBlock;
-
-    for (uint64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        // ---- phase A
-        const uint64_t k = tile * kTraceBlock + threadIdx.x;
-        const uint64_t ray = A.ray_begin + k;
-#pragma unroll
-        for (int s = 0; s < kMaxDepth; ++s) slot[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (A.ids) {
-#pragma unroll
-            for (int s = 0; s < kMaxDepth; ++s) id[s] = kNoElement;
-        }
-        bool want = false;
-        Segment g;
-        float qt = 0.f;
-        uint32_t qw = 0;
-        if (k < A.count) {
-            g = generate(A, sm.sun, ray, sm.t6);
-            slot[0] = make_float4(0.0f, g.o.x, g.o.y, g.o.z);
-            if (kFlat) {
-                qw = candidates(sm.flat, g.o, g.d, g.tmin);
-                want = qw != 0u;
-            } else {
-                Hit h;
-                h.best = traverse(A.nodes, A.prims, g.o, g.d, g.tmin, h.t, h.type);
-                if (h.best >= 0) {
-                    const Prim p = load_prim(A.prims, (uint32_t)h.best);
-                    float4 rec;
-                    int s;
-                    want = classify(p, g, h, rec, s);
-                    if (s >= 0) {
-                        slot[s] = rec;
-                        if (A.ids) id[s] = (uint32_t)h.best;
-                    }
-                    qt = h.t;
-                    qw = (uint32_t)h.best | (h.type << kTypeShift);
-                }
-            }
-        }
-        __syncwarp();
-        push(sm, want, ray, g.o, g.d, qt, qw);
-        // the warp's 32 x 80 B of records leave as 5 fully coalesced 512-byte rows (stride 80 B per
-        // lane in shared memory: the 16-byte stores of each quarter warp hit distinct banks)
-        const uint64_t warp_first = tile * kTraceBlock + (uint64_t)warp * 32;
-        if (warp_first < A.count) {
-            const uint64_t n_rec = min((uint64_t)32, A.count - warp_first) * kMaxDepth;
-            float4* gh = A.hits + warp_first * kMaxDepth;
-#pragma unroll
-            for (int s = 0; s < kMaxDepth; ++s) {
-                const uint32_t e = (uint32_t)(s * 32 + lane);
-                if (e < n_rec) gh[e] = wh[e];
-            }
-            if (A.ids) {
-                uint32_t* gi = A.ids + warp_first * kMaxDepth;
-#pragma unroll
-                for (int s = 0; s < kMaxDepth; ++s) {
-                    const uint32_t e = (uint32_t)(s * 32 + lane);
-                    if (e < n_rec) gi[e] = wi[e];
-                }
-            }
-        }
-        // ---- phase B on full batches
-        drain<kFlat>(A, sm, false);
-    }
-    drain<kFlat>(A, sm, true);
+    for (uint64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) trace_tile<C>(A, none, sm.core, &sm.stage, tile);
+    drain<C>(A, none, sm.core, true);
 }
 
 template <bool kFlat>
-cudaError_t launch_trace_t(const TraceArgs& args, int n_prims, cudaStream_t stream) {
-    (void)n_prims;
+cudaError_t launch_trace_t(const TraceArgs& args, cudaStream_t stream) {
     // persistent grid: every resident CTA slot of the device, never more CTAs than tiles
     int dev = 0, sms = 0, per_sm = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -725,6 +78,23 @@ cudaError_t launch_trace_t(const TraceArgs& args, int n_prims, cudaStream_t stre
     return cudaGetLastError();
 }
 
+// Grid-stride pass over n_records float4 records {stage, x, y, z}: stage-1 records are counted,
+// stage-2 records are counted and binned.
+__global__ void __launch_bounds__(kFluxBlock) flux_records_kernel(const float4* __restrict__ hits,
+                                                                    uint64_t n_records, const FluxTarget F) {
+    __shared__ unsigned long long stat[4];
+    if (threadIdx.x < 4) stat[threadIdx.x] = 0;
+    __syncthreads();
+    const Sink k{&F, stat};
+    for (uint64_t i = blockIdx.x * (uint64_t)kFluxBlock + threadIdx.x; i < n_records;
+         i += (uint64_t)gridDim.x * kFluxBlock) {
+        const float4 r = __ldg(hits + i);
+        if (r.x == 1.0f || r.x == 2.0f) flux_record(k, r);
+    }
+    __syncthreads();
+    if (threadIdx.x < 4 && threadIdx.x > 0 && stat[threadIdx.x]) atomicAdd(F.stats + threadIdx.x, stat[threadIdx.x]);
+}
+
 }  // namespace
 
 cudaError_t launch_prepare_sun(const Aabb* aabbs, int n, float sx, float sy, float sz, float tan_pad, int shape,
@@ -735,8 +105,19 @@ cudaError_t launch_prepare_sun(const Aabb* aabbs, int n, float sx, float sy, flo
 
 cudaError_t launch_trace(const TraceArgs& args, int n_prims, cudaStream_t stream) {
     if (args.count == 0) return cudaSuccess;
-    if (n_prims <= kFlatMax) return launch_trace_t<true>(args, n_prims, stream);
-    return launch_trace_t<false>(args, n_prims, stream);
+    if (n_prims <= kFlatMax) return launch_trace_t<true>(args, stream);
+    return launch_trace_t<false>(args, stream);
+}
+
+cudaError_t launch_flux_records(const float4* hits, uint64_t n_records, const FluxTarget& F, cudaStream_t stream) {
+    if (n_records == 0) return cudaSuccess;
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t blocks = std::min<uint64_t>((n_records + kFluxBlock - 1) / kFluxBlock, (uint64_t)sms * 8);
+    flux_records_kernel<<<(unsigned)blocks, kFluxBlock, 0, stream>>>(hits, n_records, F);
+    return cudaGetLastError();
 }
 
 }  // namespace csp

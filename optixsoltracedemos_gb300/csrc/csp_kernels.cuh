@@ -31,4 +31,62 @@ cudaError_t launch_prepare_sun(const Aabb* aabbs, int n, float sx, float sy, flo
 // hit-record write.  Scenes of up to 8 elements (n_prims) take the shared-memory element list path.
 cudaError_t launch_trace(const TraceArgs& args, int n_prims, cudaStream_t stream);
 
+// Bin the stage-2 records of a dense hit buffer into F.counts and count records into F.stats[1..3]
+// (both zeroed by the caller).
+cudaError_t launch_flux_records(const float4* hits, uint64_t n_records, const FluxTarget& F, cudaStream_t stream);
+
+// ---------------------------------------------------------------------- multi-instance launches --
+// One instance = one scene state (its own prims, optics, node boxes, sun frame) traced for
+// rays [args.ray_begin, args.ray_begin + args.count) with (args.seed, args.instance), its receiver
+// records binned into flux.counts.  Instances of one launch are laid out as consecutive tile
+// ranges; CTAs take chunks of tiles from a global counter.
+struct alignas(16) InstanceDesc {
+    TraceArgs args;       // hits = ids = nullptr
+    FluxTarget flux;
+    uint64_t tile_begin;  // first tile of this instance in the launch
+    int n_prims;
+    int pad[3];
+};
+
+struct BatchLaunch {
+    const InstanceDesc* inst;        // device
+    const uint64_t* tile_begin;      // device, [n_inst + 1]; last entry = total_tiles
+    int n_inst;
+    int chunk;                       // tiles per grab
+    uint64_t total_tiles;
+    unsigned long long* next_tile;   // device work counter, zero before the launch
+};
+
+struct BatchTuning {
+    int block;        // CTA size = tile size: 128 or 256
+    int ctas_per_sm;  // resident CTAs per SM of the persistent grid (<= occupancy limit)
+    int chunk;        // tiles taken per grab
+};
+
+// Bottom-up refit of one BVH topology into per-instance node arrays: leaves get the exact element
+// AABB, internal nodes the union of the pruning boxes of the leaves below them.
+struct RefitJob {
+    const Node* topo;   // node links of the topology (boxes ignored)
+    const Aabb* aabbs;  // exact element AABBs of the instance
+    const Aabb* prune;  // pruning boxes of the instance
+    Node* out;          // [n_nodes]
+    int n_nodes;
+    int pad;
+};
+
+struct SunJob {
+    const Aabb* aabbs;
+    int n;
+    float sx, sy, sz, tan_pad;
+    int shape;
+    float param;
+    SunFrame* out;
+};
+
+cudaError_t launch_refit(const RefitJob* jobs, int n_jobs, int max_nodes, cudaStream_t stream);
+cudaError_t launch_prepare_sun_batch(const SunJob* jobs, int n_jobs, cudaStream_t stream);
+// Occupancy limit of the multi-instance kernel for (flat, block); 0 if the block size is unsupported.
+int batch_occupancy(bool flat, int block);
+cudaError_t launch_trace_batch(const BatchLaunch& L, bool flat, const BatchTuning& t, cudaStream_t stream);
+
 }  // namespace csp

@@ -119,6 +119,39 @@ void element_frame(const csp_element& e, double euler[3], double G[9], double lo
     }
 }
 
+void flux_target(const csp_element& rcv, uint32_t nx, uint32_t ny, FluxTarget& F) {
+    double euler[3], G[9], lo[3], hi[3];
+    element_frame(rcv, euler, G, lo, hi);
+    F = FluxTarget{};
+    F.o = make_float4((float)rcv.origin[0], (float)rcv.origin[1], (float)rcv.origin[2], 0.f);
+    F.x = make_float4((float)G[0], (float)G[1], (float)G[2], 0.f);
+    F.y = make_float4((float)G[3], (float)G[4], (float)G[5], 0.f);
+    F.z = make_float4((float)G[6], (float)G[7], (float)G[8], 0.f);
+    F.nx = (int)nx;
+    F.ny = (int)ny;
+    const double w = rcv.width, h = rcv.height;
+    F.hy = (float)(h / 2.0);
+    F.ky = (float)((double)ny / h);
+    if (rcv.surface == CSP_SURFACE_CYLINDER) {
+        const double r = w / 2.0, half = h / 2.0;
+        F.kind = kFluxCylinder;
+        F.hx = 0.f;
+        F.kx = (float)((double)nx / (2.0 * M_PI));
+        F.keep = (float)(half - 1e-4 * std::max(half, r));
+    } else {
+        F.kind = kFluxFlat;
+        F.hx = (float)(w / 2.0);
+        F.kx = (float)((double)nx / w);
+        F.keep = FLT_MAX;
+    }
+}
+
+double flux_bin_area(const csp_element& rcv, uint32_t nx, uint32_t ny) {
+    const double w = rcv.width, h = rcv.height;
+    if (rcv.surface == CSP_SURFACE_CYLINDER) return (2.0 * M_PI * (w / 2.0) / nx) * (h / ny);
+    return (w / nx) * (h / ny);
+}
+
 void sun_vector_f(const double d[3], float out[3]) {
     const double len = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
     double n[3] = {0, 0, 0};

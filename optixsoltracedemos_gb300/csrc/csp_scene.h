@@ -40,6 +40,11 @@ void refit_bvh(HostScene& s);
 // y, z axes in world space) and exact double AABB of one element.
 void element_frame(const csp_element& e, double euler[3], double G[9], double lo[3], double hi[3]);
 
+// Flux map target of a receiver element for an nx x ny grid (counts and stats pointers left null),
+// and the area of one bin in m^2 (flat: (w/nx)(h/ny); cylinder: (2 pi r/nx)(h/ny)).
+void flux_target(const csp_element& rcv, uint32_t nx, uint32_t ny, FluxTarget& F);
+double flux_bin_area(const csp_element& rcv, uint32_t nx, uint32_t ny);
+
 // normalized sun vector in double, cast to float (SolTraceSystem::initialize,
 // lib/soltrace_system.cpp:81-85)
 void sun_vector_f(const double d[3], float out[3]);

@@ -37,6 +37,9 @@ struct System {
     SunFrame* d_sun = nullptr;
     float4* d_hits = nullptr;
     uint32_t* d_ids = nullptr;
+    uint32_t* d_flux = nullptr;              // csp_flux_map counts
+    unsigned long long* d_fstats = nullptr;  // [4]
+    size_t cap_flux = 0;
     size_t cap_nodes = 0, cap_prims = 0, cap_optics = 0, cap_aabbs = 0;
     uint64_t cap_rays = 0;
     bool ids_allocated = false;
@@ -61,6 +64,14 @@ struct System {
     int trace_async(cudaStream_t st);
     int run();
     int run_to_host(float* dst, uint32_t* ids);
+    int flux_map(uint32_t nx, uint32_t ny, uint32_t* counts, double dni, double* flux);
 };
+
+// |(v1 - v0) x (v3 - v0)| of a sun frame, in double
+double sun_plane_area(const SunFrame& f);
+
+// flux = counts * dni * sun area / rays / bin area
+void counts_to_flux(const uint32_t* counts, size_t n, double dni, double sun_area, uint64_t rays, double bin_area,
+                    double* flux);
 
 }  // namespace csp

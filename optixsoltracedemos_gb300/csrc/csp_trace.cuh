@@ -1,0 +1,792 @@
+// csp_trace.cuh -- device side of the trace path, shared by the single-scene kernel
+// (csp_kernels.cu) and the multi-instance kernel (csp_batch.cu).
+//
+// Everything here is compiled with -fmad=false and IEEE division/sqrt: expressions round exactly as
+// written, which keeps records bit-identical to the host restatement of the reference.
+//
+// Reference counterparts (paths inside the reference project):
+//   generate            ray generation, cuda/sun.cu:16-38 (Halton point), :72-91,106 (cone)
+//   hit_flat/parab/cyl  intersection programs, cuda/intersection.cu:47-85, 318-448, 177-296
+//   traverse            OptiX traversal: closest hit among the elements whose AABB the ray overlaps
+//   classify/shade      closest-hit programs, cuda/materials.cu:26-231; miss program :236-253
+//
+// Wavefront inside each CTA (kB threads, one tile = kB consecutive rays of one instance):
+//   phase A (one ray per thread, every ray): sun sample and the cheap, branch-free part of the first
+//     segment.  Rays with more to do are pushed into a shared-memory queue (warp ballot + one shared
+//     atomic per warp):
+//       small scenes (kFlat, <= kFlatMax elements, all in shared memory): phase A only runs the AABB
+//         slab tests; rays whose segment overlaps some element box are queued with that mask;
+//       BVH scenes: phase A traverses and records the first hit; mirror hits are queued unshaded.
+//   phase B (only on full batches of kB queued rays, and on the remainder at the end): the rest of
+//     each queued path -- intersection programs, shading, further segments.
+// In the heliostat workloads ~10% of rays meet an element; running their intersection programs and
+// shading on full warps instead of inside warps where ~90% of lanes have finished is the point.
+//
+// Output sinks (compile-time):
+//   kDense  the reference's hit_point_buffer: 5 float4 records per ray (+ optional element ids).
+//           Phase A stages the warp's records in shared memory and writes them as coalesced rows;
+//           phase B writes its records straight to global memory (their rows were written by phase A
+//           of an earlier tile of this CTA, ordered by the barriers in between).
+//   kFlux   receiver records are binned into the instance's flux map in the shading stage (global
+//           reductions), with per-instance record counters; nothing per ray leaves the SM.
+#pragma once
+
+#include <cfloat>
+
+#include "csp_kernels.cuh"
+#include "csp_math.cuh"
+
+namespace csp {
+namespace {
+
+constexpr float kTwoPi = 2.0f * 3.14159265358979323846f;  // 2.0f * M_PIf, cuda/sun.cu:85
+constexpr float kTwoPiF = 0x1.921fb6p+2f;                  // fl32(2 pi), flux angle wrap
+constexpr int kFlatMax = 8;
+constexpr uint32_t kH3TabDigits = 6, kH3Tab = 729;
+
+template <int kB_, bool kFlat_, bool kDense_, bool kFlux_>
+struct Cfg {
+    static constexpr int kB = kB_;        // CTA size = tile size (rays)
+    static constexpr int kQ = 2 * kB_;    // queue capacity: < kB left after a drain + kB pushes
+    static constexpr bool kFlat = kFlat_;
+    static constexpr bool kDense = kDense_;
+    static constexpr bool kFlux = kFlux_;
+};
+
+// ------------------------------------------------------------------------------ sun plane -----
+__device__ __forceinline__ float3 corner(const Aabb& b, int k) {
+    return make_float3((k & 1) ? b.hi.x : b.lo.x, (k & 2) ? b.hi.y : b.lo.y, (k & 4) ? b.hi.z : b.lo.z);
+}
+
+template <bool kMax>
+__device__ float block_reduce(float v, float* scratch) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const float w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = kMax ? fmaxf(v, w) : fminf(v, w);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) scratch[warp] = v;
+    __syncthreads();
+    v = scratch[0];
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) v = kMax ? fmaxf(v, scratch[i]) : fminf(v, scratch[i]);
+    return v;
+}
+
+// One block computes the sun frame of one scene: plane distance, u/v bounds, parallelogram
+// (lib/sun_utils.cu:53-179, lib/geometry_manager.cpp:97-148) and cone frame (cuda/sun.cu:76-79).
+// `scratch` holds blockDim.x / 32 floats.
+__device__ void sun_frame_block(const Aabb* __restrict__ aabbs, int n, float3 s, float tan_pad, int shape,
+                                float param, SunFrame* __restrict__ out, float* scratch) {
+    // plane distance: max over every AABB corner of |c . s| (and 0), lib/sun_utils.cu:53-104
+    float md = 0.0f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const Aabb b = aabbs[i];
+        for (int k = 0; k < 8; ++k) md = fmaxf(md, fabsf(dot(corner(b, k), s)));
+    }
+    const float d = block_reduce<true>(md, scratch);
+
+    const float3 axis = (fabsf(s.x) < 0.9f) ? f3(1.0f, 0.0f, 0.0f) : f3(0.0f, 1.0f, 0.0f);
+    const float3 su = normalize(cross(axis, s));
+    const float3 sv = normalize(cross(s, su));
+    const float3 pc = scale(d, s);
+    // u/v bounds padded by |c . s| tan(angle), lib/sun_utils.cu:106-179
+    float umin = FLT_MAX, umax = -FLT_MAX, vmin = FLT_MAX, vmax = -FLT_MAX;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const Aabb b = aabbs[i];
+        for (int k = 0; k < 8; ++k) {
+            const float3 pt = corner(b, k);
+            const float buf = fabsf(dot(pt, s)) * tan_pad;
+            const float3 proj = sub(pt, scale(dot(sub(pt, pc), s), s));
+            const float u = dot(proj, su), v = dot(proj, sv);
+            umin = fminf(umin, u - buf);
+            umax = fmaxf(umax, u + buf);
+            vmin = fminf(vmin, v - buf);
+            vmax = fmaxf(vmax, v + buf);
+        }
+    }
+    umin = block_reduce<false>(umin, scratch);
+    umax = block_reduce<true>(umax, scratch);
+    vmin = block_reduce<false>(vmin, scratch);
+    vmax = block_reduce<true>(vmax, scratch);
+    if (threadIdx.x != 0) return;
+    const float3 ds = scale(d, s);
+    const float3 v0 = add(add(scale(umin, su), scale(vmin, sv)), ds);
+    const float3 v1 = add(add(scale(umax, su), scale(vmin, sv)), ds);
+    const float3 v2 = add(add(scale(umax, su), scale(vmax, sv)), ds);
+    const float3 v3 = add(add(scale(umin, su), scale(vmax, sv)), ds);
+    // cone frame, cuda/sun.cu:76-79 with dir = -normalize(sun_vector) (cuda/sun.cu:106)
+    const float3 w = normalize(neg(normalize(s)));
+    const float3 cu = normalize(cross(fabsf(w.x) > 0.99f ? f3(0.0f, 1.0f, 0.0f) : f3(1.0f, 0.0f, 0.0f), w));
+    const float3 cv = cross(w, cu);
+    SunFrame f;
+    f.s_d = make_float4(s.x, s.y, s.z, d);
+    f.v0 = make_float4(v0.x, v0.y, v0.z, 0.f);
+    const float3 e1 = sub(v1, v0), e2 = sub(v3, v0);
+    f.e1 = make_float4(e1.x, e1.y, e1.z, 0.f);
+    f.e2 = make_float4(e2.x, e2.y, e2.z, 0.f);
+    f.v1 = make_float4(v1.x, v1.y, v1.z, 0.f);
+    f.v2 = make_float4(v2.x, v2.y, v2.z, 0.f);
+    f.v3 = make_float4(v3.x, v3.y, v3.z, 0.f);
+    f.w = make_float4(w.x, w.y, w.z, 0.f);
+    f.u = make_float4(cu.x, cu.y, cu.z, 0.f);
+    f.v = make_float4(cv.x, cv.y, cv.z, 0.f);
+    if (shape == 1) {
+        f.cos_theta = 1.0f;
+        f.sigma = param;
+    } else {
+        float sn, cs;
+        det_sincos(param, sn, cs);  // cosf(half_angle), cuda/sun.cu:82
+        f.cos_theta = cs;
+        f.sigma = 0.0f;
+    }
+    f.tan_pad = tan_pad;
+    f.pad = 0.f;
+    f.shape = shape;
+    f.n_prims = n;
+    f.pad1 = f.pad2 = 0;
+    *out = f;
+}
+
+// ------------------------------------------------------------------------------ sampling ------
+// Halton radical inverse, cuda/sun.cu:16-24: f /= b; r += f * (i mod b); i /= b, in float.
+__device__ __forceinline__ float halton2(uint64_t i) {
+    if (i < (1ull << 24)) {
+        // every partial sum is a dyadic fraction of at most 24 bits, so the float loop is exact and
+        // equals the bit-reversed index scaled by 2^-32
+        return (float)__brev((uint32_t)i) * 0x1p-32f;
+    }
+    float f = 1.0f, r = 0.0f;
+    while (i > 0) {
+        f = f * 0.5f;  // f / 2 is exact
+        r = r + f * (float)(uint32_t)(i & 1u);
+        i >>= 1;
+    }
+    return r;
+}
+
+__device__ __forceinline__ float halton3(uint64_t i) {
+    float r = 0.0f;
+    int k = 0;
+    while (i >= (1ull << 32)) {
+        const uint64_t q = i / 3u;
+        r = r + c_halton3_f[k++] * (float)(uint32_t)(i - 3u * q);
+        i = q;
+    }
+    uint32_t j = (uint32_t)i;
+    while (j > 0) {
+        const uint32_t q = j / 3u;
+        r = r + c_halton3_f[k++] * (float)(j - 3u * q);
+        j = q;
+    }
+    return r;
+}
+
+// Same fold with its first six steps looked up: t6[m] = halton3(m) for m < 3^6.  For larger i the
+// reference loop continues from exactly that partial sum with the seventh digit (a zero digit adds
+// +0, which leaves the sum unchanged), so the result is identical bit for bit.
+__device__ __forceinline__ float halton3_tab(uint64_t i, const float* __restrict__ t6) {
+    if (i >= (1ull << 32)) return halton3(i);
+    uint32_t j = (uint32_t)i;
+    uint32_t q = j / kH3Tab;
+    float r = t6[j - kH3Tab * q];
+    int k = kH3TabDigits;
+    j = q;
+    while (j > 0) {
+        q = j / 3u;
+        r = r + c_halton3_f[k++] * (float)(j - 3u * q);
+        j = q;
+    }
+    return r;
+}
+
+__device__ __forceinline__ float3 perturb(float3 n, float sigma, float g1, float g2) {
+    const float3 t1 = normalize(cross(fabsf(n.x) > 0.9f ? f3(0.0f, 1.0f, 0.0f) : f3(1.0f, 0.0f, 0.0f), n));
+    const float3 t2 = cross(n, t1);
+    return normalize(add(add(n, scale(sigma * g1, t1)), scale(sigma * g2, t2)));
+}
+
+// ------------------------------------------------------------------------------ intersection --
+// Rectangle_Flat, cuda/intersection.cu:47-85.
+__device__ __forceinline__ bool hit_flat(const Prim& p, float3 o, float3 d, float tmin, float& tout) {
+    const float3 n = xyz(p.a);
+    const float dt = dot(d, n);
+    const float t = (p.a.w - dot(n, o)) / dt;
+    if (!(t > tmin && t < kTmax)) return false;
+    const float3 v = sub(add(o, scale(t, d)), xyz(p.b));
+    const float x = dot(xyz(p.c), v), y = dot(xyz(p.d), v);
+    const float hw = p.b.w, hh = p.c.w;
+    if (x >= -hw && x <= hw && y >= -hh && y <= hh) {
+        tout = t;
+        return true;
+    }
+    return false;
+}
+
+// Rectangle_Parabolic, cuda/intersection.cu:318-419.  The reference's bounds test
+// a = x_hit / (L/2.) evaluated in double then rounded to float, |a| <= 1, is decided here as
+// |x_hit| <= L/2 in float: for floats x, h > 0, fl32(fl64(x/h)) > 1 exactly when x > h (if x > h
+// then x >= succ(h), so x/h >= 1 + 2^-24 + 2^-48 and both roundings stay above 1; if x <= h the
+// quotient is <= 1), and symmetrically for -1; NaN passes both forms.
+__device__ __forceinline__ bool hit_parab(const Prim& p, float3 o, float3 d, float tmin, float& tout) {
+    const float3 e1 = xyz(p.a), e2 = xyz(p.b), n = xyz(p.c), c = xyz(p.d);
+    const float cx = p.c.w, cy = p.d.w;
+    const float3 dd = sub(o, c);
+    const float ox = dot(dd, e1), oy = dot(dd, e2), oz = dot(dd, n);
+    const float dx = dot(d, e1), dy = dot(d, e2), dz = dot(d, n);
+    const float A = (cx * 0.5f) * (dx * dx) + (cy * 0.5f) * (dy * dy);
+    const float B = cx * (ox * dx) + cy * (oy * dy) - dz;
+    const float C = (cx * 0.5f) * (ox * ox) + (cy * 0.5f) * (oy * oy) - oz;
+    float t = 0.0f;
+    bool valid = false;
+    if (fabsf(A) < 1e-12f) {
+        t = -C / B;
+        valid = (t > 0.0f);
+    } else {
+        const float disc = B * B - 4.0f * A * C;
+        if (disc >= 0.0f) {
+            const float sq = sqrtf(disc);
+            const float t1 = (-B - sq) / (2.0f * A);
+            const float t2 = (-B + sq) / (2.0f * A);
+            if (t1 > 0.0f && t1 < t2) {
+                t = t1;
+                valid = true;
+            } else if (t2 > 0.0f) {
+                t = t2;
+                valid = true;
+            }
+        }
+    }
+    if (!valid || t < tmin || t > kTmax) return false;
+    const float xh = ox + t * dx, yh = oy + t * dy;
+    const float h1 = p.a.w, h2 = p.b.w;
+    if (xh > h1 || xh < -h1 || yh > h2 || yh < -h2) return false;
+    tout = t;
+    return true;
+}
+
+// World normal the parabolic intersection program reports for a hit at t (cuda/intersection.cu:
+// 354-361 local coordinates again, then :430-436).
+__device__ __forceinline__ float3 parab_normal(const Prim& p, float3 o, float3 d, float t) {
+    const float3 e1 = xyz(p.a), e2 = xyz(p.b), n = xyz(p.c);
+    const float3 dd = sub(o, xyz(p.d));
+    const float ox = dot(dd, e1), oy = dot(dd, e2);
+    const float dx = dot(d, e1), dy = dot(d, e2);
+    const float xh = ox + t * dx, yh = oy + t * dy;
+    const float3 nl = normalize(f3(-p.c.w * xh, -p.d.w * yh, 1.0f));
+    return normalize(add(add(scale(nl.x, e1), scale(nl.y, e2)), scale(nl.z, n)));
+}
+
+// Cylinder_Y with caps, cuda/intersection.cu:177-296.
+__device__ __forceinline__ bool hit_cyl(const Prim& p, float3 o, float3 draw, float tmin, float& tout) {
+    const float3 d = normalize(draw);
+    const float3 lo = sub(o, xyz(p.a));
+    const float3 lx = xyz(p.b), ly = xyz(p.c), lz = xyz(p.d);
+    const float Ox = dot(lo, lx), Oy = dot(lo, ly), Oz = dot(lo, lz);
+    const float Dx = dot(d, lx), Dy = dot(d, ly), Dz = dot(d, lz);
+    const float half = p.b.w, r2 = p.c.w;
+    const float A = Dx * Dx + Dz * Dz;
+    const float B = 2.0f * (Ox * Dx + Oz * Dz);
+    const float C = Ox * Ox + Oz * Oz - r2;
+    const float det = B * B - 4.0f * A * C;
+    const float inval = kTmax + 1.0f;
+    float tc = inval;
+    if (det >= 0.0f) {
+        const float sq = sqrtf(det);
+        const float t1 = (-B - sq) / (2.0f * A);
+        const float t2 = (-B + sq) / (2.0f * A);
+        if (t1 > tmin && t1 < kTmax && fabsf(Oy + t1 * Dy) <= half) tc = t1;
+        else if (t2 > tmin && t2 < kTmax && fabsf(Oy + t2 * Dy) <= half) tc = t2;
+    }
+    float tcap = inval;
+    if (fabsf(Dy) > 1e-6f) {
+        const float tb = (-half - Oy) / Dy;
+        const float bx = Ox + tb * Dx, bz = Oz + tb * Dz;
+        if (tb > tmin && tb < kTmax && bx * bx + bz * bz <= r2) tcap = tb;
+        const float tt = (half - Oy) / Dy;
+        const float tx = Ox + tt * Dx, tz = Oz + tt * Dz;
+        if (tt > tmin && tt < kTmax && tx * tx + tz * tz <= r2) tcap = fminf(tcap, tt);
+    }
+    const float t = fminf(tc, tcap);
+    if (t >= kTmax || t <= tmin) return false;
+    tout = t;
+    return true;
+}
+
+__device__ __forceinline__ bool hit_prim(uint32_t type, const Prim& p, float3 o, float3 d, float tmin, float& t) {
+    if (type == kParabolicMirror) return hit_parab(p, o, d, tmin, t);
+    if (type == kCylReceiver) return hit_cyl(p, o, d, tmin, t);
+    return hit_flat(p, o, d, tmin, t);
+}
+
+__device__ __forceinline__ Prim load_prim(const Prim* prims, uint32_t i) {
+    const float4* q = reinterpret_cast<const float4*>(prims + i);
+    Prim p;
+    p.a = __ldg(q);
+    p.b = __ldg(q + 1);
+    p.c = __ldg(q + 2);
+    p.d = __ldg(q + 3);
+    return p;
+}
+
+// Closest hit among the elements whose AABB the segment [tmin, kTmax] overlaps; equal t keeps the
+// lower element index.  Internal nodes are pruned against the closest hit so far with slack
+// (their boxes bound every surface below them with a margin); leaves test the exact AABB.
+__device__ __forceinline__ int traverse(const Node* __restrict__ nodes, const Prim* __restrict__ prims, float3 o,
+                                        float3 d, float tmin, float& best_t, uint32_t& best_type) {
+    const float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    int best = -1;
+    best_t = __int_as_float(0x7f800000);
+    float prune = kTmax;
+    int node = 0;
+    while (node >= 0) {
+        const float4* q = reinterpret_cast<const float4*>(nodes + node);
+        const float4 lo = __ldg(q), hi = __ldg(q + 1);
+        const float t0x = (lo.x - o.x) * inv.x, t1x = (hi.x - o.x) * inv.x;
+        const float t0y = (lo.y - o.y) * inv.y, t1y = (hi.y - o.y) * inv.y;
+        const float t0z = (lo.z - o.z) * inv.z, t1z = (hi.z - o.z) * inv.z;
+        const float tn = fmaxf(tmin, fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z)));
+        const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+        const uint32_t hitw = __float_as_uint(lo.w);
+        const int miss = __float_as_int(hi.w);
+        if (hitw & kLeafFlag) {
+            if (tn <= fminf(kTmax, tf)) {
+                const uint32_t prim = hitw & kPrimMask;
+                const uint32_t type = (hitw >> kTypeShift) & 7u;
+                float t;
+                if (hit_prim(type, load_prim(prims, prim), o, d, tmin, t) &&
+                    (t < best_t || (t == best_t && (int)prim < best))) {
+                    best = (int)prim;
+                    best_t = t;
+                    best_type = type;
+                    prune = fminf(kTmax, best_t + best_t * 1e-3f + 1e-3f);
+                }
+            }
+            node = miss;
+        } else {
+            node = (tn <= fminf(prune, tf)) ? (int)hitw : miss;
+        }
+    }
+    return best;
+}
+
+// ------------------------------------------------------------------------------ flux bins -----
+// Bin of a receiver record at world point p, or -1 for a cylinder cap hit (see FluxTarget).
+__device__ __forceinline__ int flux_bin(const FluxTarget& F, float3 p) {
+    const float3 t = sub(p, xyz(F.o));
+    const float lx = dot(t, xyz(F.x)), ly = dot(t, xyz(F.y));
+    float u;
+    if (F.kind == kFluxCylinder) {
+        if (!(fabsf(ly) < F.keep)) return -1;
+        const float lz = dot(t, xyz(F.z));
+        float a = det_atan2(lz, lx);
+        if (a < 0.0f) a = a + kTwoPiF;
+        u = a * F.kx;
+    } else {
+        u = (lx + F.hx) * F.kx;
+    }
+    const float v = (ly + F.hy) * F.ky;
+    const int bx = (int)fminf(fmaxf(floorf(u), 0.0f), (float)(F.nx - 1));
+    const int by = (int)fminf(fmaxf(floorf(v), 0.0f), (float)(F.ny - 1));
+    return bx * F.ny + by;
+}
+
+// ------------------------------------------------------------------------------ trace ---------
+struct Segment {
+    float3 o, d;
+    float tmin;
+    int depth;
+};
+
+// Scene copy in shared memory for kFlat launches.
+struct FlatScene {
+    Prim prim[kFlatMax];
+    Aabb box[kFlatMax];
+    Optics optics[kFlatMax];
+    uint32_t type[kFlatMax];
+    int n;
+};
+
+// AABB culling of the intersection programs (segment [tmin, kTmax] against each element box) for a
+// kFlat scene: bit k set when element k's program has to run.
+__device__ __forceinline__ uint32_t candidates(const FlatScene& fs, float3 o, float3 d, float tmin) {
+    const float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    uint32_t mask = 0;
+    const int nb = fs.n;
+#pragma unroll
+    for (int k = 0; k < kFlatMax; ++k) {
+        if (k >= nb) break;
+        const float4 lo = fs.box[k].lo, hi = fs.box[k].hi;
+        const float t0x = (lo.x - o.x) * inv.x, t1x = (hi.x - o.x) * inv.x;
+        const float t0y = (lo.y - o.y) * inv.y, t1y = (hi.y - o.y) * inv.y;
+        const float t0z = (lo.z - o.z) * inv.z, t1z = (hi.z - o.z) * inv.z;
+        const float tn = fmaxf(tmin, fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z)));
+        const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+        if (tn <= fminf(kTmax, tf)) mask |= 1u << k;
+    }
+    return mask;
+}
+
+// Closest hit among the candidate elements, in ascending index (equal t keeps the lower index).
+__device__ __forceinline__ int closest_in(const FlatScene& fs, uint32_t mask, float3 o, float3 d, float tmin,
+                                          float& best_t, uint32_t& best_type) {
+    int best = -1;
+    best_t = __int_as_float(0x7f800000);
+    while (mask) {
+        const int k = __ffs(mask) - 1;
+        mask &= mask - 1u;
+        float t;
+        if (hit_prim(fs.type[k], fs.prim[k], o, d, tmin, t) && t < best_t) {
+            best = k;
+            best_t = t;
+            best_type = fs.type[k];
+        }
+    }
+    return best;
+}
+
+struct Hit {
+    int best;  // element index, -1 on a miss
+    float t;
+    uint32_t type;
+};
+
+// What the closest-hit program of a hit records: slot depth+1 (mirrors and the cylinder always,
+// below max depth; the flat receiver only from the front, cuda/materials.cu:86-163), and whether a
+// mirror has to be shaded next (cuda/materials.cu:44-60,180-197: only below max depth).
+__device__ __forceinline__ bool classify(const Prim& p, const Segment& g, const Hit& h, float4& rec, int& slot) {
+    slot = -1;
+    const int nd = g.depth + 1;
+    if (nd >= kMaxDepth) return false;
+    const float3 hit = add(g.o, scale(h.t, g.d));
+    if (h.type == kFlatMirror || h.type == kParabolicMirror) {
+        rec = make_float4(1.0f, hit.x, hit.y, hit.z);
+        slot = nd;
+        return true;
+    }
+    if (h.type == kFlatReceiver) {
+        const float3 rn = cross(xyz(p.c), xyz(p.d));
+        if (!(dot(g.d, rn) < 0.0f)) return false;
+    }
+    rec = make_float4(2.0f, hit.x, hit.y, hit.z);
+    slot = nd;
+    return false;
+}
+
+// __closesthit__mirror / __closesthit__mirror__parabolic (cuda/materials.cu:26-84,170-231): normal
+// as the intersection program reports it, faced against the ray, ideal reflection; plus the
+// extensions (Gaussian slope and specularity error, absorption with probability 1 - reflectivity).
+// Returns false when the ray is absorbed.
+__device__ __forceinline__ bool shade_mirror(const TraceArgs& A, uint64_t ray, const Prim& p, const Optics& op,
+                                             const Segment& g, const Hit& h, Segment& next) {
+    const int nd = g.depth + 1;
+    const float3 hit = add(g.o, scale(h.t, g.d));
+    const float3 wn = (h.type == kFlatMirror) ? normalize(xyz(p.a)) : normalize(parab_normal(p, g.o, g.d, h.t));
+    float3 ffn = (dot(neg(g.d), wn) >= 0.0f) ? wn : neg(wn);
+    const bool need_rng = (op.slope > 0.0f) || (op.spec > 0.0f) || !(op.reflectivity >= 1.0f);
+    u32x4 ra = {0u, 0u, 0u, 0u};
+    if (need_rng) ra = draw_block(ray, (uint32_t)nd, 0, A.instance, A.seed);
+    if (op.slope > 0.0f) {
+        float g1, g2;
+        box_muller(u01(ra.y), u01(ra.z), g1, g2);
+        ffn = perturb(ffn, op.slope, g1, g2);
+    }
+    float3 rd = reflect(g.d, ffn);
+    if (op.spec > 0.0f) {
+        const u32x4 rb = draw_block(ray, (uint32_t)nd, 1, A.instance, A.seed);
+        float g1, g2;
+        box_muller(u01(rb.x), u01(rb.y), g1, g2);
+        rd = perturb(normalize(rd), op.spec, g1, g2);
+    }
+    if (need_rng && u01(ra.x) > op.reflectivity) return false;  // absorbed at the mirror
+    next = Segment{hit, rd, kTminBounce, nd};
+    return true;
+}
+
+// Ray generation: cuda/sun.cu:28-38 (Halton point on the sun parallelogram) and :72-91, :106
+// (direction in the sun cone; Gaussian sun as an extension).
+__device__ __forceinline__ Segment generate(const TraceArgs& A, const SunFrame& S, uint64_t ray, const float* t6) {
+    const float hu = halton2(ray), hv = halton3_tab(ray, t6);
+    const float3 pos = add(add(xyz(S.v0), scale(hu, xyz(S.e1))), scale(hv, xyz(S.e2)));
+    const u32x4 r0 = draw_block(ray, 0, 0, A.instance, A.seed);
+    const float3 w = xyz(S.w), cu = xyz(S.u), cv = xyz(S.v);
+    float3 dir;
+    if (S.shape == 1) {
+        float g1, g2;
+        box_muller(u01(r0.x), u01(r0.y), g1, g2);
+        dir = normalize(add(add(w, scale(S.sigma * g1, cu)), scale(S.sigma * g2, cv)));
+    } else {
+        const float rand1 = u01(r0.x), rand2 = u01(r0.y);
+        const float phi = kTwoPi * rand1;
+        const float z = S.cos_theta + (1.0f - S.cos_theta) * rand2;
+        const float r = sqrtf(1.0f - z * z);
+        float sp, cp;
+        det_sincos(phi, sp, cp);
+        dir = normalize(add(scale(r, add(scale(cp, cu), scale(sp, cv))), scale(z, w)));
+    }
+    return Segment{pos, dir, kTminSun, 0};
+}
+
+// Shared memory of one CTA: the ray queue, the Halton table, the sun frame and the kFlat scene.
+template <int kB>
+struct CoreSmem {
+    float qo[3][2 * kB], qd[3][2 * kB], qt[2 * kB];
+    uint32_t qw[2 * kB];  // kFlat: candidate mask; BVH: element | type << 28 of the pending mirror hit
+    uint64_t qray[2 * kB];
+    float t6[kH3Tab];
+    FlatScene flat;
+    SunFrame sun;
+    int qsize;
+};
+
+// Phase A record staging of the kDense sink, ray-major per warp.
+template <int kB>
+struct StageSmem {
+    float4 hits[kB * kMaxDepth];
+    uint32_t ids[kB * kMaxDepth];
+};
+
+// Where kFlux records go: the instance's flux target and the CTA's record counters.
+struct Sink {
+    const FluxTarget* F;
+    unsigned long long* stat;  // shared memory, [4]
+};
+
+// warp-aggregated increment by the lanes that execute it together
+__device__ __forceinline__ void warp_count(unsigned long long* s) {
+    const unsigned m = __activemask();
+    if ((int)(threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(s, (unsigned long long)__popc(m));
+}
+
+__device__ __forceinline__ void flux_record(const Sink& k, float4 rec) {
+    if (rec.x == 1.0f) {
+        warp_count(k.stat + 1);
+        return;
+    }
+    warp_count(k.stat + 2);
+    const int b = flux_bin(*k.F, make_float3(rec.y, rec.z, rec.w));
+    if (b >= 0) {
+        atomicAdd(k.F->counts + b, 1u);
+        warp_count(k.stat + 3);
+    }
+}
+
+__device__ __forceinline__ void store_record(const TraceArgs& A, uint64_t ray, int slot, float4 rec, uint32_t id) {
+    const uint64_t row = (ray - A.ray_begin) * kMaxDepth + (uint64_t)slot;
+    A.hits[row] = rec;
+    if (A.ids) A.ids[row] = id;
+}
+
+template <class C>
+__device__ __forceinline__ void emit(const TraceArgs& A, const Sink& k, uint64_t ray, int slot, float4 rec,
+                                     uint32_t id) {
+    if constexpr (C::kDense) store_record(A, ray, slot, rec, id);
+    if constexpr (C::kFlux) flux_record(k, rec);
+}
+
+// warp-aggregated append of the lanes with `want` set; every lane of the warp must call it
+template <int kB>
+__device__ __forceinline__ void push(CoreSmem<kB>& sm, bool want, uint64_t ray, float3 o, float3 d, float t,
+                                     uint32_t w) {
+    const unsigned mask = __ballot_sync(0xffffffffu, want);
+    if (mask == 0u) return;
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == __ffs(mask) - 1) base = atomicAdd(&sm.qsize, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
+    if (want) {
+        const int k = base + __popc(mask & ((1u << lane) - 1u));
+        sm.qo[0][k] = o.x;
+        sm.qo[1][k] = o.y;
+        sm.qo[2][k] = o.z;
+        sm.qd[0][k] = d.x;
+        sm.qd[1][k] = d.y;
+        sm.qd[2][k] = d.z;
+        sm.qt[k] = t;
+        sm.qw[k] = w;
+        sm.qray[k] = ray;
+    }
+}
+
+// Remainder of a path in phase B, from the closest hit `h` of segment `g`: record, shade, next
+// segment, until the ray misses, is absorbed, ends on the receiver or reaches the depth limit.
+template <class C>
+__device__ void finish_path(const TraceArgs& A, const Sink& k, const CoreSmem<C::kB>& sm, uint64_t ray, Segment g,
+                            Hit h) {
+    for (;;) {
+        if (h.best < 0) return;  // __miss__ms, cuda/materials.cu:236-253
+        const Prim p = C::kFlat ? sm.flat.prim[h.best] : load_prim(A.prims, (uint32_t)h.best);
+        float4 rec;
+        int slot;
+        const bool mirror = classify(p, g, h, rec, slot);
+        if (slot >= 0) emit<C>(A, k, ray, slot, rec, (uint32_t)h.best);
+        if (!mirror) return;
+        const Optics op = C::kFlat ? sm.flat.optics[h.best] : A.optics[h.best];
+        Segment next;
+        if (!shade_mirror(A, ray, p, op, g, h, next)) return;
+        g = next;
+        if (C::kFlat) {
+            const uint32_t m = candidates(sm.flat, g.o, g.d, g.tmin);
+            h.best = closest_in(sm.flat, m, g.o, g.d, g.tmin, h.t, h.type);
+        } else {
+            h.best = traverse(A.nodes, A.prims, g.o, g.d, g.tmin, h.t, h.type);
+        }
+    }
+}
+
+// Phase B: run full batches of kB queued rays (all = also the remainder).
+template <class C>
+__device__ void drain(const TraceArgs& A, const Sink& k, CoreSmem<C::kB>& sm, bool all) {
+    __syncthreads();
+    int qs = sm.qsize;
+    while (qs >= C::kB || (all && qs > 0)) {
+        const int n = min(qs, C::kB);
+        const int base = qs - n;
+        const bool have = (int)threadIdx.x < n;
+        float3 o = f3(0.f, 0.f, 0.f), d = f3(0.f, 0.f, 1.f);
+        float t = 0.f;
+        uint32_t w = 0;
+        uint64_t ray = 0;
+        if (have) {
+            const int q = base + threadIdx.x;
+            o = f3(sm.qo[0][q], sm.qo[1][q], sm.qo[2][q]);
+            d = f3(sm.qd[0][q], sm.qd[1][q], sm.qd[2][q]);
+            t = sm.qt[q];
+            w = sm.qw[q];
+            ray = sm.qray[q];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) sm.qsize = base;
+        __syncthreads();
+        if (have) {
+            if (C::kFlat) {
+                // first segment from the sun: intersection programs of the candidate elements
+                const Segment g{o, d, kTminSun, 0};
+                Hit h;
+                h.best = closest_in(sm.flat, w, o, d, kTminSun, h.t, h.type);
+                finish_path<C>(A, k, sm, ray, g, h);
+            } else {
+                // pending mirror hit of the first segment: its record was emitted in phase A
+                const Segment g{o, d, kTminSun, 0};
+                const Hit h{(int)(w & kPrimMask), t, w >> kTypeShift};
+                const Prim p = load_prim(A.prims, (uint32_t)h.best);
+                Segment next;
+                if (shade_mirror(A, ray, p, A.optics[h.best], g, h, next)) {
+                    Hit h2;
+                    h2.best = traverse(A.nodes, A.prims, next.o, next.d, next.tmin, h2.t, h2.type);
+                    finish_path<C>(A, k, sm, ray, next, h2);
+                }
+            }
+        }
+        __syncthreads();
+        qs = sm.qsize;
+    }
+}
+
+// Per-CTA setup of an instance: sun frame and (kFlat) the element list into shared memory.
+// Callers synchronise before the first use.
+template <class C>
+__device__ __forceinline__ void load_instance_smem(const TraceArgs& A, CoreSmem<C::kB>& sm) {
+    if (threadIdx.x < sizeof(SunFrame) / 4)
+        reinterpret_cast<uint32_t*>(&sm.sun)[threadIdx.x] = reinterpret_cast<const uint32_t*>(A.sun)[threadIdx.x];
+    if (C::kFlat && threadIdx.x < kFlatMax) {
+        const int nprim = A.sun->n_prims;
+        const int k = threadIdx.x;
+        if (k < nprim) {
+            // a kFlat scene's nodes are its leaves in element order
+            const Node nd = A.nodes[k];
+            sm.flat.prim[k] = A.prims[k];
+            sm.flat.optics[k] = A.optics[k];
+            sm.flat.box[k].lo = nd.lo;
+            sm.flat.box[k].hi = nd.hi;
+            sm.flat.type[k] = (__float_as_uint(nd.lo.w) >> kTypeShift) & 7u;
+        }
+        if (k == 0) sm.flat.n = min(nprim, kFlatMax);
+    }
+}
+
+// Phase A of one tile (rays A.ray_begin + tile * kB ...) followed by phase B on full batches.
+// `stage` is the kDense staging area (unused otherwise).
+template <class C>
+__device__ __forceinline__ void trace_tile(const TraceArgs& A, const Sink& k, CoreSmem<C::kB>& sm,
+                                           StageSmem<C::kB>* stage, uint64_t tile) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float4* wh = nullptr;
+    uint32_t* wi = nullptr;
+    float4* slot = nullptr;
+    uint32_t* id = nullptr;
+    if constexpr (C::kDense) {
+        wh = stage->hits + warp * 32 * kMaxDepth;
+        wi = stage->ids + warp * 32 * kMaxDepth;
+        slot = wh + lane * kMaxDepth;
+        id = wi + lane * kMaxDepth;
+    }
+    const uint64_t kk = tile * C::kB + threadIdx.x;
+    const uint64_t ray = A.ray_begin + kk;
+    if constexpr (C::kDense) {
+#pragma unroll
+        for (int s = 0; s < kMaxDepth; ++s) slot[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (A.ids) {
+#pragma unroll
+            for (int s = 0; s < kMaxDepth; ++s) id[s] = kNoElement;
+        }
+    }
+    bool want = false;
+    Segment g;
+    float qt = 0.f;
+    uint32_t qw = 0;
+    if (kk < A.count) {
+        g = generate(A, sm.sun, ray, sm.t6);
+        if constexpr (C::kDense) slot[0] = make_float4(0.0f, g.o.x, g.o.y, g.o.z);
+        if (C::kFlat) {
+            qw = candidates(sm.flat, g.o, g.d, g.tmin);
+            want = qw != 0u;
+        } else {
+            Hit h;
+            h.best = traverse(A.nodes, A.prims, g.o, g.d, g.tmin, h.t, h.type);
+            if (h.best >= 0) {
+                const Prim p = load_prim(A.prims, (uint32_t)h.best);
+                float4 rec;
+                int s;
+                want = classify(p, g, h, rec, s);
+                if (s >= 0) {
+                    if constexpr (C::kDense) {
+                        slot[s] = rec;
+                        if (A.ids) id[s] = (uint32_t)h.best;
+                    }
+                    if constexpr (C::kFlux) flux_record(k, rec);
+                }
+                qt = h.t;
+                qw = (uint32_t)h.best | (h.type << kTypeShift);
+            }
+        }
+    }
+    __syncwarp();
+    push<C::kB>(sm, want, ray, g.o, g.d, qt, qw);
+    if constexpr (C::kDense) {
+        // the warp's 32 x 80 B of records leave as 5 fully coalesced 512-byte rows (stride 80 B per
+        // lane in shared memory: the 16-byte stores of each quarter warp hit distinct banks)
+        const uint64_t warp_first = tile * C::kB + (uint64_t)warp * 32;
+        if (warp_first < A.count) {
+            const uint64_t n_rec = min((uint64_t)32, A.count - warp_first) * kMaxDepth;
+            float4* gh = A.hits + warp_first * kMaxDepth;
+#pragma unroll
+            for (int s = 0; s < kMaxDepth; ++s) {
+                const uint32_t e = (uint32_t)(s * 32 + lane);
+                if (e < n_rec) gh[e] = wh[e];
+            }
+            if (A.ids) {
+                uint32_t* gi = A.ids + warp_first * kMaxDepth;
+#pragma unroll
+                for (int s = 0; s < kMaxDepth; ++s) {
+                    const uint32_t e = (uint32_t)(s * 32 + lane);
+                    if (e < n_rec) gi[e] = wi[e];
+                }
+            }
+        }
+    }
+    drain<C>(A, k, sm, false);
+}
+
+}  // namespace
+}  // namespace csp

@@ -70,6 +70,24 @@ struct alignas(16) SunFrame {
     int shape, n_prims, pad1, pad2;
 };
 
+// Receiver flux map target (scripts/post_processing/flux_map_calculator.py:135-179 binning, in
+// float).  A receiver (stage-2) record at world point p has local coordinates t = p - o,
+// (lx, ly, lz) = (t.x_axis, t.y_axis, t.z_axis) and lands in bin (bx, by), counts[bx * ny + by]:
+//   flat      bx = floor((lx + hx) kx), by = floor((ly + hy) ky), kx = nx / w, ky = ny / h
+//   cylinder  a = atan2(lz, lx) in [0, 2 pi), bx = floor(a kx), kx = nx / (2 pi); by as above;
+//             only side hits (|ly| < keep) are binned, cap hits are dropped
+// both indices clamped to the grid.
+enum FluxKind : int { kFluxFlat = 0, kFluxCylinder = 1 };
+
+struct alignas(16) FluxTarget {
+    float4 o, x, y, z;          // receiver origin and local axes (xyz; w unused)
+    float hx, hy, kx, ky;
+    float keep;
+    int kind, nx, ny;
+    uint32_t* counts;           // [nx * ny]
+    unsigned long long* stats;  // [4]: rays, mirror records, receiver records, binned records
+};
+
 // Halton base-3 digit weights: f_k = fl(f_{k-1} / 3), f_0 = 1 (the float sequence cuda/sun.cu:19
 // produces), k = 1..41 enough for 64-bit indices.
 #ifdef __CUDACC__

@@ -65,6 +65,25 @@ SIGNATURES = {
     "csp_trace_noalloc": (ctypes.c_int, [ctypes.c_int, _P, ctypes.c_uint32, _P, ctypes.c_int, ctypes.c_double,
                                          ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64, _P, _P,
                                          _P]),
+    "csp_flux_map": (ctypes.c_int, [_H, ctypes.c_uint32, ctypes.c_uint32, _P, ctypes.c_double, _P]),
+    "csp_flux_target": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_uint32, _P]),
+    "csp_batch_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]),
+    "csp_batch_destroy": (ctypes.c_int, [_H]),
+    "csp_batch_set_flux_grid": (ctypes.c_int, [_H, ctypes.c_uint32, ctypes.c_uint32]),
+    "csp_batch_add_scene": (ctypes.c_int, [_H, _P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]),
+    "csp_batch_add_instance": (ctypes.c_int, [_H, ctypes.c_uint32, _P, _P, ctypes.c_int, ctypes.c_double,
+                                              ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32,
+                                              ctypes.POINTER(ctypes.c_uint32)]),
+    "csp_batch_clear_instances": (ctypes.c_int, [_H]),
+    "csp_batch_num_instances": (ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_uint32)]),
+    "csp_batch_set_tuning": (ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "csp_batch_get_tuning": (ctypes.c_int, [_H, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                            ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "csp_batch_run": (ctypes.c_int, [_H]),
+    "csp_batch_get_flux": (ctypes.c_int, [_H, ctypes.c_uint32, _P, ctypes.c_double, _P]),
+    "csp_batch_get_stats": (ctypes.c_int, [_H, ctypes.c_uint32, _P]),
+    "csp_batch_get_sun_plane": (ctypes.c_int, [_H, ctypes.c_uint32, _P]),
+    "csp_batch_get_timing": (ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
 }
 STINPUT_APPLY_OPTICS = 1
 
@@ -205,6 +224,13 @@ class Tracer:
         _check(self.lib.csp_get_sun_plane(self.h, _ptr(out)))
         return out
 
+    def flux_map(self, nx: int = 100, ny: int = 100, dni: float = 1000.0):
+        """(counts [nx, ny] uint32, flux [nx, ny] W/m^2) of the last run, binned on the device."""
+        counts = np.zeros((nx, ny), np.uint32)
+        flux = np.zeros((nx, ny), np.float64)
+        _check(self.lib.csp_flux_map(self.h, int(nx), int(ny), _ptr(counts), float(dni), _ptr(flux)))
+        return counts, flux
+
     def read_stinput(self, path: str, apply_optics: bool = False):
         _check(self.lib.csp_read_stinput(self.h, path.encode(), STINPUT_APPLY_OPTICS if apply_optics else 0))
 
@@ -227,6 +253,112 @@ class Tracer:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class Batch:
+    """One csp_batch: many scene instances traced in one persistent launch, flux maps out."""
+
+    def __init__(self, device: int = 0, nx: int = 100, ny: int = 100):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        _check(self.lib.csp_batch_create(ctypes.byref(h), int(device)))
+        self.h = h
+        self.nx, self.ny = int(nx), int(ny)
+        _check(self.lib.csp_batch_set_flux_grid(self.h, self.nx, self.ny))
+
+    def add_scene(self, elements: np.ndarray) -> int:
+        e = np.ascontiguousarray(elements)
+        if e.dtype != ELEMENT_DTYPE:
+            raise TypeError("elements must use scenes.ELEMENT_DTYPE")
+        sid = ctypes.c_uint32()
+        _check(self.lib.csp_batch_add_scene(self.h, _ptr(e), len(e), ctypes.byref(sid)))
+        return sid.value
+
+    def add_instance(self, scene: int, sun_dir, sun_shape: int, sun_param: float, num_rays: int, seed: int = 0,
+                     instance: int = 0, poses: np.ndarray | None = None) -> int:
+        p = None
+        if poses is not None:
+            p = np.ascontiguousarray(poses)
+            if p.dtype != ELEMENT_DTYPE:
+                raise TypeError("poses must use scenes.ELEMENT_DTYPE")
+        sd = np.ascontiguousarray(sun_dir, np.float64)
+        idx = ctypes.c_uint32()
+        _check(self.lib.csp_batch_add_instance(self.h, int(scene), _ptr(p), _ptr(sd), int(sun_shape),
+                                               float(sun_param), int(num_rays), int(seed), int(instance),
+                                               ctypes.byref(idx)))
+        return idx.value
+
+    def clear_instances(self):
+        _check(self.lib.csp_batch_clear_instances(self.h))
+
+    def __len__(self) -> int:
+        n = ctypes.c_uint32()
+        _check(self.lib.csp_batch_num_instances(self.h, ctypes.byref(n)))
+        return n.value
+
+    def set_tuning(self, block: int = 0, ctas_per_sm: int = 0, chunk: int = 0):
+        _check(self.lib.csp_batch_set_tuning(self.h, int(block), int(ctas_per_sm), int(chunk)))
+
+    def tuning(self, flat: bool) -> tuple[int, int, int]:
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(self.lib.csp_batch_get_tuning(self.h, 1 if flat else 0, ctypes.byref(a), ctypes.byref(b),
+                                             ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def run(self):
+        _check(self.lib.csp_batch_run(self.h))
+
+    def counts(self, index: int) -> np.ndarray:
+        out = np.zeros((self.nx, self.ny), np.uint32)
+        _check(self.lib.csp_batch_get_flux(self.h, int(index), _ptr(out), 0.0, None))
+        return out
+
+    def flux(self, index: int, dni: float = 1000.0) -> np.ndarray:
+        out = np.zeros((self.nx, self.ny), np.float64)
+        _check(self.lib.csp_batch_get_flux(self.h, int(index), None, float(dni), _ptr(out)))
+        return out
+
+    def stats(self, index: int) -> np.ndarray:
+        out = np.zeros(4, np.uint64)
+        _check(self.lib.csp_batch_get_stats(self.h, int(index), _ptr(out)))
+        return out
+
+    def sun_plane(self, index: int) -> np.ndarray:
+        out = np.zeros(16, np.float32)
+        _check(self.lib.csp_batch_get_sun_plane(self.h, int(index), _ptr(out)))
+        return out
+
+    def timing(self):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        _check(self.lib.csp_batch_get_timing(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            _check(self.lib.csp_batch_destroy(self.h))
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def flux_target(receiver: np.ndarray, nx: int = 100, ny: int = 100) -> np.ndarray:
+    """Host-only: the float binning parameters of a receiver element (csp_flux_target, 20 floats)."""
+    e = np.ascontiguousarray(np.asarray(receiver).reshape(1))
+    if e.dtype != ELEMENT_DTYPE:
+        raise TypeError("receiver must use scenes.ELEMENT_DTYPE")
+    out = np.zeros(20, np.float32)
+    _check(load().csp_flux_target(_ptr(e), int(nx), int(ny), _ptr(out)))
+    return out
 
 
 def parse_stinput(path: str, apply_optics: bool = False):

@@ -631,3 +631,40 @@ EXPORT void orc_sincos2pi_batch(const float* u, int64_t n, float* s, float* c) {
 EXPORT void orc_log_batch(const float* x, int64_t n, float* y) {
     for (int64_t i = 0; i < n; ++i) y[i] = orc_logf(x[i]);
 }
+EXPORT void orc_atan2_batch(const float* y, const float* x, int64_t n, float* out) {
+    for (int64_t i = 0; i < n; ++i) out[i] = orc_atan2f(y[i], x[i]);
+}
+
+/* Receiver flux map, scripts/post_processing/flux_map_calculator.py:135-179 (stage-2 records binned
+ * over the receiver) with the cylinder convention of plot_flux_map_gpu.py:174-210 (angle about the
+ * axis, axial coordinate, caps dropped), evaluated in float from the receiver parameters t[20] of
+ * csp_flux_target: origin (3), local x, y, z axes (9), hx, hy, kx, ky, keep, kind.
+ * rec: n float records {stage, x, y, z}.  counts[nx * ny] and stats[4] (rays unused, mirror
+ * records, receiver records, binned) are accumulated into. */
+EXPORT void orc_flux_counts(const float* rec, int64_t n, const float* t, int nx, int ny, uint32_t* counts,
+                            uint64_t* stats) {
+    for (int64_t i = 0; i < n; ++i) {
+        const float* r = rec + 4 * i;
+        if (r[0] == 1.0f) { stats[1] += 1; continue; }
+        if (r[0] != 2.0f) continue;
+        stats[2] += 1;
+        const float px = r[1] - t[0], py = r[2] - t[1], pz = r[3] - t[2];
+        const float lx = px * t[3] + py * t[4] + pz * t[5];
+        const float ly = px * t[6] + py * t[7] + pz * t[8];
+        float u;
+        if (t[17] == 1.0f) {
+            if (!(fabsf(ly) < t[16])) continue;
+            const float lz = px * t[9] + py * t[10] + pz * t[11];
+            float a = orc_atan2f(lz, lx);
+            if (a < 0.0f) a = a + 0x1.921fb6p+2f;
+            u = a * t[14];
+        } else {
+            u = (lx + t[12]) * t[14];
+        }
+        const float v = (ly + t[13]) * t[15];
+        const int bx = (int)fminf(fmaxf(floorf(u), 0.0f), (float)(nx - 1));
+        const int by = (int)fminf(fmaxf(floorf(v), 0.0f), (float)(ny - 1));
+        counts[(size_t)bx * ny + by] += 1;
+        stats[3] += 1;
+    }
+}

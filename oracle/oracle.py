@@ -79,6 +79,9 @@ class Oracle:
         for f in ("orc_sincos_batch", "orc_sincos2pi_batch"):
             getattr(L, f).argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]
         L.orc_log_batch.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
+        L.orc_atan2_batch.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
+        L.orc_flux_counts.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_void_p, ctypes.c_void_p]
 
     def trace(self, elements, sun_dir, sun_shape=0, sun_param=0.0, first_ray=0, count=1000, seed=0,
               instance=0, max_depth=MAX_DEPTH, nthreads=0, with_ids=True):
@@ -129,6 +132,23 @@ class Oracle:
         y = np.empty_like(x)
         self.lib.orc_log_batch(_p(x), x.size, _p(y))
         return y
+
+    def atan2(self, y, x):
+        y = np.ascontiguousarray(y, np.float32)
+        x = np.ascontiguousarray(x, np.float32)
+        out = np.empty_like(y)
+        self.lib.orc_atan2_batch(_p(y), _p(x), y.size, _p(out))
+        return out
+
+    def flux_counts(self, hits, target, nx=100, ny=100):
+        """(counts [nx, ny] uint32, stats [4] uint64) of float records [..., 4] for the receiver
+        parameters `target` (20 floats, as csp_flux_target returns them)."""
+        rec = np.ascontiguousarray(np.asarray(hits).reshape(-1, 4), np.float32)
+        t = np.ascontiguousarray(target, np.float32)
+        counts = np.zeros((nx, ny), np.uint32)
+        stats = np.zeros(4, np.uint64)
+        self.lib.orc_flux_counts(_p(rec), rec.shape[0], _p(t), int(nx), int(ny), _p(counts), _p(stats))
+        return counts, stats
 
 
 def ref_available() -> bool:

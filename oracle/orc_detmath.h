@@ -153,4 +153,35 @@ ORC_INLINE void orc_box_muller(float u1, float u2, float* g1, float* g2) {
     *g2 = rad * s;
 }
 
+/* atan2 by quadrant reduction to t = min/max in [0, 1], the tangent subtraction formula
+ * atan t = pi/6 + atan((t sqrt3 - 1)/(t + sqrt3)) for t > tan(pi/12), and the odd Taylor series of
+ * atan to t^13 on |t| <= tan(pi/12) (Horner, fused steps as written).  Used to bin receiver angles. */
+#define ORC_TAN_PI12 0x1.126146p-2f
+#define ORC_SQRT3 0x1.bb67aep+0f
+#define ORC_PI6 0x1.0c1524p-1f
+#define ORC_PIO2_F 0x1.921fb6p+0f
+#define ORC_PI_F 0x1.921fb6p+1f
+
+ORC_INLINE float orc_atan2f(float y, float x) {
+    const float ax = fabsf(x), ay = fabsf(y);
+    const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+    if (!(mx > 0.0f)) return 0.0f;
+    float t = mn / mx;
+    float base = 0.0f;
+    if (t > ORC_TAN_PI12) {
+        t = (t * ORC_SQRT3 - 1.0f) / (t + ORC_SQRT3);
+        base = ORC_PI6;
+    }
+    const float t2 = t * t;
+    float p = fmaf(t2, (float)(1.0 / 13.0), (float)(-1.0 / 11.0));
+    p = fmaf(t2, p, (float)(1.0 / 9.0));
+    p = fmaf(t2, p, (float)(-1.0 / 7.0));
+    p = fmaf(t2, p, (float)(1.0 / 5.0));
+    p = fmaf(t2, p, (float)(-1.0 / 3.0));
+    float r = fmaf(t * t2, p, t) + base;
+    if (ay > ax) r = ORC_PIO2_F - r;
+    if (x < 0.0f) r = ORC_PI_F - r;
+    return (y < 0.0f) ? -r : r;
+}
+
 #endif /* ORC_DETMATH_H */
