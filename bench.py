@@ -52,13 +52,17 @@ def parse():
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--rays", type=int, default=None, help="ray count (default: the workload's)")
-    p.add_argument("--workload", choices=["single_parabolic", "three_heliostats", "large_field"],
+    p.add_argument("--workload", choices=["single_parabolic", "three_heliostats", "large_field", "batched"],
                    default="single_parabolic",
                    help="single_parabolic is the benchmark line; the others are for reporting only")
+    p.add_argument("--instances", type=int, default=256, help="batched workload: number of instances")
+    p.add_argument("--heliostats", type=int, default=10000, help="batched / large_field: field size")
     p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-accuracy", action="store_true")
+    p.add_argument("--plain-instances", type=int, default=0,
+                   help="batched workload: instances timed in the plain loop (0 = all)")
     return p.parse_args()
 
 
@@ -331,10 +335,106 @@ def run_ours(args):
         pg.destroy_process_group()
 
 
+def batched_workload(n_instances, n_heliostats):
+    """The large field at per-instance sun positions with re-aimed heliostats and log-uniform ray
+    counts: (base elements, poses per instance, suns, ray counts)."""
+    from optixsoltracedemos_gb300 import scenes
+    base = scenes.large_field(n_heliostats=n_heliostats, num_rays=1).elements
+    suns, counts = scenes.batched_instances(n_instances=n_instances, n_heliostats=n_heliostats)
+    poses = [scenes.reaim(base, s) for s in suns]
+    return base, poses, suns, counts
+
+
+def run_batched(args):
+    """Batched workload: one csp_batch run (host element builds, upload, device refit, sun planes,
+    one persistent trace launch, flux maps back) against the plain per-scene loop through the
+    drop-in handle (per instance: new poses and sun, update, run, device flux map)."""
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    from optixsoltracedemos_gb300 import build as nbuild
+    nbuild.build()
+    from optixsoltracedemos_gb300 import native, scenes
+
+    base, poses, suns, counts = batched_workload(args.instances, args.heliostats)
+    total = int(counts.sum())
+    b = native.Batch(local)
+    sid = b.add_scene(base)
+    for i in range(len(suns)):
+        b.add_instance(sid, suns[i], scenes.SUN_PILLBOX, 4.65e-3, int(counts[i]), seed=0, instance=i, poses=poses[i])
+    t0 = time.perf_counter()
+    b.run()  # autotune (first run of this scene class) + graph capture
+    first_s = time.perf_counter() - t0
+    for _ in range(max(0, args.warmup - 1)):
+        b.run()
+    clk = ClockSampler(local)
+    clk.start()
+    time.sleep(0.2)
+    wall, dev = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        b.run()
+        wall.append(time.perf_counter() - t0)
+        dev.append(b.timing()[1])
+    clocks = clk.stop()
+    batch_counts = [b.counts(i).copy() for i in range(len(suns))]
+
+    # plain per-scene loop through the drop-in handle
+    tr = native.Tracer(local, int(counts.max()))
+    tr.set_elements(poses[0])
+    tr.set_sun_vector(suns[0])
+    tr.set_sun_shape(scenes.SUN_PILLBOX, 4.65e-3)
+    tr.initialize()
+    n_plain = len(suns) if args.plain_instances <= 0 else min(len(suns), args.plain_instances)
+    mismatches = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(n_plain):
+        tr.set_elements(poses[i])
+        tr.set_sun_vector(suns[i])
+        tr.set_num_rays(int(counts[i]))
+        tr.set_seed(0, i)
+        tr.update()
+        tr.run()
+        c, _ = tr.flux_map()
+        mismatches += int(not np.array_equal(c, batch_counts[i]))
+    plain_s = time.perf_counter() - t0
+    plain_rays = int(counts[:n_plain].sum())
+    tr.close()
+    tb, tl = b.tuning(True), b.tuning(False)
+    line = {
+        "metric": METRIC, "value": total / statistics.median(dev), "unit": "rays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.median(dev) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batched_{len(suns)}_instances_large_field_{args.heliostats}_heliostats",
+                   "instances": len(suns), "rays_total": total, "rays_min": int(counts.min()),
+                   "rays_max": int(counts.max()), "flux_grid": [100, 100], "sun": "pillbox 4.65 mrad",
+                   "slope_error_rad": 1.5e-3, "tuning_bvh": tl, "tuning_small": tb,
+                   "l2_policy": "per-instance scenes and flux maps; no per-ray buffers"},
+        "batched_wall_rays_per_s": total / statistics.median(wall),
+        "batched_wall_ms": statistics.median(wall) * 1e3,
+        "first_run_s": first_s,
+        "plain_loop": {"rays_per_s": plain_rays / plain_s, "instances": n_plain, "seconds": plain_s,
+                       "flux_counts_mismatching_batched": mismatches},
+        "speedup_vs_plain_loop": (total / statistics.median(wall)) / (plain_rays / plain_s),
+        "e2e": {"value": total / statistics.median(wall), "unit": "rays/s",
+                "h2d_bytes_per_step": int(sum(p.nbytes for p in poses)),
+                "d2h_bytes_per_step": int(len(suns) * 100 * 100 * 4)},
+        "gpu_launches": 1 + 1 + 1,
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched":
+        run_batched(args)
     else:
         run_ours(args)
 

@@ -27,7 +27,8 @@
  *   csp_flux_map                  FluxMapCalculator.calculate_flux_map  scripts/post_processing/
  *                                                                        flux_map_calculator.py:135-179
  * Additions with no single reference counterpart: csp_trace_async (enqueue on a caller stream),
- * csp_get_device_buffers (zero-copy consumers), csp_set_seed, csp_set_record_ids.
+ * csp_get_device_buffers (zero-copy consumers), csp_set_seed, csp_set_record_ids, csp_set_accel,
+ * the flux map target, and the batch (csp_batch_*) and server (csp_server_*) interfaces.
  */
 #ifndef CSP_C_API_H
 #define CSP_C_API_H
@@ -108,6 +109,18 @@ CSP_API int csp_set_sun_shape(csp_handle h, int shape, double param_rad);
 CSP_API int csp_set_seed(csp_handle h, uint64_t seed, uint32_t instance);
 /* Also record the element index of every slot (uint32 per slot, CSP_NO_ELEMENT when empty). */
 CSP_API int csp_set_record_ids(csp_handle h, int enable);
+/* Closest-hit search structure for scenes of more than 8 elements (the reference leaves this to
+ * OptiX's GAS): AUTO = a uniform grid over the heliostat layer when the mirrors lie in a thin
+ * layer, else a BVH; BVH or GRID force one (GRID fails at initialize() for non-planar scenes).
+ * Scenes of up to 8 elements always use the element list (CSP_ACCEL_LIST).  Results are the same
+ * whichever structure is used.  Takes effect at the next csp_initialize. */
+#define CSP_ACCEL_AUTO 0
+#define CSP_ACCEL_BVH 1
+#define CSP_ACCEL_GRID 2
+#define CSP_ACCEL_LIST 3
+CSP_API int csp_set_accel(csp_handle h, int mode);
+/* The structure the last csp_initialize / csp_update chose. */
+CSP_API int csp_get_accel(csp_handle h, int* mode);
 
 /* Build device geometry, acceleration structure and sun plane; allocate the hit buffer. */
 CSP_API int csp_initialize(csp_handle h);
@@ -214,8 +227,10 @@ CSP_API int csp_batch_num_instances(csp_batch b, uint32_t* count);
  * tiles per work grab.  block = 0 selects the autotuner (default), which times candidates on a
  * sample of the batch at the first run of each scene class and keeps the fastest per device. */
 CSP_API int csp_batch_set_tuning(csp_batch b, int block, int ctas_per_sm, int chunk);
-/* The parameters used by the last run for small (flat != 0) or BVH scenes. */
-CSP_API int csp_batch_get_tuning(csp_batch b, int flat, int* block, int* ctas_per_sm, int* chunk);
+/* The parameters the last run used for one kernel group: CSP_ACCEL_LIST (<= 8 elements),
+ * CSP_ACCEL_BVH or CSP_ACCEL_GRID instances (an instance whose poses move an origin or change a
+ * size leaves its scene's grid for the BVH). */
+CSP_API int csp_batch_get_tuning(csp_batch b, int group, int* block, int* ctas_per_sm, int* chunk);
 CSP_API int csp_batch_run(csp_batch b);
 /* Results of the last run: counts / flux as csp_flux_map; stats[4] = rays, mirror records,
  * receiver records, binned receiver records. */

@@ -60,7 +60,11 @@ void Batch::release() {
     graph = nullptr;
     for (BScene& s : scenes) {
         cudaFree(s.d_topo);
+        cudaFree(s.d_cells);
+        cudaFree(s.d_items);
+        cudaFree(s.d_global);
         s.d_topo = nullptr;
+        s.d_cells = s.d_items = s.d_global = nullptr;
     }
     cudaFree(d_arena);
     d_arena = nullptr;
@@ -94,10 +98,23 @@ int Batch::add_scene(const csp_element* el, uint32_t n, uint32_t* id) {
     if ((rc = build_elements(el, n, s.base, err))) return set_error(rc, err);
     build_bvh(s.base);
     s.flat = n <= kFlatListMax;
-    const size_t bytes = s.base.nodes.size() * sizeof(Node);
-    if ((rc = cuda_status(cudaMalloc((void**)&s.d_topo, bytes), "cudaMalloc topology"))) return rc;
-    if ((rc = cuda_status(cudaMemcpy(s.d_topo, s.base.nodes.data(), bytes, cudaMemcpyHostToDevice), "upload topology"))) {
+    if (!s.flat) build_grid(el, n, s.base, s.grid);
+    auto put = [&](auto*& dptr, const auto& host, const char* what) {
+        const size_t bytes = std::max<size_t>(1, host.size()) * sizeof(host[0]);
+        int r = cuda_status(cudaMalloc((void**)&dptr, bytes), what);
+        if (!r && !host.empty())
+            r = cuda_status(cudaMemcpy(dptr, host.data(), host.size() * sizeof(host[0]), cudaMemcpyHostToDevice), what);
+        return r;
+    };
+    rc = put(s.d_topo, s.base.nodes, "upload topology");
+    if (!rc && s.grid.valid) rc = put(s.d_cells, s.grid.cell_start, "upload grid cells");
+    if (!rc && s.grid.valid) rc = put(s.d_items, s.grid.items, "upload grid items");
+    if (!rc && s.grid.valid) rc = put(s.d_global, s.grid.global, "upload grid globals");
+    if (rc) {
         cudaFree(s.d_topo);
+        cudaFree(s.d_cells);
+        cudaFree(s.d_items);
+        cudaFree(s.d_global);
         return rc;
     }
     scenes.push_back(std::move(s));
@@ -135,14 +152,16 @@ uint32_t Batch::count_of(size_t i) const { return (uint32_t)scenes[inst[i].scene
 int Batch::layout() {
     const size_t n = inst.size();
     place.assign(n, Place{});
-    n_group[0] = n_group[1] = 0;
+    layer.assign(2 * n, 0.f);
+    for (int g = 0; g < kBatchGroups; ++g) n_group[g] = 0;
     max_nodes = 0;
     size_t off = 0;
     for (size_t i = 0; i < n; ++i) {
         const BScene& s = scenes[inst[i].scene];
         const size_t ne = s.elements.size();
         Place& p = place[i];
-        p.group = s.flat ? 0 : 1;
+        p.group = s.flat ? kAccelFlat
+                         : (s.grid.valid && grid_accepts(s.grid, elements_of(i), count_of(i)) ? kAccelGrid : kAccelBvh);
         p.slot = n_group[p.group]++;
         p.prims = off;
         off += align16(ne * sizeof(Prim));
@@ -154,11 +173,11 @@ int Batch::layout() {
         off += align16(ne * sizeof(Aabb));
         max_nodes = std::max(max_nodes, (int)s.base.nodes.size());
     }
-    for (int g = 0; g < 2; ++g) {
+    for (int g = 0; g < kBatchGroups; ++g) {
         desc_off[g] = off;
         off += align16(n_group[g] * sizeof(InstanceDesc));
     }
-    for (int g = 0; g < 2; ++g) {
+    for (int g = 0; g < kBatchGroups; ++g) {
         tb_off[g] = off;
         off += align16((n_group[g] + 1) * sizeof(uint64_t));
     }
@@ -173,7 +192,7 @@ int Batch::layout() {
     }
     zero_off = off;
     counter_off = off;
-    off += 16;
+    off += align16(kBatchGroups * sizeof(unsigned long long));
     res_off = off;
     for (size_t i = 0; i < n; ++i) {
         place[i].stats = off;
@@ -245,6 +264,7 @@ int Batch::fill_instance(size_t i, HostScene& hs, std::string& err) {
     std::memcpy(h_stage + p.optics, src->optics.data(), ne * sizeof(Optics));
     std::memcpy(h_stage + p.aabbs, src->aabbs.data(), ne * sizeof(Aabb));
     std::memcpy(h_stage + p.prune, src->prune.data(), ne * sizeof(Aabb));
+    if (p.group == kAccelGrid) grid_layer(s.grid, *src, layer[2 * i], layer[2 * i + 1]);
     RefitJob rj;
     rj.topo = s.d_topo;
     rj.aabbs = reinterpret_cast<const Aabb*>(d_arena + p.aabbs);
@@ -271,14 +291,14 @@ int Batch::fill_instance(size_t i, HostScene& hs, std::string& err) {
 
 // Instance descriptors and tile tables of both groups for the given tile sizes; `sample` > 0
 // limits every instance to its first rays (autotuner), 0 = all rays.
-void Batch::fill_descs(const int block[2], double sample, std::vector<InstanceDesc>* out_desc,
+void Batch::fill_descs(const int* block, double sample, std::vector<InstanceDesc>* out_desc,
                        std::vector<uint64_t>* out_tb) {
     const size_t n = inst.size();
-    for (int g = 0; g < 2; ++g) {
+    for (int g = 0; g < kBatchGroups; ++g) {
         out_desc[g].assign(n_group[g], InstanceDesc{});
         out_tb[g].assign(n_group[g] + 1, 0);
     }
-    uint64_t tiles[2] = {0, 0};
+    uint64_t tiles[kBatchGroups] = {};
     for (size_t i = 0; i < n; ++i) {
         const BInst& b = inst[i];
         const Place& p = place[i];
@@ -297,6 +317,29 @@ void Batch::fill_descs(const int block[2], double sample, std::vector<InstanceDe
         d.args.seed = b.seed;
         d.args.instance = b.instance;
         d.args.pad = 0;
+        d.args.grid = nullptr;
+        if (g == kAccelGrid) {
+            const HostGrid& hg = scenes[b.scene].grid;
+            const BScene& bs = scenes[b.scene];
+            d.grid.x0 = hg.x0;
+            d.grid.y0 = hg.y0;
+            d.grid.x1 = hg.x1;
+            d.grid.y1 = hg.y1;
+            d.grid.cell = hg.cell;
+            d.grid.inv_cell = hg.inv_cell;
+            d.grid.zlo = layer[2 * i];
+            d.grid.zhi = layer[2 * i + 1];
+            d.grid.nx = hg.nx;
+            d.grid.ny = hg.ny;
+            d.grid.n_global = (int)hg.global.size();
+            d.grid.pad = 0;
+            d.grid.cell_start = bs.d_cells;
+            d.grid.items = bs.d_items;
+            d.grid.global = bs.d_global;
+            d.grid.aabbs = reinterpret_cast<const Aabb*>(d_arena + p.aabbs);
+            d.args.grid = reinterpret_cast<const GridDesc*>(d_arena + desc_off[g] + p.slot * sizeof(InstanceDesc) +
+                                                            offsetof(InstanceDesc, grid));
+        }
         flux_target(elements_of(i)[count_of(i) - 1], nx, ny, d.flux);
         d.flux.counts = reinterpret_cast<uint32_t*>(d_arena + p.counts);
         d.flux.stats = reinterpret_cast<unsigned long long*>(d_arena + p.stats);
@@ -305,11 +348,11 @@ void Batch::fill_descs(const int block[2], double sample, std::vector<InstanceDe
         out_tb[g][p.slot] = tiles[g];
         tiles[g] += (rays + block[g] - 1) / block[g];
     }
-    for (int g = 0; g < 2; ++g) out_tb[g][n_group[g]] = tiles[g];
+    for (int g = 0; g < kBatchGroups; ++g) out_tb[g][n_group[g]] = tiles[g];
 }
 
 void Batch::write_descs(const std::vector<InstanceDesc>* desc, const std::vector<uint64_t>* tb, unsigned char* img) {
-    for (int g = 0; g < 2; ++g) {
+    for (int g = 0; g < kBatchGroups; ++g) {
         if (!desc[g].empty()) std::memcpy(img + desc_off[g], desc[g].data(), desc[g].size() * sizeof(InstanceDesc));
         std::memcpy(img + tb_off[g], tb[g].data(), tb[g].size() * sizeof(uint64_t));
     }
@@ -351,7 +394,7 @@ int Batch::enqueue_scene_setup(cudaStream_t st) {
 int Batch::autotune(int g, BatchTuning& best) {
     std::vector<BatchTuning> cands;
     for (int block : {128, 256}) {
-        const int occ = batch_occupancy(g == 0, block);
+        const int occ = batch_occupancy(g, block);
         if (occ <= 0) continue;
         std::vector<int> ctas = {occ};
         if (occ > 1) ctas.push_back(std::max(1, occ * 2 / 3));
@@ -362,15 +405,15 @@ int Batch::autotune(int g, BatchTuning& best) {
     uint64_t total = 0;
     for (size_t i = 0; i < inst.size(); ++i)
         if (place[i].group == g) total += inst[i].rays;
-    const double budget = g == 0 ? 256e6 : 32e6;  // rays per candidate
+    const double budget = g == kAccelFlat ? 256e6 : (g == kAccelGrid ? 96e6 : 32e6);  // rays per candidate
     const double sample = std::min(1.0, std::max(1e-4, budget / std::max<double>(1.0, (double)total)));
     std::vector<unsigned char> img(up_bytes);
     double best_ms = 1e30;
     int rc = CSP_OK;
     for (const BatchTuning& t : cands) {
-        const int block[2] = {t.block, t.block};
-        std::vector<InstanceDesc> desc[2];
-        std::vector<uint64_t> tb[2];
+        const int block[kBatchGroups] = {t.block, t.block, t.block};
+        std::vector<InstanceDesc> desc[kBatchGroups];
+        std::vector<uint64_t> tb[kBatchGroups];
         fill_descs(block, sample, desc, tb);
         // descs and tile tables only: the element records already on the device stay
         const size_t lo = desc_off[0], hi = refit_off;
@@ -381,9 +424,10 @@ int Batch::autotune(int g, BatchTuning& best) {
         const BatchLaunch L = launch_of(g, tb[g][n_group[g]], t.chunk);
         float ms_best = 1e30f;
         for (int rep = 0; rep < 2 && rc == CSP_OK; ++rep) {
-            rc = cuda_status(cudaMemsetAsync(d_arena + counter_off, 0, 16, stream), "zero counters");
+            rc = cuda_status(cudaMemsetAsync(d_arena + counter_off, 0, kBatchGroups * sizeof(unsigned long long), stream),
+                             "zero counters");
             if (!rc) rc = cuda_status(cudaEventRecord(ev0, stream), "cudaEventRecord");
-            if (!rc) rc = cuda_status(launch_trace_batch(L, g == 0, t, stream), "batch_kernel");
+            if (!rc) rc = cuda_status(launch_trace_batch(L, g, t, stream), "batch_kernel");
             if (!rc) rc = cuda_status(cudaEventRecord(ev1, stream), "cudaEventRecord");
             if (!rc) rc = cuda_status(cudaEventSynchronize(ev1), "autotune");
             float ms = 0.f;
@@ -400,16 +444,16 @@ int Batch::autotune(int g, BatchTuning& best) {
 }
 
 int Batch::resolve_tuning() {
-    uint64_t rays[2] = {0, 0};
+    uint64_t rays[kBatchGroups] = {};
     for (size_t i = 0; i < inst.size(); ++i) rays[place[i].group] += inst[i].rays;
     bool need_setup = true;
-    for (int g = 0; g < 2; ++g) {
+    for (int g = 0; g < kBatchGroups; ++g) {
         if (n_group[g] == 0) {
             used[g] = BatchTuning{128, 0, 4};
             continue;
         }
         if (user.block != 0) {
-            if (batch_occupancy(g == 0, user.block) <= 0)
+            if (batch_occupancy(g, user.block) <= 0)
                 return set_error(CSP_ERR_INVALID_ARGUMENT, "unsupported batch block size");
             used[g] = user;
             continue;
@@ -471,18 +515,21 @@ int Batch::run() {
         if (wrc[w]) return set_error(wrc[w], werr[w]);
 
     if ((rc = resolve_tuning())) return rc;
-    const int block[2] = {used[0].block, used[1].block};
-    std::vector<InstanceDesc> desc[2];
-    std::vector<uint64_t> tb[2];
+    int block[kBatchGroups];
+    for (int g = 0; g < kBatchGroups; ++g) block[g] = used[g].block;
+    std::vector<InstanceDesc> desc[kBatchGroups];
+    std::vector<uint64_t> tb[kBatchGroups];
     fill_descs(block, 0.0, desc, tb);
     write_descs(desc, tb, h_stage);
-    const uint64_t tiles[2] = {tb[0][n_group[0]], tb[1][n_group[1]]};
+    uint64_t tiles[kBatchGroups];
+    for (int g = 0; g < kBatchGroups; ++g) tiles[g] = tb[g][n_group[g]];
 
     // graph signature: everything the captured launches depend on besides the staged contents
     std::vector<uint64_t> sig = {(uint64_t)(uintptr_t)d_arena, (uint64_t)(uintptr_t)h_stage,
-                                 (uint64_t)(uintptr_t)h_result, up_bytes, zero_bytes, res_bytes, n, nx, ny,
-                                 tiles[0], tiles[1]};
-    for (int g = 0; g < 2; ++g) {
+                                 (uint64_t)(uintptr_t)h_result, up_bytes, zero_bytes, res_bytes, n, nx, ny};
+    for (int g = 0; g < kBatchGroups; ++g) {
+        sig.push_back(tiles[g]);
+        sig.push_back((uint64_t)n_group[g]);
         sig.push_back((uint64_t)used[g].block);
         sig.push_back((uint64_t)used[g].ctas_per_sm);
         sig.push_back((uint64_t)used[g].chunk);
@@ -496,9 +543,9 @@ int Batch::run() {
         int crc = enqueue_prefix(stream);
         if (!crc) crc = cuda_status(cudaEventRecordWithFlags(ev0, stream, cudaEventRecordExternal), "event");
         if (!crc) crc = enqueue_scene_setup(stream);
-        for (int gi = 0; gi < 2 && !crc; ++gi)
+        for (int gi = 0; gi < kBatchGroups && !crc; ++gi)
             if (n_group[gi] > 0)
-                crc = cuda_status(launch_trace_batch(launch_of(gi, tiles[gi], used[gi].chunk), gi == 0, used[gi], stream),
+                crc = cuda_status(launch_trace_batch(launch_of(gi, tiles[gi], used[gi].chunk), gi, used[gi], stream),
                                   "batch_kernel");
         if (!crc) crc = cuda_status(cudaEventRecordWithFlags(ev1, stream, cudaEventRecordExternal), "event");
         if (!crc)
@@ -625,9 +672,10 @@ int csp_batch_set_tuning(csp_batch bh, int block, int ctas_per_sm, int chunk) {
     return CSP_OK;
 }
 
-int csp_batch_get_tuning(csp_batch bh, int flat, int* block, int* ctas_per_sm, int* chunk) {
+int csp_batch_get_tuning(csp_batch bh, int group, int* block, int* ctas_per_sm, int* chunk) {
     CSP_BGUARD(bh);
-    const csp::BatchTuning& t = reinterpret_cast<Batch*>(bh)->used[flat ? 0 : 1];
+    if (group < 0 || group >= csp::kBatchGroups) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "no such group");
+    const csp::BatchTuning& t = reinterpret_cast<Batch*>(bh)->used[group];
     if (block) *block = t.block;
     if (ctas_per_sm) *ctas_per_sm = t.ctas_per_sm;
     if (chunk) *chunk = t.chunk;

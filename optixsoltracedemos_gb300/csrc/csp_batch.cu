@@ -96,9 +96,9 @@ __device__ __forceinline__ void finish_instance(BatchSmem<C::kB>& sm, const Sink
     __syncthreads();
 }
 
-template <int kB, bool kFlat>
+template <int kB, int kAccel>
 __global__ void __launch_bounds__(kB, 768 / kB) batch_kernel(const BatchLaunch L) {
-    using C = Cfg<kB, kFlat, false, true>;
+    using C = Cfg<kB, kAccel, false, true>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BatchSmem<kB>& sm = *reinterpret_cast<BatchSmem<kB>*>(smem_raw);
     for (uint32_t m = threadIdx.x; m < kH3Tab; m += kB) sm.core.t6[m] = halton3(m);
@@ -144,37 +144,37 @@ __global__ void __launch_bounds__(kB, 768 / kB) batch_kernel(const BatchLaunch L
     if (have) finish_instance<C>(sm, k);
 }
 
-template <int kB, bool kFlat>
+template <int kB>
 constexpr size_t batch_smem() {
     return sizeof(BatchSmem<kB>);
 }
 
-template <int kB, bool kFlat>
+template <int kB, int kAccel>
 int occupancy_t() {
     static int cached = -1;
     if (cached >= 0) return cached;
-    if (cudaFuncSetAttribute(batch_kernel<kB, kFlat>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)batch_smem<kB, kFlat>()) != cudaSuccess)
+    if (cudaFuncSetAttribute(batch_kernel<kB, kAccel>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)batch_smem<kB>()) != cudaSuccess)
         return 0;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<kB, kFlat>, kB,
-                                                      batch_smem<kB, kFlat>()) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<kB, kAccel>, kB, batch_smem<kB>()) !=
+        cudaSuccess)
         return 0;
     cached = per_sm;
     return per_sm;
 }
 
-template <int kB, bool kFlat>
+template <int kB, int kAccel>
 cudaError_t launch_t(const BatchLaunch& L, const BatchTuning& t, cudaStream_t stream) {
     int dev = 0, sms = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    const int occ = occupancy_t<kB, kFlat>();
+    const int occ = occupancy_t<kB, kAccel>();
     if (occ <= 0) return cudaErrorInvalidConfiguration;
     const int per_sm = std::max(1, std::min(occ, t.ctas_per_sm > 0 ? t.ctas_per_sm : occ));
     const uint64_t grid = std::min<uint64_t>(std::max<uint64_t>(L.total_tiles, 1), (uint64_t)sms * per_sm);
-    batch_kernel<kB, kFlat><<<(unsigned)grid, kB, batch_smem<kB, kFlat>(), stream>>>(L);
+    batch_kernel<kB, kAccel><<<(unsigned)grid, kB, batch_smem<kB>(), stream>>>(L);
     return cudaGetLastError();
 }
 
@@ -193,18 +193,30 @@ cudaError_t launch_prepare_sun_batch(const SunJob* jobs, int n_jobs, cudaStream_
     return cudaGetLastError();
 }
 
-int batch_occupancy(bool flat, int block) {
-    if (block == 128) return flat ? occupancy_t<128, true>() : occupancy_t<128, false>();
-    if (block == 256) return flat ? occupancy_t<256, true>() : occupancy_t<256, false>();
-    return 0;
+int batch_occupancy(int accel, int block) {
+    switch (accel * 1000 + block) {
+        case kAccelFlat * 1000 + 128: return occupancy_t<128, kAccelFlat>();
+        case kAccelFlat * 1000 + 256: return occupancy_t<256, kAccelFlat>();
+        case kAccelBvh * 1000 + 128: return occupancy_t<128, kAccelBvh>();
+        case kAccelBvh * 1000 + 256: return occupancy_t<256, kAccelBvh>();
+        case kAccelGrid * 1000 + 128: return occupancy_t<128, kAccelGrid>();
+        case kAccelGrid * 1000 + 256: return occupancy_t<256, kAccelGrid>();
+        default: return 0;
+    }
 }
 
-cudaError_t launch_trace_batch(const BatchLaunch& L, bool flat, const BatchTuning& t, cudaStream_t stream) {
+cudaError_t launch_trace_batch(const BatchLaunch& L, int accel, const BatchTuning& t, cudaStream_t stream) {
     if (L.total_tiles == 0 || L.n_inst <= 0) return cudaSuccess;
     if (t.chunk <= 0) return cudaErrorInvalidValue;
-    if (t.block == 128) return flat ? launch_t<128, true>(L, t, stream) : launch_t<128, false>(L, t, stream);
-    if (t.block == 256) return flat ? launch_t<256, true>(L, t, stream) : launch_t<256, false>(L, t, stream);
-    return cudaErrorInvalidValue;
+    switch (accel * 1000 + t.block) {
+        case kAccelFlat * 1000 + 128: return launch_t<128, kAccelFlat>(L, t, stream);
+        case kAccelFlat * 1000 + 256: return launch_t<256, kAccelFlat>(L, t, stream);
+        case kAccelBvh * 1000 + 128: return launch_t<128, kAccelBvh>(L, t, stream);
+        case kAccelBvh * 1000 + 256: return launch_t<256, kAccelBvh>(L, t, stream);
+        case kAccelGrid * 1000 + 128: return launch_t<128, kAccelGrid>(L, t, stream);
+        case kAccelGrid * 1000 + 256: return launch_t<256, kAccelGrid>(L, t, stream);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace csp

@@ -18,6 +18,10 @@ struct BScene {
     HostScene base;         // element records + BVH topology of the scene's own poses
     Node* d_topo = nullptr; // topology on the device (links; boxes of the scene's own poses)
     bool flat = false;      // <= kFlatListMax elements: shared-memory element list kernel
+    HostGrid grid;          // field grid (valid for field-like scenes)
+    uint32_t* d_cells = nullptr;
+    uint32_t* d_items = nullptr;
+    uint32_t* d_global = nullptr;
 };
 
 struct BInst {
@@ -33,7 +37,7 @@ struct BInst {
 // Byte offsets of one instance's arrays in the device arena (and the staging image).
 struct Place {
     size_t prims = 0, optics = 0, aabbs = 0, prune = 0, nodes = 0, sun = 0, counts = 0, stats = 0;
-    int group = 0;  // 0 small-scene kernel, 1 BVH kernel
+    int group = 0;  // kAccelFlat, kAccelBvh or kAccelGrid: the kernel that traces the instance
     int slot = 0;   // index within the group
 };
 
@@ -45,7 +49,7 @@ struct Batch {
     std::vector<BScene> scenes;
     std::vector<BInst> inst;
     BatchTuning user{0, 0, 0};  // block 0: autotune
-    BatchTuning used[2] = {{128, 0, 4}, {128, 0, 4}};
+    BatchTuning used[kBatchGroups] = {{128, 0, 4}, {128, 0, 4}, {128, 0, 4}};
 
     unsigned char* d_arena = nullptr;
     size_t arena_cap = 0;
@@ -56,8 +60,9 @@ struct Batch {
 
     std::vector<Place> place;
     size_t up_bytes = 0, zero_off = 0, zero_bytes = 0, res_off = 0, res_bytes = 0;
-    size_t desc_off[2] = {0, 0}, tb_off[2] = {0, 0}, refit_off = 0, sunjob_off = 0, counter_off = 0;
-    int n_group[2] = {0, 0};
+    size_t desc_off[kBatchGroups] = {}, tb_off[kBatchGroups] = {}, refit_off = 0, sunjob_off = 0, counter_off = 0;
+    int n_group[kBatchGroups] = {};
+    std::vector<float> layer;  // per instance: zlo, zhi of grid instances
     int max_nodes = 0;
 
     cudaGraphExec_t graph = nullptr;
@@ -74,7 +79,7 @@ struct Batch {
     uint32_t count_of(size_t i) const;
     int layout();
     int fill_instance(size_t i, HostScene& scratch, std::string& err);
-    void fill_descs(const int block[2], double sample, std::vector<InstanceDesc>* desc, std::vector<uint64_t>* tb);
+    void fill_descs(const int* block, double sample, std::vector<InstanceDesc>* desc, std::vector<uint64_t>* tb);
     void write_descs(const std::vector<InstanceDesc>* desc, const std::vector<uint64_t>* tb, unsigned char* img);
     BatchLaunch launch_of(int g, uint64_t total_tiles, int chunk) const;
     int enqueue_prefix(cudaStream_t st);

@@ -64,6 +64,13 @@ void System::release() {
     cudaFree(d_sun);
     cudaFree(d_hits);
     cudaFree(d_ids);
+    cudaFree(d_grid);
+    cudaFree(d_cells);
+    cudaFree(d_items);
+    cudaFree(d_global);
+    d_grid = nullptr;
+    d_cells = d_items = d_global = nullptr;
+    cap_cells = cap_items = cap_global = 0;
     cudaFree(d_flux);
     cudaFree(d_fstats);
     d_flux = nullptr;
@@ -109,6 +116,38 @@ int System::upload_scene() {
         if ((rc = cuda_status(cudaMalloc((void**)&d_sun, sizeof(SunFrame)), "cudaMalloc sun"))) return rc;
     }
     return CSP_OK;
+}
+
+// Field grid on the device: the cell arrays (when `arrays`) and the descriptor with the layer of
+// the current poses.
+int System::upload_grid(bool arrays) {
+    if (!grid.valid) return CSP_OK;
+    int rc;
+    if (arrays) {
+        if ((rc = upload(d_cells, cap_cells, grid.cell_start, stream, "upload grid cells"))) return rc;
+        if ((rc = upload(d_items, cap_items, grid.items, stream, "upload grid items"))) return rc;
+        if ((rc = upload(d_global, cap_global, grid.global, stream, "upload grid globals"))) return rc;
+    }
+    if (!d_grid && (rc = cuda_status(cudaMalloc((void**)&d_grid, sizeof(GridDesc)), "cudaMalloc grid"))) return rc;
+    GridDesc g;
+    g.x0 = grid.x0;
+    g.y0 = grid.y0;
+    g.x1 = grid.x1;
+    g.y1 = grid.y1;
+    g.cell = grid.cell;
+    g.inv_cell = grid.inv_cell;
+    grid_layer(grid, scene, g.zlo, g.zhi);
+    g.nx = grid.nx;
+    g.ny = grid.ny;
+    g.n_global = (int)grid.global.size();
+    g.pad = 0;
+    g.cell_start = d_cells;
+    g.items = d_items;
+    g.global = d_global;
+    g.aabbs = d_aabbs;
+    grid_desc = g;
+    return cuda_status(cudaMemcpyAsync(d_grid, &grid_desc, sizeof(GridDesc), cudaMemcpyHostToDevice, stream),
+                       "upload grid");
 }
 
 float System::pad_angle() const {
@@ -157,7 +196,12 @@ int System::initialize() {
     std::string err;
     if ((rc = build_elements(elements.data(), (uint32_t)elements.size(), scene, err))) return fail(rc, err);
     build_bvh(scene);
+    grid = HostGrid{};
+    if (accel != CSP_ACCEL_BVH) build_grid(elements.data(), (uint32_t)elements.size(), scene, grid);
+    if (accel == CSP_ACCEL_GRID && !grid.valid && elements.size() > kFlatListMax)
+        return fail(CSP_ERR_BAD_SCENE, "the scene is not a planar field: no grid (use CSP_ACCEL_AUTO or _BVH)");
     if ((rc = upload_scene())) return rc;
+    if ((rc = upload_grid(true))) return rc;
     if ((rc = prepare_sun())) return rc;
     if ((rc = ensure_hit_buffers())) return rc;
     if ((rc = cuda_status(cudaStreamSynchronize(stream), "initialize"))) return rc;
@@ -174,7 +218,13 @@ int System::update() {
     int rc = build_elements(elements.data(), (uint32_t)elements.size(), scene, err);
     if (rc) return fail(rc, err);
     refit_bvh(scene);
+    bool rebuilt = false;
+    if (grid.valid && !grid_accepts(grid, elements.data(), (uint32_t)elements.size())) {
+        build_grid(elements.data(), (uint32_t)elements.size(), scene, grid);  // origins or sizes moved
+        rebuilt = true;
+    }
     if ((rc = upload_scene())) return rc;
+    if ((rc = upload_grid(rebuilt))) return rc;
     if ((rc = prepare_sun())) return rc;
     if ((rc = ensure_hit_buffers())) return rc;
     return cuda_status(cudaStreamSynchronize(stream), "update");
@@ -193,6 +243,7 @@ TraceArgs System::args(uint64_t begin, uint64_t count) const {
     a.seed = seed;
     a.instance = instance;
     a.pad = 0;
+    a.grid = grid.valid ? d_grid : nullptr;
     return a;
 }
 
@@ -397,6 +448,24 @@ int csp_set_seed(csp_handle h, uint64_t seed, uint32_t instance) {
     System* s = reinterpret_cast<System*>(h);
     s->seed = seed;
     s->instance = instance;
+    return CSP_OK;
+}
+
+int csp_set_accel(csp_handle h, int mode) {
+    CSP_GUARD(h);
+    if (mode != CSP_ACCEL_AUTO && mode != CSP_ACCEL_BVH && mode != CSP_ACCEL_GRID)
+        return fail(CSP_ERR_INVALID_ARGUMENT, "unknown acceleration mode");
+    System* s = reinterpret_cast<System*>(h);
+    s->accel = mode;
+    s->initialized = false;  // takes effect at the next initialize()
+    return CSP_OK;
+}
+
+int csp_get_accel(csp_handle h, int* mode) {
+    CSP_GUARD(h);
+    if (!mode) return fail(CSP_ERR_INVALID_ARGUMENT, "null output");
+    const System* s = reinterpret_cast<System*>(h);
+    *mode = (s->elements.size() <= csp::kFlatListMax) ? CSP_ACCEL_LIST : (s->grid.valid ? CSP_ACCEL_GRID : CSP_ACCEL_BVH);
     return CSP_OK;
 }
 

@@ -33,8 +33,8 @@ __global__ void __launch_bounds__(kPrepBlock) prepare_sun_kernel(const Aabb* __r
     sun_frame_block(aabbs, n, s, tan_pad, shape, param, out, scratch);
 }
 
-template <bool kFlat>
-using PlainCfg = Cfg<kTraceBlock, kFlat, true, false>;
+template <int kAccel>
+using PlainCfg = Cfg<kTraceBlock, kAccel, true, false>;
 
 struct TraceSmem {
     StageSmem<kTraceBlock> stage;
@@ -42,9 +42,9 @@ struct TraceSmem {
 };
 
 // Persistent kernel over the tiles of one launch (static round robin); dense records out.
-template <bool kFlat>
+template <int kAccel>
 __global__ void __launch_bounds__(kTraceBlock, 6) trace_kernel(const TraceArgs A) {
-    using C = PlainCfg<kFlat>;
+    using C = PlainCfg<kAccel>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TraceSmem& sm = *reinterpret_cast<TraceSmem*>(smem_raw);
     load_instance_smem<C>(A, sm.core);
@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(kTraceBlock, 6) trace_kernel(const TraceArgs A
     drain<C>(A, none, sm.core, true);
 }
 
-template <bool kFlat>
+template <int kAccel>
 cudaError_t launch_trace_t(const TraceArgs& args, cudaStream_t stream) {
     // persistent grid: every resident CTA slot of the device, never more CTAs than tiles
     int dev = 0, sms = 0, per_sm = 0;
@@ -65,16 +65,17 @@ cudaError_t launch_trace_t(const TraceArgs& args, cudaStream_t stream) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     static bool attr_set = false;  // per process; the attribute belongs to the function
     if (e == cudaSuccess && !attr_set) {
-        e = cudaFuncSetAttribute(trace_kernel<kFlat>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(trace_kernel<kAccel>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)sizeof(TraceSmem));
         attr_set = (e == cudaSuccess);
     }
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel<kFlat>, kTraceBlock, sizeof(TraceSmem));
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel<kAccel>, kTraceBlock,
+                                                          sizeof(TraceSmem));
     if (e != cudaSuccess) return e;
     const uint64_t tiles = (args.count + kTraceBlock - 1) / kTraceBlock;
     const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)std::max(1, sms * std::max(1, per_sm)));
-    trace_kernel<kFlat><<<(unsigned)grid, kTraceBlock, sizeof(TraceSmem), stream>>>(args);
+    trace_kernel<kAccel><<<(unsigned)grid, kTraceBlock, sizeof(TraceSmem), stream>>>(args);
     return cudaGetLastError();
 }
 
@@ -105,8 +106,9 @@ cudaError_t launch_prepare_sun(const Aabb* aabbs, int n, float sx, float sy, flo
 
 cudaError_t launch_trace(const TraceArgs& args, int n_prims, cudaStream_t stream) {
     if (args.count == 0) return cudaSuccess;
-    if (n_prims <= kFlatMax) return launch_trace_t<true>(args, stream);
-    return launch_trace_t<false>(args, stream);
+    if (n_prims <= kFlatMax) return launch_trace_t<kAccelFlat>(args, stream);
+    if (args.grid) return launch_trace_t<kAccelGrid>(args, stream);
+    return launch_trace_t<kAccelBvh>(args, stream);
 }
 
 cudaError_t launch_flux_records(const float4* hits, uint64_t n_records, const FluxTarget& F, cudaStream_t stream) {

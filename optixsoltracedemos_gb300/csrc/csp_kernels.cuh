@@ -8,6 +8,10 @@
 
 namespace csp {
 
+// Closest-hit search of a launch: the element list in shared memory (<= 8 elements), the BVH, or
+// the field grid (GridDesc).
+enum Accel : int { kAccelFlat = 0, kAccelBvh = 1, kAccelGrid = 2 };
+
 struct TraceArgs {
     const Node* nodes;
     const Prim* prims;
@@ -20,6 +24,7 @@ struct TraceArgs {
     uint64_t seed;
     uint32_t instance;
     int pad;
+    const GridDesc* grid;  // field grid of the scene, nullptr: BVH (or element list) traversal
 };
 
 // Sun-plane distance and parallelogram (lib/geometry_manager.cpp:97-148 with the reductions of
@@ -41,8 +46,9 @@ cudaError_t launch_flux_records(const float4* hits, uint64_t n_records, const Fl
 // records binned into flux.counts.  Instances of one launch are laid out as consecutive tile
 // ranges; CTAs take chunks of tiles from a global counter.
 struct alignas(16) InstanceDesc {
-    TraceArgs args;       // hits = ids = nullptr
+    TraceArgs args;       // hits = ids = nullptr; args.grid -> grid (grid instances)
     FluxTarget flux;
+    GridDesc grid;
     uint64_t tile_begin;  // first tile of this instance in the launch
     int n_prims;
     int pad[3];
@@ -85,8 +91,10 @@ struct SunJob {
 
 cudaError_t launch_refit(const RefitJob* jobs, int n_jobs, int max_nodes, cudaStream_t stream);
 cudaError_t launch_prepare_sun_batch(const SunJob* jobs, int n_jobs, cudaStream_t stream);
-// Occupancy limit of the multi-instance kernel for (flat, block); 0 if the block size is unsupported.
-int batch_occupancy(bool flat, int block);
-cudaError_t launch_trace_batch(const BatchLaunch& L, bool flat, const BatchTuning& t, cudaStream_t stream);
+// Closest-hit search of a batch group: 0 element list (<= 8 elements), 1 BVH, 2 field grid.
+constexpr int kBatchGroups = 3;
+// Occupancy limit of the multi-instance kernel for (accel, block); 0 if unsupported.
+int batch_occupancy(int accel, int block);
+cudaError_t launch_trace_batch(const BatchLaunch& L, int accel, const BatchTuning& t, cudaStream_t stream);
 
 }  // namespace csp

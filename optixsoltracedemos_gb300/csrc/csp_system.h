@@ -29,6 +29,8 @@ struct System {
     bool initialized = false;
 
     HostScene scene;
+    HostGrid grid;
+    int accel = CSP_ACCEL_AUTO;
 
     Node* d_nodes = nullptr;
     Prim* d_prims = nullptr;
@@ -37,6 +39,12 @@ struct System {
     SunFrame* d_sun = nullptr;
     float4* d_hits = nullptr;
     uint32_t* d_ids = nullptr;
+    GridDesc* d_grid = nullptr;
+    GridDesc grid_desc{};  // host copy (source of the async upload)
+    uint32_t* d_cells = nullptr;
+    uint32_t* d_items = nullptr;
+    uint32_t* d_global = nullptr;
+    size_t cap_cells = 0, cap_items = 0, cap_global = 0;
     uint32_t* d_flux = nullptr;              // csp_flux_map counts
     unsigned long long* d_fstats = nullptr;  // [4]
     size_t cap_flux = 0;
@@ -55,6 +63,7 @@ struct System {
     void release();
     int ensure_streams();
     int upload_scene();
+    int upload_grid(bool arrays);
     int prepare_sun();
     float pad_angle() const;
     int ensure_hit_buffers();

@@ -16,7 +16,8 @@
 //     atomic per warp):
 //       small scenes (kFlat, <= kFlatMax elements, all in shared memory): phase A only runs the AABB
 //         slab tests; rays whose segment overlaps some element box are queued with that mask;
-//       BVH scenes: phase A traverses and records the first hit; mirror hits are queued unshaded.
+//       BVH and grid scenes: phase A finds and records the first hit; mirror hits are queued
+//         unshaded.
 //   phase B (only on full batches of kB queued rays, and on the remainder at the end): the rest of
 //     each queued path -- intersection programs, shading, further segments.
 // In the heliostat workloads ~10% of rays meet an element; running their intersection programs and
@@ -44,11 +45,12 @@ constexpr float kTwoPiF = 0x1.921fb6p+2f;                  // fl32(2 pi), flux a
 constexpr int kFlatMax = 8;
 constexpr uint32_t kH3TabDigits = 6, kH3Tab = 729;
 
-template <int kB_, bool kFlat_, bool kDense_, bool kFlux_>
+template <int kB_, int kAccel_, bool kDense_, bool kFlux_>
 struct Cfg {
     static constexpr int kB = kB_;        // CTA size = tile size (rays)
     static constexpr int kQ = 2 * kB_;    // queue capacity: < kB left after a drain + kB pushes
-    static constexpr bool kFlat = kFlat_;
+    static constexpr int kAccel = kAccel_;
+    static constexpr bool kFlat = kAccel_ == kAccelFlat;
     static constexpr bool kDense = kDense_;
     static constexpr bool kFlux = kFlux_;
 };
@@ -370,6 +372,91 @@ __device__ __forceinline__ int traverse(const Node* __restrict__ nodes, const Pr
     return best;
 }
 
+// Exact-AABB culling and intersection program of one candidate element (a BVH leaf's work).
+__device__ __forceinline__ void test_element(uint32_t w, const Prim* __restrict__ prims, const Aabb* __restrict__ aabbs,
+                                             float3 o, float3 d, float3 inv, float tmin, int& best, float& best_t,
+                                             uint32_t& best_type, float& prune) {
+    const uint32_t prim = w & kPrimMask;
+    const float4* q = reinterpret_cast<const float4*>(aabbs + prim);
+    const float4 lo = __ldg(q), hi = __ldg(q + 1);
+    const float t0x = (lo.x - o.x) * inv.x, t1x = (hi.x - o.x) * inv.x;
+    const float t0y = (lo.y - o.y) * inv.y, t1y = (hi.y - o.y) * inv.y;
+    const float t0z = (lo.z - o.z) * inv.z, t1z = (hi.z - o.z) * inv.z;
+    const float tn = fmaxf(tmin, fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z)));
+    const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+    if (!(tn <= fminf(kTmax, tf))) return;
+    const uint32_t type = (w >> kTypeShift) & 7u;
+    float t;
+    if (hit_prim(type, load_prim(prims, prim), o, d, tmin, t) && (t < best_t || (t == best_t && (int)prim < best))) {
+        best = (int)prim;
+        best_t = t;
+        best_type = type;
+        prune = fminf(kTmax, best_t + best_t * 1e-3f + 1e-3f);
+    }
+}
+
+// Restrict [ta, tb] to the parameters where coordinate o + t d lies in [lo, hi] (an empty range
+// stays empty).
+__device__ __forceinline__ void clip_axis(float o, float d, float inv, float lo, float hi, float& ta, float& tb) {
+    if (d == 0.0f) {
+        if (!(o >= lo && o <= hi)) {
+            ta = 1.0f;
+            tb = 0.0f;
+        }
+        return;
+    }
+    const float t0 = (lo - o) * inv, t1 = (hi - o) * inv;
+    ta = fmaxf(ta, fminf(t0, t1));
+    tb = fminf(tb, fmaxf(t0, t1));
+}
+
+// Closest hit through the field grid: the global elements, then the cells of the xy path inside
+// the layer in ray order (2D DDA), each cell's candidates through test_element, until a cell is
+// entered beyond the pruning distance.  The result equals traverse()'s: every element whose
+// surface holds a hit point at t is registered in the cell the walk assigns to that point (the
+// registered squares exceed the surfaces by a margin far above the walk's rounding), that cell is
+// entered at or before t, and the walk only stops beyond best_t + best_t 1e-3 + 1e-3.
+__device__ __forceinline__ int traverse_grid(const GridDesc& G, const Prim* __restrict__ prims, float3 o, float3 d,
+                                             float tmin, float& best_t, uint32_t& best_type) {
+    const float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    int best = -1;
+    best_t = __int_as_float(0x7f800000);
+    float prune = kTmax;
+    for (int g = 0; g < G.n_global; ++g)
+        test_element(__ldg(G.global + g), prims, G.aabbs, o, d, inv, tmin, best, best_t, best_type, prune);
+    float ta = tmin, tb = kTmax;
+    clip_axis(o.z, d.z, inv.z, G.zlo, G.zhi, ta, tb);
+    clip_axis(o.x, d.x, inv.x, G.x0, G.x1, ta, tb);
+    clip_axis(o.y, d.y, inv.y, G.y0, G.y1, ta, tb);
+    if (!(ta <= tb) || ta > prune) return best;
+    const float px = o.x + ta * d.x, py = o.y + ta * d.y;
+    int ix = (int)fminf(fmaxf(floorf((px - G.x0) * G.inv_cell), 0.0f), (float)(G.nx - 1));
+    int iy = (int)fminf(fmaxf(floorf((py - G.y0) * G.inv_cell), 0.0f), (float)(G.ny - 1));
+    const int sx = d.x > 0.0f ? 1 : -1, sy = d.y > 0.0f ? 1 : -1;
+    const float inf = __int_as_float(0x7f800000);
+    float tc = ta;
+    for (int step = 0; step <= G.nx + G.ny; ++step) {
+        const int c = iy * G.nx + ix;
+        const uint32_t b = __ldg(G.cell_start + c), e = __ldg(G.cell_start + c + 1);
+        for (uint32_t j = b; j < e; ++j)
+            test_element(__ldg(G.items + j), prims, G.aabbs, o, d, inv, tmin, best, best_t, best_type, prune);
+        // parameters of the next x and y cell boundaries, from the cell index (no accumulation)
+        const float tnx = (d.x != 0.0f) ? (G.x0 + (float)(ix + (sx > 0)) * G.cell - o.x) * inv.x : inf;
+        const float tny = (d.y != 0.0f) ? (G.y0 + (float)(iy + (sy > 0)) * G.cell - o.y) * inv.y : inf;
+        if (tnx < tny) {
+            tc = fmaxf(tc, tnx);
+            ix += sx;
+            if (ix < 0 || ix >= G.nx) break;
+        } else {
+            tc = fmaxf(tc, tny);
+            iy += sy;
+            if (iy < 0 || iy >= G.ny) break;
+        }
+        if (tc > tb || tc > prune) break;
+    }
+    return best;
+}
+
 // ------------------------------------------------------------------------------ flux bins -----
 // Bin of a receiver record at world point p, or -1 for a cylinder cap hit (see FluxTarget).
 __device__ __forceinline__ int flux_bin(const FluxTarget& F, float3 p) {
@@ -536,8 +623,17 @@ struct CoreSmem {
     float t6[kH3Tab];
     FlatScene flat;
     SunFrame sun;
+    GridDesc grid;
     int qsize;
 };
+
+// Closest hit of a segment in a BVH or grid launch.
+template <class C>
+__device__ __forceinline__ int find_closest(const TraceArgs& A, const CoreSmem<C::kB>& sm, float3 o, float3 d,
+                                            float tmin, float& t, uint32_t& type) {
+    if constexpr (C::kAccel == kAccelGrid) return traverse_grid(sm.grid, A.prims, o, d, tmin, t, type);
+    else return traverse(A.nodes, A.prims, o, d, tmin, t, type);
+}
 
 // Phase A record staging of the kDense sink, ray-major per warp.
 template <int kB>
@@ -629,7 +725,7 @@ __device__ void finish_path(const TraceArgs& A, const Sink& k, const CoreSmem<C:
             const uint32_t m = candidates(sm.flat, g.o, g.d, g.tmin);
             h.best = closest_in(sm.flat, m, g.o, g.d, g.tmin, h.t, h.type);
         } else {
-            h.best = traverse(A.nodes, A.prims, g.o, g.d, g.tmin, h.t, h.type);
+            h.best = find_closest<C>(A, sm, g.o, g.d, g.tmin, h.t, h.type);
         }
     }
 }
@@ -673,7 +769,7 @@ __device__ void drain(const TraceArgs& A, const Sink& k, CoreSmem<C::kB>& sm, bo
                 Segment next;
                 if (shade_mirror(A, ray, p, A.optics[h.best], g, h, next)) {
                     Hit h2;
-                    h2.best = traverse(A.nodes, A.prims, next.o, next.d, next.tmin, h2.t, h2.type);
+                    h2.best = find_closest<C>(A, sm, next.o, next.d, next.tmin, h2.t, h2.type);
                     finish_path<C>(A, k, sm, ray, next, h2);
                 }
             }
@@ -703,6 +799,8 @@ __device__ __forceinline__ void load_instance_smem(const TraceArgs& A, CoreSmem<
         }
         if (k == 0) sm.flat.n = min(nprim, kFlatMax);
     }
+    if (C::kAccel == kAccelGrid && threadIdx.x < sizeof(GridDesc) / 4)
+        reinterpret_cast<uint32_t*>(&sm.grid)[threadIdx.x] = reinterpret_cast<const uint32_t*>(A.grid)[threadIdx.x];
 }
 
 // Phase A of one tile (rays A.ray_begin + tile * kB ...) followed by phase B on full batches.
@@ -743,7 +841,7 @@ __device__ __forceinline__ void trace_tile(const TraceArgs& A, const Sink& k, Co
             want = qw != 0u;
         } else {
             Hit h;
-            h.best = traverse(A.nodes, A.prims, g.o, g.d, g.tmin, h.t, h.type);
+            h.best = find_closest<C>(A, sm, g.o, g.d, g.tmin, h.t, h.type);
             if (h.best >= 0) {
                 const Prim p = load_prim(A.prims, (uint32_t)h.best);
                 float4 rec;

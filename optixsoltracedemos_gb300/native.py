@@ -65,6 +65,8 @@ SIGNATURES = {
     "csp_trace_noalloc": (ctypes.c_int, [ctypes.c_int, _P, ctypes.c_uint32, _P, ctypes.c_int, ctypes.c_double,
                                          ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64, _P, _P,
                                          _P]),
+    "csp_set_accel": (ctypes.c_int, [_H, ctypes.c_int]),
+    "csp_get_accel": (ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_int)]),
     "csp_flux_map": (ctypes.c_int, [_H, ctypes.c_uint32, ctypes.c_uint32, _P, ctypes.c_double, _P]),
     "csp_flux_target": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_uint32, _P]),
     "csp_batch_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]),
@@ -86,6 +88,8 @@ SIGNATURES = {
     "csp_batch_get_timing": (ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
 }
 STINPUT_APPLY_OPTICS = 1
+ACCEL_AUTO, ACCEL_BVH, ACCEL_GRID, ACCEL_LIST = 0, 1, 2, 3
+GROUP_LIST, GROUP_BVH, GROUP_GRID = 0, 1, 2  # batch kernel groups
 
 _lib = None
 _lock = threading.Lock()
@@ -172,6 +176,15 @@ class Tracer:
     def set_record_ids(self, enable: bool = True):
         _check(self.lib.csp_set_record_ids(self.h, 1 if enable else 0))
         self.record_ids = bool(enable)
+
+    def set_accel(self, mode: int):
+        """ACCEL_AUTO / ACCEL_BVH / ACCEL_GRID (next initialize())."""
+        _check(self.lib.csp_set_accel(self.h, int(mode)))
+
+    def accel(self) -> int:
+        m = ctypes.c_int()
+        _check(self.lib.csp_get_accel(self.h, ctypes.byref(m)))
+        return m.value
 
     # ---- lifecycle
     def initialize(self):
@@ -299,10 +312,11 @@ class Batch:
     def set_tuning(self, block: int = 0, ctas_per_sm: int = 0, chunk: int = 0):
         _check(self.lib.csp_batch_set_tuning(self.h, int(block), int(ctas_per_sm), int(chunk)))
 
-    def tuning(self, flat: bool) -> tuple[int, int, int]:
+    def tuning(self, group: int) -> tuple[int, int, int]:
+        """(block, ctas_per_sm, chunk) of the last run for a kernel group: GROUP_LIST (<= 8 elements),
+        GROUP_BVH or GROUP_GRID."""
         a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-        _check(self.lib.csp_batch_get_tuning(self.h, 1 if flat else 0, ctypes.byref(a), ctypes.byref(b),
-                                             ctypes.byref(c)))
+        _check(self.lib.csp_batch_get_tuning(self.h, int(group), ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
         return a.value, b.value, c.value
 
     def run(self):
@@ -395,9 +409,10 @@ def write_hits_csv(hits: np.ndarray, path: str) -> None:
 
 
 def tracer_for(scene, device: int = 0, seed: int = 0, instance: int = 0, record_ids: bool = True,
-               num_rays: int | None = None) -> Tracer:
+               num_rays: int | None = None, accel: int = ACCEL_AUTO) -> Tracer:
     """Tracer configured and initialized for a scenes.Scene."""
     t = Tracer(device, scene.num_rays if num_rays is None else num_rays)
+    t.set_accel(accel)
     t.set_elements(scene.elements)
     t.set_sun_vector(scene.sun_dir)
     t.set_sun_shape(scene.sun_shape, scene.sun_param)

@@ -115,6 +115,30 @@ def test_batch_instances_equal_plain_runs(gpu):
         b.close()
 
 
+def test_batch_groups(gpu):
+    """Re-aimed field instances run in the grid group; an instance whose poses move a heliostat
+    runs in the BVH group; both equal plain runs."""
+    from optixsoltracedemos_gb300 import native
+    b = native.Batch(0)
+    try:
+        base = _field(800, scenes.sun_vector(45.0, 0.0))
+        sid = b.add_scene(base)
+        sun = scenes.sun_vector(20.0, 60.0)
+        reaimed = scenes.reaim(base, sun)
+        moved = reaimed.copy()
+        moved["origin"][5] += [3.0, -2.0, 0.0]
+        b.add_instance(sid, sun, scenes.SUN_PILLBOX, 4.65e-3, 150000, seed=1, instance=1, poses=reaimed)
+        b.add_instance(sid, sun, scenes.SUN_PILLBOX, 4.65e-3, 150000, seed=1, instance=1, poses=moved)
+        b.run()
+        assert b.tuning(native.GROUP_GRID)[0] in (128, 256)
+        assert b.tuning(native.GROUP_BVH)[0] in (128, 256)
+        for i, poses in enumerate((reaimed, moved)):
+            counts, _, _ = _plain_counts(native, poses, sun, scenes.SUN_PILLBOX, 4.65e-3, 150000, 1, 1)
+            np.testing.assert_array_equal(b.counts(i), counts)
+    finally:
+        b.close()
+
+
 def test_batch_independent_of_launch_parameters(gpu):
     from optixsoltracedemos_gb300 import native
     results = []
@@ -124,10 +148,9 @@ def test_batch_independent_of_launch_parameters(gpu):
             b.set_tuning(*tune)
             b.run()
             results.append([b.counts(i).copy() for i in range(len(jobs))])
-            if tune[0]:
-                assert b.tuning(True)[0] == tune[0] and b.tuning(False)[0] == tune[0]
-            else:
-                assert b.tuning(True)[0] in (128, 256) and b.tuning(False)[0] in (128, 256)
+            groups = (native.GROUP_LIST, native.GROUP_GRID)
+            for g in groups:
+                assert b.tuning(g)[0] == (tune[0] if tune[0] else b.tuning(g)[0]) and b.tuning(g)[0] in (128, 256)
         finally:
             b.close()
     for r in results[1:]:

@@ -15,8 +15,8 @@ pytestmark = pytest.mark.gpu
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
 
 
-def gpu_trace(sc, n, seed=0, instance=0, first=0, count=None):
-    t = native.tracer_for(sc, seed=seed, instance=instance, num_rays=n)
+def gpu_trace(sc, n, seed=0, instance=0, first=0, count=None, accel=native.ACCEL_AUTO):
+    t = native.tracer_for(sc, seed=seed, instance=instance, num_rays=n, accel=accel)
     t.run()
     hits, ids = t.copy_hits(first, count)
     t.close()
@@ -51,19 +51,24 @@ def test_gpu_matches_oracle_bit_exact(gpu, oracle32, name):
     if name == "single_parabolic_pillbox_spec":
         sc.elements["specularity_error"][0] = 0.5e-3
         sc.elements["reflectivity"][0] = 0.93
-    n = 60000  # above 2 x 27648: the BVH path's coherent ray order covers two whole blocks and a tail
+    n = 60000
+    # fields run through both search structures (grid by default, BVH forced)
+    accels = (native.ACCEL_AUTO, native.ACCEL_BVH) if name.startswith("field") else (native.ACCEL_AUTO,)
     for seed, inst in ((0, 0), (987654321, 5)):
-        hits, ids = gpu_trace(sc, n, seed=seed, instance=inst)
         oh, oi = oracle32.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, count=n, seed=seed, instance=inst)
-        np.testing.assert_array_equal(ids, oi)
-        np.testing.assert_array_equal(hits, oh.astype(np.float32))
+        for accel in accels:
+            hits, ids = gpu_trace(sc, n, seed=seed, instance=inst, accel=accel)
+            np.testing.assert_array_equal(ids, oi)
+            np.testing.assert_array_equal(hits, oh.astype(np.float32))
 
 
-def test_gpu_large_field_bvh_bit_exact(gpu, oracle32):
-    """2000 flat heliostats, cylinder receiver (BVH path, coherent ray order): a window of 100k rays
-    starting mid-launch, against the oracle's brute-force closest hit."""
+@pytest.mark.parametrize("accel", [native.ACCEL_BVH, native.ACCEL_GRID], ids=["bvh", "grid"])
+def test_gpu_large_field_bit_exact(gpu, oracle32, accel):
+    """2000 flat heliostats, cylinder receiver, through the BVH and through the field grid: a window
+    of 100k rays starting mid-launch, against the oracle's brute-force closest hit."""
     sc = scenes.large_field(n_heliostats=2000, sun=scenes.sun_vector(35.0, 70.0))
-    t = native.tracer_for(sc, seed=4, num_rays=400000)
+    t = native.tracer_for(sc, seed=4, num_rays=400000, accel=accel)
+    assert t.accel() == accel
     t.run()
     first, n = 150001, 100000
     hits, ids = t.copy_hits(first, n)
@@ -72,6 +77,60 @@ def test_gpu_large_field_bvh_bit_exact(gpu, oracle32):
     np.testing.assert_array_equal(ids, oi)
     np.testing.assert_array_equal(hits, oh.astype(np.float32))
     assert (hits[:, :, 0] == 2).sum() > 1000
+
+
+@pytest.mark.parametrize("el,az,parabolic", [(45.0, 0.0, False), (11.0, 80.0, False), (78.0, -100.0, True),
+                                              (25.0, 180.0, True)])
+def test_grid_equals_bvh_full_field(gpu, el, az, parabolic):
+    """10,000-heliostat field at several sun positions (low sun: long walks through the layer): the
+    grid and the BVH give identical records and element ids for 1M rays; after re-aiming the
+    heliostats (csp_update) too."""
+    sc = scenes.large_field(sun=scenes.sun_vector(el, az), parabolic=parabolic)
+    n = 1 << 20
+    out = {}
+    for accel in (native.ACCEL_GRID, native.ACCEL_BVH):
+        t = native.tracer_for(sc, seed=7, num_rays=n, accel=accel)
+        assert t.accel() == accel
+        t.run()
+        a = t.copy_hits()
+        t.set_elements(scenes.reaim(sc.elements, scenes.sun_vector(el + 5.0, az + 10.0)))
+        t.set_sun_vector(scenes.sun_vector(el + 5.0, az + 10.0))
+        t.update()
+        t.run()
+        out[accel] = (a, t.copy_hits())
+        t.close()
+    for k in range(2):
+        np.testing.assert_array_equal(out[native.ACCEL_GRID][k][1], out[native.ACCEL_BVH][k][1])
+        np.testing.assert_array_equal(out[native.ACCEL_GRID][k][0], out[native.ACCEL_BVH][k][0])
+    assert (out[native.ACCEL_GRID][0][0][:, :, 0] == 2).sum() > 1000
+
+
+def test_accel_selection(gpu):
+    """AUTO picks the grid for a planar field, the BVH for a non-planar scene of more than 8
+    elements, the element list for small scenes; GRID on a non-planar scene is an error."""
+    field = scenes.large_field(n_heliostats=300)
+    t = native.tracer_for(field, num_rays=1)
+    assert t.accel() == native.ACCEL_GRID
+    t.close()
+    t = native.tracer_for(scenes.three_heliostats(), num_rays=1)
+    assert t.accel() == native.ACCEL_LIST
+    t.close()
+    # a stack of mirrors: 12 mirrors at heights 0..110 m, the layer is as tall as the field is wide
+    e = scenes.make_elements(13)
+    e["origin"][:12] = [[0.0, 0.0, 10.0 * k] for k in range(12)]
+    e["aim_point"][:12] = [[0.0, 1.0, 10.0 * k + 1.0] for k in range(12)]
+    e["width"][:12] = 5.0
+    e["height"][:12] = 5.0
+    e["origin"][12] = [0.0, 50.0, 50.0]
+    e["aim_point"][12] = [0.0, 0.0, 50.0]
+    e["width"][12] = 10.0
+    e["height"][12] = 10.0
+    stack = scenes.Scene("stack", e, np.array([0.0, 1.0, 0.2]), 0, 4.65e-3, 1)
+    t = native.tracer_for(stack, num_rays=1)
+    assert t.accel() == native.ACCEL_BVH
+    t.close()
+    with pytest.raises(native.CspError):
+        native.tracer_for(stack, num_rays=1, accel=native.ACCEL_GRID)
 
 
 def test_gpu_sun_plane_matches_oracle(gpu, oracle32):
