@@ -422,37 +422,44 @@ __device__ __forceinline__ int traverse_grid(const GridDesc& G, const Prim* __re
     int best = -1;
     best_t = __int_as_float(0x7f800000);
     float prune = kTmax;
-    for (int g = 0; g < G.n_global; ++g)
-        test_element(__ldg(G.global + g), prims, G.aabbs, o, d, inv, tmin, best, best_t, best_type, prune);
     float ta = tmin, tb = kTmax;
     clip_axis(o.z, d.z, inv.z, G.zlo, G.zhi, ta, tb);
     clip_axis(o.x, d.x, inv.x, G.x0, G.x1, ta, tb);
     clip_axis(o.y, d.y, inv.y, G.y0, G.y1, ta, tb);
-    if (!(ta <= tb) || ta > prune) return best;
+    const bool walk = ta <= tb;
     const float px = o.x + ta * d.x, py = o.y + ta * d.y;
     int ix = (int)fminf(fmaxf(floorf((px - G.x0) * G.inv_cell), 0.0f), (float)(G.nx - 1));
     int iy = (int)fminf(fmaxf(floorf((py - G.y0) * G.inv_cell), 0.0f), (float)(G.ny - 1));
     const int sx = d.x > 0.0f ? 1 : -1, sy = d.y > 0.0f ? 1 : -1;
     const float inf = __int_as_float(0x7f800000);
     float tc = ta;
-    for (int step = 0; step <= G.nx + G.ny; ++step) {
-        const int c = iy * G.nx + ix;
-        const uint32_t b = __ldg(G.cell_start + c), e = __ldg(G.cell_start + c + 1);
-        for (uint32_t j = b; j < e; ++j)
-            test_element(__ldg(G.items + j), prims, G.aabbs, o, d, inv, tmin, best, best_t, best_type, prune);
-        // parameters of the next x and y cell boundaries, from the cell index (no accumulation)
-        const float tnx = (d.x != 0.0f) ? (G.x0 + (float)(ix + (sx > 0)) * G.cell - o.x) * inv.x : inf;
-        const float tny = (d.y != 0.0f) ? (G.y0 + (float)(iy + (sy > 0)) * G.cell - o.y) * inv.y : inf;
-        if (tnx < tny) {
-            tc = fmaxf(tc, tnx);
-            ix += sx;
-            if (ix < 0 || ix >= G.nx) break;
-        } else {
-            tc = fmaxf(tc, tny);
-            iy += sy;
-            if (iy < 0 || iy >= G.ny) break;
+    // candidate lists in order: the global elements, then the cells of the walk (one test site)
+    const uint32_t* list = G.global;
+    uint32_t j = 0, e = (uint32_t)G.n_global;
+    int step = -1;
+    for (;;) {
+        for (; j < e; ++j) test_element(__ldg(list + j), prims, G.aabbs, o, d, inv, tmin, best, best_t, best_type, prune);
+        if (step >= 0) {
+            // next cell: parameters of the next x and y cell boundaries, from the cell index
+            const float tnx = (d.x != 0.0f) ? (G.x0 + (float)(ix + (sx > 0)) * G.cell - o.x) * inv.x : inf;
+            const float tny = (d.y != 0.0f) ? (G.y0 + (float)(iy + (sy > 0)) * G.cell - o.y) * inv.y : inf;
+            if (tnx < tny) {
+                tc = fmaxf(tc, tnx);
+                ix += sx;
+                if (ix < 0 || ix >= G.nx) break;
+            } else {
+                tc = fmaxf(tc, tny);
+                iy += sy;
+                if (iy < 0 || iy >= G.ny) break;
+            }
+        } else if (!walk) {
+            break;
         }
-        if (tc > tb || tc > prune) break;
+        if (tc > tb || tc > prune || ++step > G.nx + G.ny) break;
+        const int c = iy * G.nx + ix;
+        list = G.items;
+        j = __ldg(G.cell_start + c);
+        e = __ldg(G.cell_start + c + 1);
     }
     return best;
 }
@@ -706,17 +713,21 @@ __device__ __forceinline__ void push(CoreSmem<kB>& sm, bool want, uint64_t ray, 
 
 // Remainder of a path in phase B, from the closest hit `h` of segment `g`: record, shade, next
 // segment, until the ray misses, is absorbed, ends on the receiver or reaches the depth limit.
+// pending: `h` is a mirror hit whose record was already emitted (phase A), shading comes next.
 template <class C>
 __device__ void finish_path(const TraceArgs& A, const Sink& k, const CoreSmem<C::kB>& sm, uint64_t ray, Segment g,
-                            Hit h) {
+                            Hit h, bool pending) {
     for (;;) {
         if (h.best < 0) return;  // __miss__ms, cuda/materials.cu:236-253
         const Prim p = C::kFlat ? sm.flat.prim[h.best] : load_prim(A.prims, (uint32_t)h.best);
-        float4 rec;
-        int slot;
-        const bool mirror = classify(p, g, h, rec, slot);
-        if (slot >= 0) emit<C>(A, k, ray, slot, rec, (uint32_t)h.best);
-        if (!mirror) return;
+        if (!pending) {
+            float4 rec;
+            int slot;
+            const bool mirror = classify(p, g, h, rec, slot);
+            if (slot >= 0) emit<C>(A, k, ray, slot, rec, (uint32_t)h.best);
+            if (!mirror) return;
+        }
+        pending = false;
         const Optics op = C::kFlat ? sm.flat.optics[h.best] : A.optics[h.best];
         Segment next;
         if (!shade_mirror(A, ray, p, op, g, h, next)) return;
@@ -755,24 +766,16 @@ __device__ void drain(const TraceArgs& A, const Sink& k, CoreSmem<C::kB>& sm, bo
         if (threadIdx.x == 0) sm.qsize = base;
         __syncthreads();
         if (have) {
+            const Segment g{o, d, kTminSun, 0};
+            Hit h;
             if (C::kFlat) {
                 // first segment from the sun: intersection programs of the candidate elements
-                const Segment g{o, d, kTminSun, 0};
-                Hit h;
                 h.best = closest_in(sm.flat, w, o, d, kTminSun, h.t, h.type);
-                finish_path<C>(A, k, sm, ray, g, h);
             } else {
                 // pending mirror hit of the first segment: its record was emitted in phase A
-                const Segment g{o, d, kTminSun, 0};
-                const Hit h{(int)(w & kPrimMask), t, w >> kTypeShift};
-                const Prim p = load_prim(A.prims, (uint32_t)h.best);
-                Segment next;
-                if (shade_mirror(A, ray, p, A.optics[h.best], g, h, next)) {
-                    Hit h2;
-                    h2.best = find_closest<C>(A, sm, next.o, next.d, next.tmin, h2.t, h2.type);
-                    finish_path<C>(A, k, sm, ray, next, h2);
-                }
+                h = Hit{(int)(w & kPrimMask), t, w >> kTypeShift};
             }
+            finish_path<C>(A, k, sm, ray, g, h, !C::kFlat);
         }
         __syncthreads();
         qs = sm.qsize;
