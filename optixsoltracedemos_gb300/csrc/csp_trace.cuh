@@ -53,7 +53,33 @@ struct Cfg {
     static constexpr bool kFlat = kAccel_ == kAccelFlat;
     static constexpr bool kDense = kDense_;
     static constexpr bool kFlux = kFlux_;
+    // grid and BVH launches give each warp 32 rays whose sun-plane points are close together
+    static constexpr bool kCoherent = kAccel_ != kAccelFlat;
 };
+
+// Coherent ray order: position kk of a launch of `count` rays -> ray offset.  Rays come in blocks
+// of 32 S; in a block, the warp at position m takes offsets m + j S (lane j).  The Halton
+// coordinates of offsets that differ by a multiple of S = 2^a 3^b differ by less than 2^-a in u
+// (base 2) and 3^-b in v (base 3), so a warp's rays start within a small patch of the sun plane and
+// walk the same grid cells.  Whole blocks of S = 2^8 3^5 first, then of S = 2^7 3^4 over the rest,
+// then the identity order for the tail: a bijection on [0, count).
+constexpr uint64_t kCoherentS1 = 256u * 243u, kCoherentB1 = 32u * kCoherentS1;
+constexpr uint64_t kCoherentS2 = 128u * 81u, kCoherentB2 = 32u * kCoherentS2;
+
+__device__ __forceinline__ uint64_t coherent_order(uint64_t kk, uint64_t count) {
+    const uint64_t full1 = (count / kCoherentB1) * kCoherentB1;
+    if (kk < full1) {
+        const uint64_t blk = kk / kCoherentB1, r = kk - blk * kCoherentB1;
+        return blk * kCoherentB1 + (r >> 5) + (r & 31u) * kCoherentS1;
+    }
+    const uint64_t k2 = kk - full1;
+    const uint64_t full2 = ((count - full1) / kCoherentB2) * kCoherentB2;
+    if (k2 < full2) {
+        const uint64_t blk = k2 / kCoherentB2, r = k2 - blk * kCoherentB2;
+        return full1 + blk * kCoherentB2 + (r >> 5) + (r & 31u) * kCoherentS2;
+    }
+    return kk;
+}
 
 // ------------------------------------------------------------------------------ sun plane -----
 __device__ __forceinline__ float3 corner(const Aabb& b, int k) {
@@ -823,7 +849,9 @@ __device__ __forceinline__ void trace_tile(const TraceArgs& A, const Sink& k, Co
         id = wi + lane * kMaxDepth;
     }
     const uint64_t kk = tile * C::kB + threadIdx.x;
-    const uint64_t ray = A.ray_begin + kk;
+    uint64_t pos = kk;
+    if constexpr (C::kCoherent) pos = coherent_order(kk, A.count);
+    const uint64_t ray = A.ray_begin + pos;
     if constexpr (C::kDense) {
 #pragma unroll
         for (int s = 0; s < kMaxDepth; ++s) slot[s] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -864,7 +892,19 @@ __device__ __forceinline__ void trace_tile(const TraceArgs& A, const Sink& k, Co
     }
     __syncwarp();
     push<C::kB>(sm, want, ray, g.o, g.d, qt, qw);
-    if constexpr (C::kDense) {
+    if constexpr (C::kDense && C::kCoherent) {
+        // each lane writes its own ray's 80 B row
+        if (kk < A.count) {
+            float4* gh = A.hits + pos * kMaxDepth;
+#pragma unroll
+            for (int s = 0; s < kMaxDepth; ++s) gh[s] = slot[s];
+            if (A.ids) {
+                uint32_t* gi = A.ids + pos * kMaxDepth;
+#pragma unroll
+                for (int s = 0; s < kMaxDepth; ++s) gi[s] = id[s];
+            }
+        }
+    } else if constexpr (C::kDense) {
         // the warp's 32 x 80 B of records leave as 5 fully coalesced 512-byte rows (stride 80 B per
         // lane in shared memory: the 16-byte stores of each quarter warp hit distinct banks)
         const uint64_t warp_first = tile * C::kB + (uint64_t)warp * 32;

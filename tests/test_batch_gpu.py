@@ -127,13 +127,14 @@ def test_batch_groups(gpu):
         reaimed = scenes.reaim(base, sun)
         moved = reaimed.copy()
         moved["origin"][5] += [3.0, -2.0, 0.0]
-        b.add_instance(sid, sun, scenes.SUN_PILLBOX, 4.65e-3, 150000, seed=1, instance=1, poses=reaimed)
+        rays = 1990656 + 331776 + 999  # both coherent block sizes and a tail
+        b.add_instance(sid, sun, scenes.SUN_PILLBOX, 4.65e-3, rays, seed=1, instance=1, poses=reaimed)
         b.add_instance(sid, sun, scenes.SUN_PILLBOX, 4.65e-3, 150000, seed=1, instance=1, poses=moved)
         b.run()
         assert b.tuning(native.GROUP_GRID)[0] in (128, 256)
         assert b.tuning(native.GROUP_BVH)[0] in (128, 256)
-        for i, poses in enumerate((reaimed, moved)):
-            counts, _, _ = _plain_counts(native, poses, sun, scenes.SUN_PILLBOX, 4.65e-3, 150000, 1, 1)
+        for i, (poses, n) in enumerate(((reaimed, rays), (moved, 150000))):
+            counts, _, _ = _plain_counts(native, poses, sun, scenes.SUN_PILLBOX, 4.65e-3, n, 1, 1)
             np.testing.assert_array_equal(b.counts(i), counts)
     finally:
         b.close()

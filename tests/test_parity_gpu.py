@@ -79,6 +79,22 @@ def test_gpu_large_field_bit_exact(gpu, oracle32, accel):
     assert (hits[:, :, 0] == 2).sum() > 1000
 
 
+def test_coherent_order_windows_bit_exact(gpu, oracle32):
+    """Field launches give each warp rays at a Halton-coherent stride (blocks of 1,990,656 rays, then
+    of 331,776, then the identity order): windows in every region of a 2.4M-ray launch, and the
+    block boundaries, against the oracle."""
+    sc = scenes.large_field(n_heliostats=2000, sun=scenes.sun_vector(50.0, -30.0))
+    N = 1990656 + 331776 + 5000
+    t = native.tracer_for(sc, seed=9, num_rays=N)
+    t.run()
+    for first, n in ((0, 20000), (1990656 - 7000, 14000), (1990656 + 331776 - 7000, 12000), (N - 3000, 3000)):
+        hits, ids = t.copy_hits(first, n)
+        oh, oi = oracle32.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, first_ray=first, count=n, seed=9)
+        np.testing.assert_array_equal(ids, oi)
+        np.testing.assert_array_equal(hits, oh.astype(np.float32))
+    t.close()
+
+
 @pytest.mark.parametrize("el,az,parabolic", [(45.0, 0.0, False), (11.0, 80.0, False), (78.0, -100.0, True),
                                               (25.0, 180.0, True)])
 def test_grid_equals_bvh_full_field(gpu, el, az, parabolic):
