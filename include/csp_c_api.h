@@ -241,6 +241,38 @@ CSP_API int csp_batch_get_sun_plane(csp_batch b, uint32_t index, float* out);
 /* setup_s: host element builds and upload; trace_s: device time of refit + sun planes + trace. */
 CSP_API int csp_batch_get_timing(csp_batch b, double* setup_s, double* trace_s);
 
+/* ---- Serving: a request loop with continuous batching ----
+ * A server owns one worker thread, one CUDA stream and a device-memory arena of memory_budget
+ * bytes (0 = half the free device memory, at most 8 GiB).  Scenes are added once and stay resident
+ * (element records, BVH topology, field grid).  csp_server_submit (any thread, non-blocking)
+ * queues a trace request: a scene, optional per-request poses (same count and surfaces: heliostat
+ * tracking, refitted in place on the device), a sun, a ray count, seed and Philox instance id.
+ * The worker admits requests as slots (max_active) and arena memory free up and traces every active
+ * request's next slice of rays (step_rays across all active requests per step, 0 = 64M) in one
+ * persistent launch per kernel group, so requests that arrive while others run share the GPU.
+ * Each request's flux map is accumulated on the device and equals the batch / plain result for the
+ * same inputs, alone or in any mix.  Replaces the reference's one-scene run() loop
+ * (lib/soltrace_system.cpp:145-184) for many concurrent callers. */
+typedef struct csp_server_s* csp_server;
+CSP_API int csp_server_create(csp_server* out, int device, uint64_t memory_budget, uint32_t max_active,
+                              uint64_t step_rays);
+/* Finishes the admitted and queued requests, then stops the worker and frees everything. */
+CSP_API int csp_server_destroy(csp_server s);
+CSP_API int csp_server_add_scene(csp_server s, const csp_element* elements, uint32_t count, uint32_t* scene_id);
+CSP_API int csp_server_submit(csp_server s, uint32_t scene_id, const csp_element* poses, const double* sun_dir,
+                              int sun_shape, double sun_param, uint64_t num_rays, uint64_t seed, uint32_t instance,
+                              uint64_t* request_id);
+/* Block until the request is done (timeout_s < 0: no limit; CSP_ERR_TIMEOUT otherwise), then hand
+ * out its results and forget it: counts[100 * 100] (bin (i, j) at i * 100 + j, as csp_flux_map),
+ * stats[4] (rays, mirror records, receiver records, binned records), latency_s[2] (submission to
+ * completion, submission to admission); any output may be NULL. */
+CSP_API int csp_server_wait(csp_server s, uint64_t request_id, double timeout_s, uint32_t* counts, uint64_t* stats,
+                            double* latency_s);
+/* out[8]: completed requests, rays traced, p50 and p99 latency (s) of the completed requests,
+ * rays/s from the first submission to the last completion, peak active requests, peak arena bytes,
+ * steps. */
+CSP_API int csp_server_stats(csp_server s, double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -28,6 +28,7 @@ SOURCES = [
     "csp_noalloc.cu",
     "csp_batch.cu",
     "csp_batch.cpp",
+    "csp_server.cpp",
     "../cpp/src/dropin.cpp",
 ]
 COMMON = [

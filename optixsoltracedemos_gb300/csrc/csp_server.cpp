@@ -1,0 +1,780 @@
+// csp_server.cpp -- trace-request server with continuous batching (csp_server_* of
+// include/csp_c_api.h).
+//
+// Requests (a resident scene, optional new heliostat poses, a sun, a ray count, seed and instance
+// id) are submitted from any host thread.  One worker thread runs steps:
+//   1. launch step k: every active request traces its next slice of rays in the same persistent
+//      launch per kernel group (the batch kernels of csp_batch.cu), receiver records binned into the
+//      request's resident flux map; requests whose last slice is in the step copy their flux map,
+//      counters and sun frame to pinned host memory behind the launch;
+//   2. while the GPU runs: admit pending requests while slots and device memory allow -- host
+//      element builds (the reference's geometry arithmetic, as the single-scene path), upload,
+//      refit of the scene's BVH topology in place into the request's nodes, sun plane; all queued on
+//      the stream behind step k, so the request joins step k+1;
+//   3. wait for the step, complete the finished requests (latency = completion - submission), free
+//      their device memory.
+// A request's result does not depend on what it was batched with or how its rays were sliced: its
+// rays are traced with the same (seed, instance, ray index) and its flux map is an integer sum.
+//
+// Device memory: one arena of the configured budget, first-fit blocks per request (element
+// records when the request has its own poses, refitted nodes, sun frame, flux map).  A request is
+// admitted when its block fits; requests larger than the whole budget fail.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "csp_c_api.h"
+#include "csp_kernels.cuh"
+#include "csp_scene.h"
+#include "csp_system.h"
+
+namespace csp {
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct SScene {
+    std::vector<csp_element> elements;
+    HostScene base;
+    HostGrid grid;
+    int group = kAccelBvh;
+    Node* d_topo = nullptr;
+    uint32_t* d_cells = nullptr;
+    uint32_t* d_items = nullptr;
+    uint32_t* d_global = nullptr;
+    // the scene's own element records, for requests without poses
+    Prim* d_prims = nullptr;
+    Optics* d_optics = nullptr;
+    Aabb* d_aabbs = nullptr;
+    Node* d_nodes = nullptr;
+    float zlo = 0.f, zhi = 0.f;
+};
+
+enum ReqState { kPending = 0, kActive = 1, kDone = 2, kFailed = 3 };
+
+struct SRequest {
+    uint64_t id = 0;
+    uint32_t scene = 0;
+    const SScene* sc = nullptr;  // set at submission (the scene list may grow meanwhile)
+    std::vector<csp_element> poses;
+    double sun[3] = {0, 0, 1};
+    int shape = CSP_SUN_PILLBOX;
+    double param = 0;
+    uint64_t rays = 0, seed = 0;
+    uint32_t instance = 0;
+
+    ReqState state = kPending;
+    std::string error;
+    uint64_t next_ray = 0;
+    int group = kAccelBvh;
+    size_t off = 0, bytes = 0;  // arena block
+    size_t o_prims = 0, o_optics = 0, o_aabbs = 0, o_prune = 0, o_nodes = 0, o_sun = 0, o_grid = 0, o_counts = 0,
+           o_stats = 0;
+    bool own_records = false;
+    int result_slot = -1;
+    Clock::time_point t_submit, t_admit, t_done;
+    std::vector<uint32_t> counts;
+    uint64_t stats[4] = {0, 0, 0, 0};
+    SunFrame sunf{};
+};
+
+// First-fit allocator over [0, cap) with coalescing frees.
+struct Arena {
+    size_t cap = 0, used = 0, peak = 0;
+    std::map<size_t, size_t> free_blocks;  // offset -> size
+    void reset(size_t c) {
+        cap = c;
+        used = peak = 0;
+        free_blocks.clear();
+        if (c) free_blocks[0] = c;
+    }
+    bool alloc(size_t bytes, size_t& off) {
+        for (auto it = free_blocks.begin(); it != free_blocks.end(); ++it) {
+            if (it->second >= bytes) {
+                off = it->first;
+                const size_t rest = it->second - bytes;
+                free_blocks.erase(it);
+                if (rest) free_blocks[off + bytes] = rest;
+                used += bytes;
+                peak = std::max(peak, used);
+                return true;
+            }
+        }
+        return false;
+    }
+    void release(size_t off, size_t bytes) {
+        used -= bytes;
+        auto it = free_blocks.emplace(off, bytes).first;
+        auto nx = std::next(it);
+        if (nx != free_blocks.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_blocks.erase(nx);
+        }
+        if (it != free_blocks.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_blocks.erase(it);
+            }
+        }
+    }
+};
+
+}  // namespace
+
+struct Server {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    uint32_t nx = 100, ny = 100;
+    int max_active = 64;
+    uint64_t step_rays = 64ull << 20;  // rays per step across all active requests (target)
+    size_t budget = 0;
+
+    std::vector<std::unique_ptr<SScene>> scenes;
+    std::map<uint64_t, std::unique_ptr<SRequest>> requests;
+    std::deque<SRequest*> pending;
+    std::vector<SRequest*> active;
+    uint64_t next_id = 1;
+    // refit and sun-plane job tables of one admission round (at most max_active requests); the
+    // kernels that read them finish at the step synchronisation before the next round
+    unsigned char* d_jobs = nullptr;
+    size_t jobs_cap = 0;
+
+    unsigned char* d_arena = nullptr;
+    Arena arena;
+    // per-step device tables and their pinned staging
+    unsigned char* d_step = nullptr;
+    unsigned char* h_step = nullptr;
+    size_t step_bytes = 0;
+    // admission staging (pinned) and results (pinned, one slot per active request)
+    unsigned char* h_adm = nullptr;
+    size_t adm_cap = 0;
+    unsigned char* h_res = nullptr;
+    size_t res_slot_bytes = 0;
+    std::vector<int> free_res_slots;
+    unsigned long long* d_counter = nullptr;
+
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::thread worker;
+    bool stopping = false;
+    std::string fatal;
+
+    // statistics
+    std::vector<double> latencies;  // seconds, completed requests
+    uint64_t rays_done = 0, completed = 0, steps = 0;
+    int peak_active = 0;
+    bool have_first = false;
+    Clock::time_point t_first_submit, t_last_done;
+
+    ~Server();
+    int start(int dev, size_t budget_bytes, int max_act, uint64_t step_target);
+    void stop();
+    int add_scene(const csp_element* el, uint32_t n, uint32_t* id);
+    int submit(const SRequest& r, uint64_t* id);
+    void run_worker();
+    size_t request_bytes(const SRequest& r) const;
+    int admit(std::vector<SRequest*>& admitted, std::string& err);
+    int step_launch(std::vector<SRequest*>& finishing, uint64_t& rays);
+};
+
+Server::~Server() { stop(); }
+
+void Server::stop() {
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        stopping = true;
+    }
+    cv_work.notify_all();
+    if (worker.joinable()) worker.join();
+    if (device >= 0) cudaSetDevice(device);
+    if (stream) cudaStreamSynchronize(stream);
+    for (auto& s : scenes) {
+        cudaFree(s->d_topo);
+        cudaFree(s->d_cells);
+        cudaFree(s->d_items);
+        cudaFree(s->d_global);
+        cudaFree(s->d_prims);
+        cudaFree(s->d_optics);
+        cudaFree(s->d_aabbs);
+        cudaFree(s->d_nodes);
+    }
+    scenes.clear();
+    cudaFree(d_arena);
+    cudaFree(d_step);
+    cudaFree(d_counter);
+    cudaFree(d_jobs);
+    d_jobs = nullptr;
+    if (h_step) cudaFreeHost(h_step);
+    if (h_adm) cudaFreeHost(h_adm);
+    if (h_res) cudaFreeHost(h_res);
+    d_arena = d_step = nullptr;
+    d_counter = nullptr;
+    h_step = h_adm = h_res = nullptr;
+    if (stream) cudaStreamDestroy(stream);
+    stream = nullptr;
+}
+
+int Server::start(int dev, size_t budget_bytes, int max_act, uint64_t step_target) {
+    device = dev;
+    max_active = std::max(1, std::min(max_act, 4096));
+    step_rays = std::max<uint64_t>(step_target, 1u << 20);
+    int rc = cuda_status(cudaSetDevice(device), "cudaSetDevice");
+    if (rc) return rc;
+    if ((rc = cuda_status(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate"))) return rc;
+    size_t free_b = 0, total_b = 0;
+    if ((rc = cuda_status(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo"))) return rc;
+    budget = budget_bytes ? budget_bytes : std::min<size_t>(free_b / 2, (size_t)8 << 30);
+    if (budget > free_b) return set_error(CSP_ERR_OUT_OF_MEMORY, "server memory budget exceeds free device memory");
+    if ((rc = cuda_status(cudaMalloc((void**)&d_arena, budget), "cudaMalloc server arena"))) return rc;
+    arena.reset(budget);
+    step_bytes = align256((size_t)max_active * sizeof(InstanceDesc)) * kBatchGroups +
+                 align256((size_t)(max_active + 1) * sizeof(uint64_t)) * kBatchGroups;
+    if ((rc = cuda_status(cudaMalloc((void**)&d_step, step_bytes), "cudaMalloc step tables"))) return rc;
+    if ((rc = cuda_status(cudaHostAlloc((void**)&h_step, step_bytes, cudaHostAllocDefault), "cudaHostAlloc"))) return rc;
+    if ((rc = cuda_status(cudaMalloc((void**)&d_counter, kBatchGroups * sizeof(unsigned long long)), "cudaMalloc")))
+        return rc;
+    jobs_cap = align256((size_t)max_active * sizeof(RefitJob)) + align256((size_t)max_active * sizeof(SunJob));
+    if ((rc = cuda_status(cudaMalloc((void**)&d_jobs, jobs_cap), "cudaMalloc job tables"))) return rc;
+    res_slot_bytes = align256((size_t)nx * ny * sizeof(uint32_t) + 4 * sizeof(unsigned long long) + sizeof(SunFrame));
+    if ((rc = cuda_status(cudaHostAlloc((void**)&h_res, res_slot_bytes * max_active, cudaHostAllocDefault),
+                          "cudaHostAlloc results")))
+        return rc;
+    for (int k = max_active - 1; k >= 0; --k) free_res_slots.push_back(k);
+    worker = std::thread([this] { run_worker(); });
+    return CSP_OK;
+}
+
+int Server::add_scene(const csp_element* el, uint32_t n, uint32_t* id) {
+    auto s = std::make_unique<SScene>();
+    s->elements.assign(el, el + n);
+    std::string err;
+    int rc = build_elements(el, n, s->base, err);
+    if (rc) return set_error(rc, err);
+    build_bvh(s->base);
+    if (n > kFlatListMax) build_grid(el, n, s->base, s->grid);
+    s->group = n <= kFlatListMax ? kAccelFlat : (s->grid.valid ? kAccelGrid : kAccelBvh);
+    if (s->grid.valid) grid_layer(s->grid, s->base, s->zlo, s->zhi);
+    auto put = [&](auto*& dptr, const auto& host, const char* what) {
+        const size_t bytes = std::max<size_t>(1, host.size()) * sizeof(host[0]);
+        int r = cuda_status(cudaMalloc((void**)&dptr, bytes), what);
+        if (!r && !host.empty())
+            r = cuda_status(cudaMemcpy(dptr, host.data(), host.size() * sizeof(host[0]), cudaMemcpyHostToDevice), what);
+        return r;
+    };
+    rc = put(s->d_topo, s->base.nodes, "upload topology");
+    if (!rc) rc = put(s->d_nodes, s->base.nodes, "upload nodes");
+    if (!rc) rc = put(s->d_prims, s->base.prims, "upload prims");
+    if (!rc) rc = put(s->d_optics, s->base.optics, "upload optics");
+    if (!rc) rc = put(s->d_aabbs, s->base.aabbs, "upload aabbs");
+    if (!rc && s->grid.valid) rc = put(s->d_cells, s->grid.cell_start, "upload grid cells");
+    if (!rc && s->grid.valid) rc = put(s->d_items, s->grid.items, "upload grid items");
+    if (!rc && s->grid.valid) rc = put(s->d_global, s->grid.global, "upload grid globals");
+    std::lock_guard<std::mutex> lk(mu);
+    scenes.push_back(std::move(s));
+    if (rc) return rc;
+    if (id) *id = (uint32_t)(scenes.size() - 1);
+    return CSP_OK;
+}
+
+size_t Server::request_bytes(const SRequest& r) const {
+    const SScene& s = *r.sc;
+    const size_t n = s.elements.size();
+    size_t b = align256(sizeof(SunFrame)) + align256(sizeof(GridDesc)) + align256((size_t)nx * ny * sizeof(uint32_t)) +
+               align256(4 * sizeof(unsigned long long));
+    if (!r.poses.empty()) {
+        b += align256(n * sizeof(Prim)) + align256(n * sizeof(Optics)) + 2 * align256(n * sizeof(Aabb));
+        if (r.group != kAccelGrid) b += align256(s.base.nodes.size() * sizeof(Node));
+    }
+    return b;
+}
+
+int Server::submit(const SRequest& in, uint64_t* id) {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!fatal.empty()) return set_error(CSP_ERR_CUDA, "server stopped: " + fatal);
+    if (in.scene >= scenes.size()) return set_error(CSP_ERR_INVALID_ARGUMENT, "no such scene");
+    const SScene& s = *scenes[in.scene];
+    if (!in.poses.empty()) {
+        if (in.poses.size() != s.elements.size())
+            return set_error(CSP_ERR_BAD_SCENE, "request poses must have the scene's element count");
+        for (size_t k = 0; k < s.elements.size(); ++k)
+            if (in.poses[k].surface != s.elements[k].surface || in.poses[k].aperture != s.elements[k].aperture)
+                return set_error(CSP_ERR_BAD_SCENE, "request pose " + std::to_string(k) + " changes the surface type");
+    }
+    if (in.shape != CSP_SUN_PILLBOX && in.shape != CSP_SUN_GAUSSIAN)
+        return set_error(CSP_ERR_INVALID_ARGUMENT, "unknown sun shape");
+    if (!(in.param >= 0.0) || in.param > 0.5) return set_error(CSP_ERR_INVALID_ARGUMENT, "sun shape parameter out of range");
+    if (in.rays == 0 || in.rays >= (1ull << 40)) return set_error(CSP_ERR_INVALID_ARGUMENT, "bad ray count");
+    auto r = std::make_unique<SRequest>(in);
+    r->id = next_id++;
+    r->sc = &s;
+    r->group = s.group;
+    if (r->group == kAccelGrid && !r->poses.empty() &&
+        !grid_accepts(s.grid, r->poses.data(), (uint32_t)r->poses.size()))
+        r->group = kAccelBvh;  // poses move an origin or change a size: the scene's grid does not hold
+    r->bytes = request_bytes(*r);
+    if (r->bytes > budget) return set_error(CSP_ERR_OUT_OF_MEMORY, "request larger than the server memory budget");
+    r->t_submit = Clock::now();
+    if (!have_first) {
+        have_first = true;
+        t_first_submit = r->t_submit;
+    }
+    if (id) *id = r->id;
+    pending.push_back(r.get());
+    requests[r->id] = std::move(r);
+    cv_work.notify_one();
+    return CSP_OK;
+}
+
+// Move pending requests into device memory while slots and memory last; queue their uploads,
+// refits and sun planes on the stream.  Called with the lock NOT held.
+int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        while (!pending.empty() && (int)(active.size() + admitted.size()) < max_active && !free_res_slots.empty()) {
+            SRequest* r = pending.front();
+            size_t off = 0;
+            if (!arena.alloc(r->bytes, off)) break;  // wait for completions to free memory
+            pending.pop_front();
+            r->off = off;
+            r->result_slot = free_res_slots.back();
+            free_res_slots.pop_back();
+            admitted.push_back(r);
+        }
+    }
+    if (admitted.empty()) return CSP_OK;
+    // layout inside each block; host builds into pinned staging
+    size_t stage = 0;
+    std::vector<size_t> stage_off(admitted.size());
+    for (size_t i = 0; i < admitted.size(); ++i) {
+        SRequest& r = *admitted[i];
+        const SScene& s = *r.sc;
+        const size_t n = s.elements.size();
+        size_t o = r.off;
+        r.o_sun = o;
+        o += align256(sizeof(SunFrame));
+        r.o_grid = o;
+        o += align256(sizeof(GridDesc));
+        r.o_counts = o;
+        o += align256((size_t)nx * ny * sizeof(uint32_t));
+        r.o_stats = o;
+        o += align256(4 * sizeof(unsigned long long));
+        r.own_records = !r.poses.empty();
+        if (r.own_records) {
+            r.o_prims = o;
+            o += align256(n * sizeof(Prim));
+            r.o_optics = o;
+            o += align256(n * sizeof(Optics));
+            r.o_aabbs = o;
+            o += align256(n * sizeof(Aabb));
+            r.o_prune = o;
+            o += align256(n * sizeof(Aabb));
+            if (r.group != kAccelGrid) {
+                r.o_nodes = o;
+                o += align256(s.base.nodes.size() * sizeof(Node));
+            }
+        }
+        stage_off[i] = stage;
+        if (r.own_records) stage += n * (sizeof(Prim) + sizeof(Optics) + 2 * sizeof(Aabb));
+        stage = align256(stage + sizeof(GridDesc));
+    }
+    const size_t refit_at = stage;
+    stage += align256(admitted.size() * sizeof(RefitJob));
+    const size_t sun_at = stage;
+    stage += align256(admitted.size() * sizeof(SunJob));
+    if (stage > adm_cap) {
+        // the previous round's uploads from h_adm finished at the step synchronisation before this call
+        if (h_adm) cudaFreeHost(h_adm);
+        h_adm = nullptr;
+        adm_cap = 0;
+        int rc = cuda_status(cudaHostAlloc((void**)&h_adm, stage, cudaHostAllocDefault), "cudaHostAlloc admission");
+        if (rc) return rc;
+        adm_cap = stage;
+    }
+    HostScene hs;
+    RefitJob* refits = reinterpret_cast<RefitJob*>(h_adm + refit_at);
+    SunJob* suns = reinterpret_cast<SunJob*>(h_adm + sun_at);
+    int n_refit = 0, n_sun = 0, max_nodes = 0;
+    for (size_t i = 0; i < admitted.size(); ++i) {
+        SRequest& r = *admitted[i];
+        const SScene& s = *r.sc;
+        const uint32_t n = (uint32_t)s.elements.size();
+        unsigned char* h = h_adm + stage_off[i];
+        const HostScene* src = &s.base;
+        const Aabb* d_aabbs = s.d_aabbs;
+        if (r.own_records) {
+            int rc = build_elements(r.poses.data(), n, hs, err);
+            if (rc) {
+                r.state = kFailed;
+                r.error = err;
+                continue;
+            }
+            src = &hs;
+            const size_t bp = n * sizeof(Prim), bo = n * sizeof(Optics), ba = n * sizeof(Aabb);
+            std::memcpy(h, hs.prims.data(), bp);
+            std::memcpy(h + bp, hs.optics.data(), bo);
+            std::memcpy(h + bp + bo, hs.aabbs.data(), ba);
+            std::memcpy(h + bp + bo + ba, hs.prune.data(), ba);
+            int rc2 = cuda_status(cudaMemcpyAsync(d_arena + r.o_prims, h, bp, cudaMemcpyHostToDevice, stream), "upload");
+            if (!rc2) rc2 = cuda_status(cudaMemcpyAsync(d_arena + r.o_optics, h + bp, bo, cudaMemcpyHostToDevice, stream), "upload");
+            if (!rc2) rc2 = cuda_status(cudaMemcpyAsync(d_arena + r.o_aabbs, h + bp + bo, ba, cudaMemcpyHostToDevice, stream), "upload");
+            if (!rc2) rc2 = cuda_status(cudaMemcpyAsync(d_arena + r.o_prune, h + bp + bo + ba, ba, cudaMemcpyHostToDevice, stream), "upload");
+            if (rc2) return rc2;
+            h += bp + bo + 2 * ba;
+            d_aabbs = reinterpret_cast<const Aabb*>(d_arena + r.o_aabbs);
+            if (r.group != kAccelGrid) {
+                RefitJob& j = refits[n_refit++];
+                j.topo = s.d_topo;
+                j.aabbs = d_aabbs;
+                j.prune = reinterpret_cast<const Aabb*>(d_arena + r.o_prune);
+                j.out = reinterpret_cast<Node*>(d_arena + r.o_nodes);
+                j.n_nodes = (int)s.base.nodes.size();
+                j.pad = 0;
+                max_nodes = std::max(max_nodes, j.n_nodes);
+            }
+        }
+        if (r.group == kAccelGrid) {
+            GridDesc g;
+            g.x0 = s.grid.x0;
+            g.y0 = s.grid.y0;
+            g.x1 = s.grid.x1;
+            g.y1 = s.grid.y1;
+            g.cell = s.grid.cell;
+            g.inv_cell = s.grid.inv_cell;
+            if (r.own_records) grid_layer(s.grid, *src, g.zlo, g.zhi);
+            else {
+                g.zlo = s.zlo;
+                g.zhi = s.zhi;
+            }
+            g.nx = s.grid.nx;
+            g.ny = s.grid.ny;
+            g.n_global = (int)s.grid.global.size();
+            g.pad = 0;
+            g.cell_start = s.d_cells;
+            g.items = s.d_items;
+            g.global = s.d_global;
+            g.aabbs = d_aabbs;
+            std::memcpy(h, &g, sizeof g);
+            int rc2 = cuda_status(cudaMemcpyAsync(d_arena + r.o_grid, h, sizeof g, cudaMemcpyHostToDevice, stream), "upload");
+            if (rc2) return rc2;
+        }
+        float sv[3];
+        sun_vector_f(r.sun, sv);
+        SunJob& sj = suns[n_sun++];
+        sj.aabbs = d_aabbs;
+        sj.n = (int)n;
+        sj.sx = sv[0];
+        sj.sy = sv[1];
+        sj.sz = sv[2];
+        sj.tan_pad = tanf((float)(r.shape == CSP_SUN_GAUSSIAN ? 5.0 * r.param : r.param));
+        sj.shape = r.shape;
+        sj.param = (float)r.param;
+        sj.out = reinterpret_cast<SunFrame*>(d_arena + r.o_sun);
+        int rc2 = cuda_status(cudaMemsetAsync(d_arena + r.o_counts, 0, (size_t)nx * ny * sizeof(uint32_t), stream), "memset");
+        if (!rc2) rc2 = cuda_status(cudaMemsetAsync(d_arena + r.o_stats, 0, 4 * sizeof(unsigned long long), stream), "memset");
+        if (rc2) return rc2;
+        r.t_admit = Clock::now();
+    }
+    if (n_sun == 0) return CSP_OK;
+    // job tables: an arena block released once the stream has passed the kernels that read them
+    const size_t job_bytes = stage - refit_at;
+    if (job_bytes > jobs_cap) return set_error(CSP_ERR_STATE, "admission job tables exceed their buffer");
+    int rc = cuda_status(cudaMemcpyAsync(d_jobs, h_adm + refit_at, job_bytes, cudaMemcpyHostToDevice, stream),
+                         "upload admission jobs");
+    if (!rc && n_refit)
+        rc = cuda_status(launch_refit(reinterpret_cast<const RefitJob*>(d_jobs), n_refit, max_nodes, stream),
+                         "refit_kernel");
+    if (!rc)
+        rc = cuda_status(
+            launch_prepare_sun_batch(reinterpret_cast<const SunJob*>(d_jobs + (sun_at - refit_at)), n_sun, stream),
+            "prepare_sun_batch_kernel");
+    return rc;
+}
+
+// Queue one step over the active requests; `finishing` receives the requests whose last rays are in
+// it (their results are copied behind the launch).
+int Server::step_launch(std::vector<SRequest*>& finishing, uint64_t& rays) {
+    rays = 0;
+    finishing.clear();
+    if (active.empty()) return CSP_OK;
+    const uint64_t quantum = std::max<uint64_t>(1u << 20, step_rays / active.size());
+    std::vector<InstanceDesc> desc[kBatchGroups];
+    std::vector<uint64_t> tb[kBatchGroups];
+    uint64_t tiles[kBatchGroups] = {};
+    const int block = 128;
+    const size_t desc_stride = align256((size_t)max_active * sizeof(InstanceDesc));
+    const size_t tb_base = desc_stride * kBatchGroups;
+    const size_t tb_stride = align256((size_t)(max_active + 1) * sizeof(uint64_t));
+    for (SRequest* r : active) {
+        const SScene& s = *r->sc;
+        const int g = r->group;
+        const uint64_t slice = std::min<uint64_t>(quantum, r->rays - r->next_ray);
+        InstanceDesc d{};
+        d.args.nodes = r->own_records && g != kAccelGrid ? reinterpret_cast<const Node*>(d_arena + r->o_nodes) : s.d_nodes;
+        d.args.prims = r->own_records ? reinterpret_cast<const Prim*>(d_arena + r->o_prims) : s.d_prims;
+        d.args.optics = r->own_records ? reinterpret_cast<const Optics*>(d_arena + r->o_optics) : s.d_optics;
+        d.args.sun = reinterpret_cast<const SunFrame*>(d_arena + r->o_sun);
+        d.args.hits = nullptr;
+        d.args.ids = nullptr;
+        d.args.ray_begin = r->next_ray;
+        d.args.count = slice;
+        d.args.seed = r->seed;
+        d.args.instance = r->instance;
+        d.args.pad = 0;
+        d.args.grid = g == kAccelGrid ? reinterpret_cast<const GridDesc*>(d_arena + r->o_grid) : nullptr;
+        const csp_element& rcv = (r->poses.empty() ? s.elements : r->poses).back();
+        flux_target(rcv, nx, ny, d.flux);
+        d.flux.counts = reinterpret_cast<uint32_t*>(d_arena + r->o_counts);
+        d.flux.stats = reinterpret_cast<unsigned long long*>(d_arena + r->o_stats);
+        d.tile_begin = tiles[g];
+        d.n_prims = (int)s.elements.size();
+        tb[g].push_back(tiles[g]);
+        tiles[g] += (slice + block - 1) / block;
+        desc[g].push_back(d);
+        r->next_ray += slice;
+        rays += slice;
+        if (r->next_ray >= r->rays) finishing.push_back(r);
+    }
+    for (int g = 0; g < kBatchGroups; ++g) {
+        tb[g].push_back(tiles[g]);
+        if (!desc[g].empty())
+            std::memcpy(h_step + desc_stride * g, desc[g].data(), desc[g].size() * sizeof(InstanceDesc));
+        std::memcpy(h_step + tb_base + tb_stride * g, tb[g].data(), tb[g].size() * sizeof(uint64_t));
+    }
+    int rc = cuda_status(cudaMemcpyAsync(d_step, h_step, step_bytes, cudaMemcpyHostToDevice, stream), "upload step");
+    if (!rc) rc = cuda_status(cudaMemsetAsync(d_counter, 0, kBatchGroups * sizeof(unsigned long long), stream), "memset");
+    for (int g = 0; g < kBatchGroups && !rc; ++g) {
+        if (desc[g].empty()) continue;
+        BatchLaunch L;
+        L.inst = reinterpret_cast<const InstanceDesc*>(d_step + desc_stride * g);
+        L.tile_begin = reinterpret_cast<const uint64_t*>(d_step + tb_base + tb_stride * g);
+        L.n_inst = (int)desc[g].size();
+        L.chunk = 4;
+        L.total_tiles = tiles[g];
+        L.next_tile = d_counter + g;
+        rc = cuda_status(launch_trace_batch(L, g, BatchTuning{block, 0, 4}, stream), "batch_kernel");
+    }
+    for (SRequest* r : finishing) {
+        if (rc) break;
+        unsigned char* slot = h_res + res_slot_bytes * r->result_slot;
+        rc = cuda_status(cudaMemcpyAsync(slot, d_arena + r->o_counts, (size_t)nx * ny * sizeof(uint32_t),
+                                         cudaMemcpyDeviceToHost, stream),
+                         "D2H flux map");
+        if (!rc)
+            rc = cuda_status(cudaMemcpyAsync(slot + (size_t)nx * ny * sizeof(uint32_t), d_arena + r->o_stats,
+                                             4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream),
+                             "D2H stats");
+        if (!rc)
+            rc = cuda_status(cudaMemcpyAsync(slot + (size_t)nx * ny * sizeof(uint32_t) + 4 * sizeof(unsigned long long),
+                                             d_arena + r->o_sun, sizeof(SunFrame), cudaMemcpyDeviceToHost, stream),
+                             "D2H sun frame");
+    }
+    return rc;
+}
+
+void Server::run_worker() {
+    cudaSetDevice(device);
+    std::vector<SRequest*> finishing, admitted;
+    for (;;) {
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            cv_work.wait(lk, [&] { return stopping || !pending.empty() || !active.empty(); });
+            if (stopping && pending.empty() && active.empty()) break;
+        }
+        uint64_t rays = 0;
+        std::string err;
+        // 1. launch the step over the requests already active
+        int rc = step_launch(finishing, rays);
+        // 2. admit while it runs
+        admitted.clear();
+        if (!rc) rc = admit(admitted, err);
+        if (!rc && finishing.empty() && active.empty() && admitted.empty()) {
+            // nothing fits yet (memory) and nothing runs: cannot happen, a request never exceeds
+            // the budget; guard against a spin anyway
+            std::unique_lock<std::mutex> lk(mu);
+            cv_work.wait_for(lk, std::chrono::milliseconds(1));
+        }
+        // 3. wait for the step (and the admissions' setup queued behind it)
+        if (!rc) rc = cuda_status(cudaStreamSynchronize(stream), "server step");
+        const Clock::time_point now = Clock::now();
+        std::lock_guard<std::mutex> lk(mu);
+        if (rc) {
+            fatal = csp_last_error();
+            for (SRequest* r : active) {
+                r->state = kFailed;
+                r->error = fatal;
+            }
+            for (SRequest* r : admitted) {
+                r->state = kFailed;
+                r->error = fatal;
+            }
+            for (SRequest* r : pending) {
+                r->state = kFailed;
+                r->error = fatal;
+            }
+            active.clear();
+            pending.clear();
+            cv_done.notify_all();
+            break;
+        }
+        if (rays) ++steps;
+        rays_done += rays;
+        for (SRequest* r : finishing) {
+            const unsigned char* slot = h_res + res_slot_bytes * r->result_slot;
+            r->counts.assign(reinterpret_cast<const uint32_t*>(slot),
+                             reinterpret_cast<const uint32_t*>(slot) + (size_t)nx * ny);
+            std::memcpy(r->stats, slot + (size_t)nx * ny * sizeof(uint32_t), 4 * sizeof(uint64_t));
+            r->stats[0] = r->rays;
+            std::memcpy(&r->sunf, slot + (size_t)nx * ny * sizeof(uint32_t) + 4 * sizeof(unsigned long long),
+                        sizeof(SunFrame));
+            r->state = kDone;
+            r->t_done = now;
+            t_last_done = now;
+            latencies.push_back(std::chrono::duration<double>(r->t_done - r->t_submit).count());
+            ++completed;
+            arena.release(r->off, r->bytes);
+            free_res_slots.push_back(r->result_slot);
+            r->result_slot = -1;
+            active.erase(std::find(active.begin(), active.end(), r));
+        }
+        for (SRequest* r : admitted) {
+            if (r->state == kFailed) {
+                arena.release(r->off, r->bytes);
+                free_res_slots.push_back(r->result_slot);
+                continue;
+            }
+            r->state = kActive;
+            active.push_back(r);
+        }
+        peak_active = std::max(peak_active, (int)active.size());
+        if (!finishing.empty() || !admitted.empty()) cv_done.notify_all();
+    }
+}
+
+}  // namespace csp
+
+using csp::Server;
+
+#define CSP_SGUARD(s)                                                                      \
+    do {                                                                                   \
+        if (!(s)) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "null server handle");    \
+    } while (0)
+
+extern "C" {
+
+int csp_server_create(csp_server* out, int device, uint64_t memory_budget, uint32_t max_active, uint64_t step_rays) {
+    if (!out) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "null output handle");
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess) return csp::cuda_status(e, "cudaGetDeviceCount");
+    if (device < 0 || device >= count) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "no such CUDA device");
+    Server* s = new (std::nothrow) Server();
+    if (!s) return csp::set_error(CSP_ERR_OUT_OF_MEMORY, "host allocation failed");
+    const int rc = s->start(device, (size_t)memory_budget, max_active ? (int)max_active : 64,
+                            step_rays ? step_rays : (64ull << 20));
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    *out = reinterpret_cast<csp_server>(s);
+    return CSP_OK;
+}
+
+int csp_server_destroy(csp_server sh) {
+    CSP_SGUARD(sh);
+    delete reinterpret_cast<Server*>(sh);
+    return CSP_OK;
+}
+
+int csp_server_add_scene(csp_server sh, const csp_element* el, uint32_t n, uint32_t* id) {
+    CSP_SGUARD(sh);
+    if (!el || n == 0) return csp::set_error(CSP_ERR_BAD_SCENE, "scene has no elements");
+    return reinterpret_cast<Server*>(sh)->add_scene(el, n, id);
+}
+
+int csp_server_submit(csp_server sh, uint32_t scene, const csp_element* poses, const double* sun, int shape,
+                      double param, uint64_t rays, uint64_t seed, uint32_t instance, uint64_t* request) {
+    CSP_SGUARD(sh);
+    if (!sun) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "null sun vector");
+    Server* s = reinterpret_cast<Server*>(sh);
+    csp::SRequest r;
+    r.scene = scene;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (poses && scene < s->scenes.size()) r.poses.assign(poses, poses + s->scenes[scene]->elements.size());
+    }
+    r.sun[0] = sun[0];
+    r.sun[1] = sun[1];
+    r.sun[2] = sun[2];
+    r.shape = shape;
+    r.param = param;
+    r.rays = rays;
+    r.seed = seed;
+    r.instance = instance;
+    return s->submit(r, request);
+}
+
+int csp_server_wait(csp_server sh, uint64_t request, double timeout_s, uint32_t* counts, uint64_t* stats,
+                    double* latency_s) {
+    CSP_SGUARD(sh);
+    Server* s = reinterpret_cast<Server*>(sh);
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->requests.find(request);
+    if (it == s->requests.end()) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "no such request");
+    csp::SRequest* r = it->second.get();
+    auto done = [&] { return r->state == csp::kDone || r->state == csp::kFailed; };
+    if (timeout_s < 0) s->cv_done.wait(lk, done);
+    else if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), done))
+        return csp::set_error(CSP_ERR_TIMEOUT, "request not finished within the timeout");
+    if (r->state == csp::kFailed) {
+        const std::string msg = r->error;
+        s->requests.erase(it);
+        return csp::set_error(CSP_ERR_CUDA, "request failed: " + msg);
+    }
+    if (counts) std::memcpy(counts, r->counts.data(), r->counts.size() * sizeof(uint32_t));
+    if (stats) std::memcpy(stats, r->stats, sizeof r->stats);
+    if (latency_s) {
+        latency_s[0] = std::chrono::duration<double>(r->t_done - r->t_submit).count();
+        latency_s[1] = std::chrono::duration<double>(r->t_admit - r->t_submit).count();
+    }
+    s->requests.erase(it);
+    return CSP_OK;
+}
+
+int csp_server_stats(csp_server sh, double* out) {
+    CSP_SGUARD(sh);
+    if (!out) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "null output");
+    Server* s = reinterpret_cast<Server*>(sh);
+    std::lock_guard<std::mutex> lk(s->mu);
+    std::vector<double> l = s->latencies;
+    std::sort(l.begin(), l.end());
+    auto pct = [&](double p) {
+        if (l.empty()) return 0.0;
+        const size_t k = (size_t)std::min<double>((double)l.size() - 1, std::ceil(p * l.size()) - 1);
+        return l[k];
+    };
+    const double span = s->completed ? std::chrono::duration<double>(s->t_last_done - s->t_first_submit).count() : 0.0;
+    out[0] = (double)s->completed;
+    out[1] = (double)s->rays_done;
+    out[2] = pct(0.50);
+    out[3] = pct(0.99);
+    out[4] = span > 0 ? (double)s->rays_done / span : 0.0;
+    out[5] = (double)s->peak_active;
+    out[6] = (double)s->arena.peak;
+    out[7] = (double)s->steps;
+    return CSP_OK;
+}
+
+}  // extern "C"

@@ -86,6 +86,14 @@ SIGNATURES = {
     "csp_batch_get_stats": (ctypes.c_int, [_H, ctypes.c_uint32, _P]),
     "csp_batch_get_sun_plane": (ctypes.c_int, [_H, ctypes.c_uint32, _P]),
     "csp_batch_get_timing": (ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    "csp_server_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_uint64,
+                                         ctypes.c_uint32, ctypes.c_uint64]),
+    "csp_server_destroy": (ctypes.c_int, [_H]),
+    "csp_server_add_scene": (ctypes.c_int, [_H, _P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]),
+    "csp_server_submit": (ctypes.c_int, [_H, ctypes.c_uint32, _P, _P, ctypes.c_int, ctypes.c_double, ctypes.c_uint64,
+                                         ctypes.c_uint64, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)]),
+    "csp_server_wait": (ctypes.c_int, [_H, ctypes.c_uint64, ctypes.c_double, _P, _P, _P]),
+    "csp_server_stats": (ctypes.c_int, [_H, _P]),
 }
 STINPUT_APPLY_OPTICS = 1
 ACCEL_AUTO, ACCEL_BVH, ACCEL_GRID, ACCEL_LIST = 0, 1, 2, 3
@@ -350,6 +358,69 @@ class Batch:
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:
             _check(self.lib.csp_batch_destroy(self.h))
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class Server:
+    """One csp_server: a request loop with continuous batching over resident scenes."""
+
+    def __init__(self, device: int = 0, memory_budget: int = 0, max_active: int = 64, step_rays: int = 0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        _check(self.lib.csp_server_create(ctypes.byref(h), int(device), int(memory_budget), int(max_active),
+                                          int(step_rays)))
+        self.h = h
+
+    def add_scene(self, elements: np.ndarray) -> int:
+        e = np.ascontiguousarray(elements)
+        if e.dtype != ELEMENT_DTYPE:
+            raise TypeError("elements must use scenes.ELEMENT_DTYPE")
+        sid = ctypes.c_uint32()
+        _check(self.lib.csp_server_add_scene(self.h, _ptr(e), len(e), ctypes.byref(sid)))
+        return sid.value
+
+    def submit(self, scene: int, sun_dir, sun_shape: int, sun_param: float, num_rays: int, seed: int = 0,
+               instance: int = 0, poses: np.ndarray | None = None) -> int:
+        p = None
+        if poses is not None:
+            p = np.ascontiguousarray(poses)
+            if p.dtype != ELEMENT_DTYPE:
+                raise TypeError("poses must use scenes.ELEMENT_DTYPE")
+        sd = np.ascontiguousarray(sun_dir, np.float64)
+        rid = ctypes.c_uint64()
+        _check(self.lib.csp_server_submit(self.h, int(scene), _ptr(p), _ptr(sd), int(sun_shape), float(sun_param),
+                                          int(num_rays), int(seed), int(instance), ctypes.byref(rid)))
+        return rid.value
+
+    def wait(self, request: int, timeout: float = -1.0):
+        """(counts [100, 100] uint32, stats [4] uint64, (latency s, queueing s))."""
+        counts = np.zeros((100, 100), np.uint32)
+        stats = np.zeros(4, np.uint64)
+        lat = np.zeros(2, np.float64)
+        _check(self.lib.csp_server_wait(self.h, int(request), float(timeout), _ptr(counts), _ptr(stats), _ptr(lat)))
+        return counts, stats, (float(lat[0]), float(lat[1]))
+
+    def stats(self) -> dict:
+        out = np.zeros(8, np.float64)
+        _check(self.lib.csp_server_stats(self.h, _ptr(out)))
+        keys = ["completed", "rays", "p50_s", "p99_s", "rays_per_s", "peak_active", "peak_arena_bytes", "steps"]
+        return dict(zip(keys, out.tolist()))
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            _check(self.lib.csp_server_destroy(self.h))
             self.h = ctypes.c_void_p()
 
     def __del__(self):
