@@ -52,7 +52,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--rays", type=int, default=None, help="ray count (default: the workload's)")
-    p.add_argument("--workload", choices=["single_parabolic", "three_heliostats", "large_field", "batched"],
+    p.add_argument("--workload", choices=["single_parabolic", "three_heliostats", "large_field", "batched", "served"],
                    default="single_parabolic",
                    help="single_parabolic is the benchmark line; the others are for reporting only")
     p.add_argument("--instances", type=int, default=256, help="batched workload: number of instances")
@@ -61,6 +61,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-accuracy", action="store_true")
+    p.add_argument("--requests", type=int, default=300, help="served workload: number of requests")
+    p.add_argument("--rate", type=float, default=200.0, help="served workload: Poisson arrival rate (1/s)")
     p.add_argument("--plain-instances", type=int, default=0,
                    help="batched workload: instances timed in the plain loop (0 = all)")
     return p.parse_args()
@@ -403,7 +405,7 @@ def run_batched(args):
     plain_s = time.perf_counter() - t0
     plain_rays = int(counts[:n_plain].sum())
     tr.close()
-    tb, tl = b.tuning(True), b.tuning(False)
+    tg, tl = b.tuning(native.GROUP_GRID), b.tuning(native.GROUP_BVH)
     line = {
         "metric": METRIC, "value": total / statistics.median(dev), "unit": "rays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.median(dev) * 1e3,
@@ -411,7 +413,7 @@ def run_batched(args):
         "config": {"workload": f"batched_{len(suns)}_instances_large_field_{args.heliostats}_heliostats",
                    "instances": len(suns), "rays_total": total, "rays_min": int(counts.min()),
                    "rays_max": int(counts.max()), "flux_grid": [100, 100], "sun": "pillbox 4.65 mrad",
-                   "slope_error_rad": 1.5e-3, "tuning_bvh": tl, "tuning_small": tb,
+                   "slope_error_rad": 1.5e-3, "tuning_grid": tg, "tuning_bvh": tl,
                    "l2_policy": "per-instance scenes and flux maps; no per-ray buffers"},
         "batched_wall_rays_per_s": total / statistics.median(wall),
         "batched_wall_ms": statistics.median(wall) * 1e3,
@@ -429,12 +431,156 @@ def run_batched(args):
         print(json.dumps(line), flush=True)
 
 
+def served_workload(n_requests, rate):
+    """Requests over resident scenes of 3, 1,000 and 10,000 heliostats, flat and parabolic (focal
+    length 100 m): Poisson arrivals (seed 4), per-request sun (elevation U(10, 80), azimuth
+    U(-120, 120) deg) with the heliostats re-aimed, ray counts log-uniform in [2^20, 2^26] (seed 5).
+    Returns (scene element arrays, requests (scene, poses, sun, rays, arrival s))."""
+    import math
+    import numpy as np
+    from optixsoltracedemos_gb300 import scenes
+    th = scenes.three_heliostats().elements
+    thp = th.copy()
+    thp["surface"][:3] = scenes.SURFACE_PARABOLIC
+    thp["curv_x"][:3] = thp["curv_y"][:3] = 1.0 / 200.0
+    scene_list = [th, thp]
+    for n in (1000, 10000):
+        for par in (False, True):
+            scene_list.append(scenes.large_field(n_heliostats=n, parabolic=par, num_rays=1).elements)
+    ra = np.random.default_rng(4)
+    arrivals = np.cumsum(ra.exponential(1.0 / rate, n_requests))
+    rs = np.random.default_rng(5)
+    reqs = []
+    for k in range(n_requests):
+        sid = int(rs.integers(0, len(scene_list)))
+        sun = scenes.sun_vector(rs.uniform(10.0, 80.0), rs.uniform(-120.0, 120.0))
+        rays = int(math.exp(rs.uniform(20 * math.log(2), 26 * math.log(2))))
+        reqs.append((sid, scenes.reaim(scene_list[sid], sun), sun, rays, float(arrivals[k])))
+    return scene_list, reqs
+
+
+def run_served(args):
+    """Serving workload through csp_server (continuous batching) against the plain per-scene loop
+    (one drop-in handle per scene: update, run, device flux map per request, in arrival order), at
+    saturation (all requests queued at once) and with real-time Poisson arrivals."""
+    import threading
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    from optixsoltracedemos_gb300 import build as nbuild
+    nbuild.build()
+    from optixsoltracedemos_gb300 import native, scenes
+
+    scene_list, reqs = served_workload(args.requests, args.rate)
+    total = sum(r[3] for r in reqs)
+
+    def serve(realtime: bool):
+        srv = native.Server(local, memory_budget=16 << 30, max_active=64)
+        sids = [srv.add_scene(e) for e in scene_list]
+        # warm up every scene once (first-launch costs)
+        for sid in sids:
+            srv.wait(srv.submit(sid, reqs[0][2], scenes.SUN_PILLBOX, 4.65e-3, 1 << 16))
+        ids = [None] * len(reqs)
+        lat = [None] * len(reqs)
+        t0 = time.perf_counter()
+
+        def submitter():
+            for k, (sid, poses, sun, rays, at) in enumerate(reqs):
+                if realtime:
+                    d = t0 + at - time.perf_counter()
+                    if d > 0:
+                        time.sleep(d)
+                ids[k] = srv.submit(sids[sid], sun, scenes.SUN_PILLBOX, 4.65e-3, rays, seed=k, instance=k,
+                                    poses=poses)
+        th = threading.Thread(target=submitter)
+        th.start()
+        counts = []
+        for k in range(len(reqs)):
+            while ids[k] is None:
+                time.sleep(1e-4)
+            c, st, l = srv.wait(ids[k])
+            counts.append(c)
+            lat[k] = l[0]
+        t1 = time.perf_counter()
+        th.join()
+        srv.close()
+        return {"seconds": t1 - t0, "rays_per_s": total / (t1 - t0), "p50_s": float(np.percentile(lat, 50)),
+                "p99_s": float(np.percentile(lat, 99))}, counts
+
+    def plain(realtime: bool, ref_counts=None):
+        tracers = []
+        for e in scene_list:
+            t = native.Tracer(local, 1 << 26)  # hit buffer sized for the largest request up front
+            t.set_elements(e)
+            t.set_sun_vector(reqs[0][2])
+            t.set_sun_shape(scenes.SUN_PILLBOX, 4.65e-3)
+            t.initialize()
+            t.run()
+            tracers.append(t)
+        lat, mism = [], 0
+        t0 = time.perf_counter()
+        for k, (sid, poses, sun, rays, at) in enumerate(reqs):
+            if realtime:
+                d = t0 + at - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+            t = tracers[sid]
+            t.set_elements(poses)
+            t.set_sun_vector(sun)
+            t.set_num_rays(rays)
+            t.set_seed(k, k)
+            t.update()
+            t.run()
+            c, _ = t.flux_map()
+            if ref_counts is not None:
+                mism += int(not np.array_equal(c, ref_counts[k]))
+            lat.append(time.perf_counter() - (t0 + at if realtime else t0))
+        t1 = time.perf_counter()
+        for t in tracers:
+            t.close()
+        return {"seconds": t1 - t0, "rays_per_s": total / (t1 - t0), "p50_s": float(np.percentile(lat, 50)),
+                "p99_s": float(np.percentile(lat, 99)), "flux_counts_mismatching_served": mism}
+
+    clk = ClockSampler(local)
+    clk.start()
+    time.sleep(0.2)
+    sat, counts = serve(False)
+    rt, _ = serve(True)
+    clocks = clk.stop()
+    psat = plain(False, counts)
+    prt = plain(True)
+    line = {
+        "metric": METRIC, "value": sat["rays_per_s"], "unit": "rays/s", "n_gpus": world, "steps": len(reqs),
+        "warmup": len(scene_list), "ms_per_step": sat["seconds"] / len(reqs) * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "served_requests_fields_3_1000_10000_flat_parabolic", "requests": len(reqs),
+                   "rays_total": total, "arrival_rate_per_s": args.rate, "rays_per_request": "log-uniform [2^20, 2^26]",
+                   "sun": "pillbox 4.65 mrad, per-request elevation U(10,80) azimuth U(-120,120), heliostats re-aimed",
+                   "flux_grid": [100, 100], "max_active": 64,
+                   "l2_policy": "per-request scenes and flux maps; no per-ray buffers"},
+        "served_saturation": sat, "served_poisson": rt,
+        "plain_loop_saturation": psat, "plain_loop_poisson": prt,
+        "speedup_vs_plain_loop": sat["rays_per_s"] / psat["rays_per_s"],
+        "e2e": {"value": sat["rays_per_s"], "unit": "rays/s",
+                "h2d_bytes_per_step": int(sum(r[1].nbytes for r in reqs) / len(reqs)),
+                "d2h_bytes_per_step": 100 * 100 * 4},
+        "gpu_launches": None,
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batched":
         run_batched(args)
+    elif args.workload == "served":
+        run_served(args)
     else:
         run_ours(args)
 
