@@ -82,6 +82,7 @@ struct BatchSmem {
     FluxTarget F;
     unsigned long long stat[4];
     unsigned long long grab;
+    unsigned long long want;
 };
 
 // Drain the queue of the current instance and add its record counters to the instance's totals.
@@ -103,17 +104,27 @@ __global__ void __launch_bounds__(kB, 768 / kB) batch_kernel(const BatchLaunch L
     BatchSmem<kB>& sm = *reinterpret_cast<BatchSmem<kB>*>(smem_raw);
     for (uint32_t m = threadIdx.x; m < kH3Tab; m += kB) sm.core.t6[m] = halton3(m);
     if (threadIdx.x < 4) sm.stat[threadIdx.x] = 0;
-    if (threadIdx.x == 0) sm.core.qsize = 0;
+    if (threadIdx.x == 0) {
+        sm.core.qsize = 0;
+        sm.grab = 0;
+    }
     const Sink k{&sm.F, sm.stat};
     bool have = false;
     uint64_t t0 = 0, t1 = 0;  // tile range of the current instance
     for (;;) {
         __syncthreads();
-        if (threadIdx.x == 0) sm.grab = atomicAdd(L.next_tile, (unsigned long long)L.chunk);
+        if (threadIdx.x == 0) {
+            // chunks of L.chunk tiles while much work is left, single tiles near the end (a chunk
+            // taken last would otherwise run alone)
+            const unsigned long long left = L.total_tiles > sm.grab ? L.total_tiles - sm.grab : 0;
+            const unsigned long long want = left > (unsigned long long)gridDim.x * L.chunk * 4 ? L.chunk : 1;
+            sm.grab = atomicAdd(L.next_tile, want);
+            sm.want = want;
+        }
         __syncthreads();
         const uint64_t g0 = sm.grab;
         if (g0 >= L.total_tiles) break;
-        const uint64_t g1 = min(g0 + (uint64_t)L.chunk, L.total_tiles);
+        const uint64_t g1 = min(g0 + (uint64_t)sm.want, L.total_tiles);
         for (uint64_t g = g0; g < g1; ++g) {
             if (!have || g < t0 || g >= t1) {
                 // instance of tile g: the last i with tile_begin[i] <= g (empty instances skipped)

@@ -687,7 +687,9 @@ __device__ __forceinline__ void warp_count(unsigned long long* s) {
     if ((int)(threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(s, (unsigned long long)__popc(m));
 }
 
-__device__ __forceinline__ void flux_record(const Sink& k, float4 rec) {
+// Out of line: one copy serves every emit site (the phase A and phase B paths), which keeps the
+// flux kernels' instruction footprint close to the dense ones'.
+__device__ __noinline__ void flux_record(const Sink& k, float4 rec) {
     if (rec.x == 1.0f) {
         warp_count(k.stat + 1);
         return;
