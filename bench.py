@@ -61,6 +61,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-accuracy", action="store_true")
+    p.add_argument("--tuning", type=str, default="", help="batched workload: block,ctas_per_sm,chunk (default: autotune)")
     p.add_argument("--requests", type=int, default=300, help="served workload: number of requests")
     p.add_argument("--rate", type=float, default=200.0, help="served workload: Poisson arrival rate (1/s)")
     p.add_argument("--plain-instances", type=int, default=0,
@@ -366,6 +367,8 @@ def run_batched(args):
     sid = b.add_scene(base)
     for i in range(len(suns)):
         b.add_instance(sid, suns[i], scenes.SUN_PILLBOX, 4.65e-3, int(counts[i]), seed=0, instance=i, poses=poses[i])
+    if args.tuning:
+        b.set_tuning(*[int(x) for x in args.tuning.split(",")])
     t0 = time.perf_counter()
     b.run()  # autotune (first run of this scene class) + graph capture
     first_s = time.perf_counter() - t0
