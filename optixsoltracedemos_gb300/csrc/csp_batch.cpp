@@ -64,7 +64,8 @@ void Batch::release() {
         cudaFree(s.d_items);
         cudaFree(s.d_global);
         s.d_topo = nullptr;
-        s.d_cells = s.d_items = s.d_global = nullptr;
+        s.d_cells = nullptr;
+        s.d_items = s.d_global = nullptr;
     }
     cudaFree(d_arena);
     d_arena = nullptr;
@@ -98,7 +99,7 @@ int Batch::add_scene(const csp_element* el, uint32_t n, uint32_t* id) {
     if ((rc = build_elements(el, n, s.base, err))) return set_error(rc, err);
     build_bvh(s.base);
     s.flat = n <= kFlatListMax;
-    if (!s.flat) build_grid(el, n, s.base, s.grid);
+    if (!s.flat) build_grid(s.base, s.grid);
     auto put = [&](auto*& dptr, const auto& host, const char* what) {
         const size_t bytes = std::max<size_t>(1, host.size()) * sizeof(host[0]);
         int r = cuda_status(cudaMalloc((void**)&dptr, bytes), what);
@@ -152,7 +153,6 @@ uint32_t Batch::count_of(size_t i) const { return (uint32_t)scenes[inst[i].scene
 int Batch::layout() {
     const size_t n = inst.size();
     place.assign(n, Place{});
-    layer.assign(2 * n, 0.f);
     for (int g = 0; g < kBatchGroups; ++g) n_group[g] = 0;
     max_nodes = 0;
     size_t off = 0;
@@ -160,8 +160,7 @@ int Batch::layout() {
         const BScene& s = scenes[inst[i].scene];
         const size_t ne = s.elements.size();
         Place& p = place[i];
-        p.group = s.flat ? kAccelFlat
-                         : (s.grid.valid && grid_accepts(s.grid, elements_of(i), count_of(i)) ? kAccelGrid : kAccelBvh);
+        p.group = s.flat ? kAccelFlat : (grid_of(i).valid ? kAccelGrid : kAccelBvh);
         p.slot = n_group[p.group]++;
         p.prims = off;
         off += align16(ne * sizeof(Prim));
@@ -171,6 +170,15 @@ int Batch::layout() {
         off += align16(ne * sizeof(Aabb));
         p.prune = off;
         off += align16(ne * sizeof(Aabb));
+        if (p.group == kAccelGrid && !inst[i].poses.empty()) {
+            const HostGrid& hg = builds[i].grid;
+            p.cells = off;
+            off += align16(hg.cell_start.size() * sizeof(uint32_t));
+            p.items = off;
+            off += align16(hg.items.size() * sizeof(Aabb));
+            p.global = off;
+            off += align16(std::max<size_t>(1, hg.global.size()) * sizeof(Aabb));
+        }
         max_nodes = std::max(max_nodes, (int)s.base.nodes.size());
     }
     for (int g = 0; g < kBatchGroups; ++g) {
@@ -248,23 +256,44 @@ int Batch::layout() {
     return CSP_OK;
 }
 
-// Host build of instance i into the staging image: element records, refit job, sun job.
-int Batch::fill_instance(size_t i, HostScene& hs, std::string& err) {
+// Host build of an instance with its own poses: element records (the reference's geometry
+// arithmetic) and, for field-like scenes, the grid of those poses.
+int Batch::build_instance(size_t i, std::string& err) {
+    const BInst& b = inst[i];
+    if (b.poses.empty()) return CSP_OK;
+    InstBuild& ib = builds[i];
+    int rc = build_elements(b.poses.data(), count_of(i), ib.hs, err);
+    if (rc) return rc;
+    ib.grid = HostGrid{};
+    if (!scenes[b.scene].flat) build_grid(ib.hs, ib.grid);
+    return CSP_OK;
+}
+
+const HostScene& Batch::scene_of(size_t i) const {
+    return inst[i].poses.empty() ? scenes[inst[i].scene].base : builds[i].hs;
+}
+
+const HostGrid& Batch::grid_of(size_t i) const {
+    return inst[i].poses.empty() ? scenes[inst[i].scene].grid : builds[i].grid;
+}
+
+// Instance i into the staging image: element records, own grid arrays, refit job, sun job.
+void Batch::fill_instance(size_t i) {
     const BInst& b = inst[i];
     const Place& p = place[i];
     const BScene& s = scenes[b.scene];
     const uint32_t ne = count_of(i);
-    const HostScene* src = &s.base;
-    if (!b.poses.empty()) {
-        int rc = build_elements(b.poses.data(), ne, hs, err);
-        if (rc) return rc;
-        src = &hs;
-    }
+    const HostScene* src = &scene_of(i);
     std::memcpy(h_stage + p.prims, src->prims.data(), ne * sizeof(Prim));
     std::memcpy(h_stage + p.optics, src->optics.data(), ne * sizeof(Optics));
     std::memcpy(h_stage + p.aabbs, src->aabbs.data(), ne * sizeof(Aabb));
     std::memcpy(h_stage + p.prune, src->prune.data(), ne * sizeof(Aabb));
-    if (p.group == kAccelGrid) grid_layer(s.grid, *src, layer[2 * i], layer[2 * i + 1]);
+    if (p.group == kAccelGrid && !b.poses.empty()) {
+        const HostGrid& hg = builds[i].grid;
+        std::memcpy(h_stage + p.cells, hg.cell_start.data(), hg.cell_start.size() * sizeof(uint32_t));
+        std::memcpy(h_stage + p.items, hg.items.data(), hg.items.size() * sizeof(Aabb));
+        if (!hg.global.empty()) std::memcpy(h_stage + p.global, hg.global.data(), hg.global.size() * sizeof(Aabb));
+    }
     RefitJob rj;
     rj.topo = s.d_topo;
     rj.aabbs = reinterpret_cast<const Aabb*>(d_arena + p.aabbs);
@@ -286,7 +315,6 @@ int Batch::fill_instance(size_t i, HostScene& hs, std::string& err) {
     sj.param = (float)b.param;
     sj.out = reinterpret_cast<SunFrame*>(d_arena + p.sun);
     std::memcpy(h_stage + sunjob_off + i * sizeof(SunJob), &sj, sizeof sj);
-    return CSP_OK;
 }
 
 // Instance descriptors and tile tables of both groups for the given tile sizes; `sample` > 0
@@ -319,24 +347,11 @@ void Batch::fill_descs(const int* block, double sample, std::vector<InstanceDesc
         d.args.pad = 0;
         d.args.grid = nullptr;
         if (g == kAccelGrid) {
-            const HostGrid& hg = scenes[b.scene].grid;
+            const bool own = !b.poses.empty();
             const BScene& bs = scenes[b.scene];
-            d.grid.x0 = hg.x0;
-            d.grid.y0 = hg.y0;
-            d.grid.x1 = hg.x1;
-            d.grid.y1 = hg.y1;
-            d.grid.cell = hg.cell;
-            d.grid.inv_cell = hg.inv_cell;
-            d.grid.zlo = layer[2 * i];
-            d.grid.zhi = layer[2 * i + 1];
-            d.grid.nx = hg.nx;
-            d.grid.ny = hg.ny;
-            d.grid.n_global = (int)hg.global.size();
-            d.grid.pad = 0;
-            d.grid.cell_start = bs.d_cells;
-            d.grid.items = bs.d_items;
-            d.grid.global = bs.d_global;
-            d.grid.aabbs = reinterpret_cast<const Aabb*>(d_arena + p.aabbs);
+            d.grid = grid_desc(grid_of(i), own ? reinterpret_cast<const uint32_t*>(d_arena + p.cells) : bs.d_cells,
+                               own ? reinterpret_cast<const Aabb*>(d_arena + p.items) : bs.d_items,
+                               own ? reinterpret_cast<const Aabb*>(d_arena + p.global) : bs.d_global);
             d.args.grid = reinterpret_cast<const GridDesc*>(d_arena + desc_off[g] + p.slot * sizeof(InstanceDesc) +
                                                             offsetof(InstanceDesc, grid));
         }
@@ -486,33 +501,44 @@ int Batch::run() {
     const auto t0 = std::chrono::steady_clock::now();
     int rc = ensure_stream();
     if (rc) return rc;
-    if ((rc = layout())) return rc;
 
-    // host element builds, parallel over instances
+    // host builds of the instances with their own poses, then the copies into the staging image,
+    // both parallel over instances
     const size_t n = inst.size();
+    builds.clear();
+    builds.resize(n);
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     const size_t workers = std::min<size_t>(std::min<size_t>(hw, 64), n);
-    std::vector<int> wrc(workers, CSP_OK);
-    std::vector<std::string> werr(workers);
-    auto work = [&](size_t w) {
-        HostScene hs;
-        for (size_t i = w; i < n; i += workers) {
-            const int r = fill_instance(i, hs, werr[w]);
-            if (r) {
-                wrc[w] = r;
-                werr[w] = "instance " + std::to_string(i) + ": " + werr[w];
-                return;
+    auto parallel = [&](auto&& fn) {
+        std::vector<int> wrc(workers, CSP_OK);
+        std::vector<std::string> werr(workers);
+        auto work = [&](size_t w) {
+            for (size_t i = w; i < n; i += workers) {
+                const int r = fn(i, werr[w]);
+                if (r) {
+                    wrc[w] = r;
+                    werr[w] = "instance " + std::to_string(i) + ": " + werr[w];
+                    return;
+                }
             }
+        };
+        if (workers <= 1) work(0);
+        else {
+            std::vector<std::thread> th;
+            for (size_t w = 0; w < workers; ++w) th.emplace_back(work, w);
+            for (auto& t : th) t.join();
         }
+        for (size_t w = 0; w < workers; ++w)
+            if (wrc[w]) return set_error(wrc[w], werr[w]);
+        return (int)CSP_OK;
     };
-    if (workers <= 1) work(0);
-    else {
-        std::vector<std::thread> th;
-        for (size_t w = 0; w < workers; ++w) th.emplace_back(work, w);
-        for (auto& t : th) t.join();
-    }
-    for (size_t w = 0; w < workers; ++w)
-        if (wrc[w]) return set_error(wrc[w], werr[w]);
+    if ((rc = parallel([&](size_t i, std::string& err) { return build_instance(i, err); }))) return rc;
+    if ((rc = layout())) return rc;
+    if ((rc = parallel([&](size_t i, std::string&) {
+             fill_instance(i);
+             return (int)CSP_OK;
+         })))
+        return rc;
 
     if ((rc = resolve_tuning())) return rc;
     int block[kBatchGroups];
@@ -521,12 +547,15 @@ int Batch::run() {
     std::vector<uint64_t> tb[kBatchGroups];
     fill_descs(block, 0.0, desc, tb);
     write_descs(desc, tb, h_stage);
+    builds.clear();  // everything the device needs is in the staging image now
+    builds.shrink_to_fit();
     uint64_t tiles[kBatchGroups];
     for (int g = 0; g < kBatchGroups; ++g) tiles[g] = tb[g][n_group[g]];
 
     // graph signature: everything the captured launches depend on besides the staged contents
     std::vector<uint64_t> sig = {(uint64_t)(uintptr_t)d_arena, (uint64_t)(uintptr_t)h_stage,
-                                 (uint64_t)(uintptr_t)h_result, up_bytes, zero_bytes, res_bytes, n, nx, ny};
+                                 (uint64_t)(uintptr_t)h_result, up_bytes, zero_bytes, res_bytes, n, nx, ny,
+                                 desc_off[0], zero_off, res_off};
     for (int g = 0; g < kBatchGroups; ++g) {
         sig.push_back(tiles[g]);
         sig.push_back((uint64_t)n_group[g]);

@@ -18,10 +18,16 @@ struct BScene {
     HostScene base;         // element records + BVH topology of the scene's own poses
     Node* d_topo = nullptr; // topology on the device (links; boxes of the scene's own poses)
     bool flat = false;      // <= kFlatListMax elements: shared-memory element list kernel
-    HostGrid grid;          // field grid (valid for field-like scenes)
+    HostGrid grid;          // field grid of the scene's own poses (valid for field-like scenes)
     uint32_t* d_cells = nullptr;
-    uint32_t* d_items = nullptr;
-    uint32_t* d_global = nullptr;
+    Aabb* d_items = nullptr;
+    Aabb* d_global = nullptr;
+};
+
+// Host build of one instance with its own poses: element records and the grid of those poses.
+struct InstBuild {
+    HostScene hs;
+    HostGrid grid;
 };
 
 struct BInst {
@@ -37,6 +43,7 @@ struct BInst {
 // Byte offsets of one instance's arrays in the device arena (and the staging image).
 struct Place {
     size_t prims = 0, optics = 0, aabbs = 0, prune = 0, nodes = 0, sun = 0, counts = 0, stats = 0;
+    size_t cells = 0, items = 0, global = 0;  // own grid arrays (instances with poses in the grid group)
     int group = 0;  // kAccelFlat, kAccelBvh or kAccelGrid: the kernel that traces the instance
     int slot = 0;   // index within the group
 };
@@ -62,7 +69,7 @@ struct Batch {
     size_t up_bytes = 0, zero_off = 0, zero_bytes = 0, res_off = 0, res_bytes = 0;
     size_t desc_off[kBatchGroups] = {}, tb_off[kBatchGroups] = {}, refit_off = 0, sunjob_off = 0, counter_off = 0;
     int n_group[kBatchGroups] = {};
-    std::vector<float> layer;  // per instance: zlo, zhi of grid instances
+    std::vector<InstBuild> builds;  // per instance, during a run (instances with poses)
     int max_nodes = 0;
 
     cudaGraphExec_t graph = nullptr;
@@ -78,7 +85,10 @@ struct Batch {
     const csp_element* elements_of(size_t i) const;
     uint32_t count_of(size_t i) const;
     int layout();
-    int fill_instance(size_t i, HostScene& scratch, std::string& err);
+    int build_instance(size_t i, std::string& err);
+    const HostScene& scene_of(size_t i) const;
+    const HostGrid& grid_of(size_t i) const;
+    void fill_instance(size_t i);
     void fill_descs(const int* block, double sample, std::vector<InstanceDesc>* desc, std::vector<uint64_t>* tb);
     void write_descs(const std::vector<InstanceDesc>* desc, const std::vector<uint64_t>* tb, unsigned char* img);
     BatchLaunch launch_of(int g, uint64_t total_tiles, int chunk) const;

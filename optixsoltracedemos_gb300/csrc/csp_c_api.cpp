@@ -69,7 +69,8 @@ void System::release() {
     cudaFree(d_items);
     cudaFree(d_global);
     d_grid = nullptr;
-    d_cells = d_items = d_global = nullptr;
+    d_cells = nullptr;
+    d_items = d_global = nullptr;
     cap_cells = cap_items = cap_global = 0;
     cudaFree(d_flux);
     cudaFree(d_fstats);
@@ -118,8 +119,7 @@ int System::upload_scene() {
     return CSP_OK;
 }
 
-// Field grid on the device: the cell arrays (when `arrays`) and the descriptor with the layer of
-// the current poses.
+// Field grid on the device: the cell arrays (when `arrays`) and the descriptor.
 int System::upload_grid(bool arrays) {
     if (!grid.valid) return CSP_OK;
     int rc;
@@ -129,24 +129,8 @@ int System::upload_grid(bool arrays) {
         if ((rc = upload(d_global, cap_global, grid.global, stream, "upload grid globals"))) return rc;
     }
     if (!d_grid && (rc = cuda_status(cudaMalloc((void**)&d_grid, sizeof(GridDesc)), "cudaMalloc grid"))) return rc;
-    GridDesc g;
-    g.x0 = grid.x0;
-    g.y0 = grid.y0;
-    g.x1 = grid.x1;
-    g.y1 = grid.y1;
-    g.cell = grid.cell;
-    g.inv_cell = grid.inv_cell;
-    grid_layer(grid, scene, g.zlo, g.zhi);
-    g.nx = grid.nx;
-    g.ny = grid.ny;
-    g.n_global = (int)grid.global.size();
-    g.pad = 0;
-    g.cell_start = d_cells;
-    g.items = d_items;
-    g.global = d_global;
-    g.aabbs = d_aabbs;
-    grid_desc = g;
-    return cuda_status(cudaMemcpyAsync(d_grid, &grid_desc, sizeof(GridDesc), cudaMemcpyHostToDevice, stream),
+    grid_host = csp::grid_desc(grid, d_cells, d_items, d_global);
+    return cuda_status(cudaMemcpyAsync(d_grid, &grid_host, sizeof(GridDesc), cudaMemcpyHostToDevice, stream),
                        "upload grid");
 }
 
@@ -197,7 +181,7 @@ int System::initialize() {
     if ((rc = build_elements(elements.data(), (uint32_t)elements.size(), scene, err))) return fail(rc, err);
     build_bvh(scene);
     grid = HostGrid{};
-    if (accel != CSP_ACCEL_BVH) build_grid(elements.data(), (uint32_t)elements.size(), scene, grid);
+    if (accel != CSP_ACCEL_BVH) build_grid(scene, grid);
     if (accel == CSP_ACCEL_GRID && !grid.valid && elements.size() > kFlatListMax)
         return fail(CSP_ERR_BAD_SCENE, "the scene is not a planar field: no grid (use CSP_ACCEL_AUTO or _BVH)");
     if ((rc = upload_scene())) return rc;
@@ -218,13 +202,13 @@ int System::update() {
     int rc = build_elements(elements.data(), (uint32_t)elements.size(), scene, err);
     if (rc) return fail(rc, err);
     refit_bvh(scene);
-    bool rebuilt = false;
-    if (grid.valid && !grid_accepts(grid, elements.data(), (uint32_t)elements.size())) {
-        build_grid(elements.data(), (uint32_t)elements.size(), scene, grid);  // origins or sizes moved
-        rebuilt = true;
-    }
+    // the grid holds one set of poses: rebuilt for the new ones
+    grid = HostGrid{};
+    if (accel != CSP_ACCEL_BVH) build_grid(scene, grid);
+    if (accel == CSP_ACCEL_GRID && !grid.valid && elements.size() > kFlatListMax)
+        return fail(CSP_ERR_BAD_SCENE, "the new poses are not a planar field: no grid (use CSP_ACCEL_AUTO or _BVH)");
     if ((rc = upload_scene())) return rc;
-    if ((rc = upload_grid(rebuilt))) return rc;
+    if ((rc = upload_grid(true))) return rc;
     if ((rc = prepare_sun())) return rc;
     if ((rc = ensure_hit_buffers())) return rc;
     return cuda_status(cudaStreamSynchronize(stream), "update");

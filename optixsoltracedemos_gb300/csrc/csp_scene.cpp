@@ -470,61 +470,48 @@ namespace csp {
 
 namespace {
 
-void grid_key(const csp_element& e, double* k) {
-    k[0] = e.origin[0];
-    k[1] = e.origin[1];
-    k[2] = e.origin[2];
-    k[3] = e.width;
-    k[4] = e.height;
-    k[5] = e.curv_x;
-    k[6] = e.curv_y;
-}
-
-constexpr int kGridKey = 7;
 constexpr int kGridMaxCellsPerItem = 64;
 constexpr size_t kGridMaxCells = 1u << 22;
 
 }  // namespace
 
-void build_grid(const csp_element* el, uint32_t n, const HostScene& s, HostGrid& g) {
+void build_grid(const HostScene& s, HostGrid& g) {
     g = HostGrid{};
+    const uint32_t n = (uint32_t)s.prims.size();
     if (n <= kFlatListMax) return;
-    // registered xy squares and z extents of the mirror bounding spheres
-    std::vector<double> lo(2 * n), hi(2 * n), zr(2 * n);
-    std::vector<double> size;
-    double zmin = DBL_MAX, zmax = -DBL_MAX, X0 = DBL_MAX, Y0 = DBL_MAX, X1 = -DBL_MAX, Y1 = -DBL_MAX;
+    // registered xy boxes: pruning box + margin; gridded = every element but the last (receiver)
+    std::vector<double> lo(2 * n), hi(2 * n), size(n, 0.0);
+    std::vector<uint8_t> gridded(n, 0);
+    std::vector<double> sizes;
     for (uint32_t i = 0; i + 1 < n; ++i) {
-        const csp_element& e = el[i];
-        const double hw = 0.5 * e.width, hh = 0.5 * e.height;
-        double R = std::sqrt(hw * hw + hh * hh);
-        if (e.surface == CSP_SURFACE_PARABOLIC) R += 0.5 * (std::fabs(e.curv_x) * hw * hw + std::fabs(e.curv_y) * hh * hh);
-        const double o = std::max(std::fabs(e.origin[0]), std::max(std::fabs(e.origin[1]), std::fabs(e.origin[2])));
-        const double r = R + 2e-5 * (o + R) + 0.05;
-        lo[2 * i] = e.origin[0] - r;
-        lo[2 * i + 1] = e.origin[1] - r;
-        hi[2 * i] = e.origin[0] + r;
-        hi[2 * i + 1] = e.origin[1] + r;
-        zr[2 * i] = e.origin[2] - r;
-        zr[2 * i + 1] = e.origin[2] + r;
-        size.push_back(2 * r);
+        const Aabb& b = s.prune[i];
+        const double m = 2e-5 * std::max(std::max(std::fabs((double)b.lo.x), std::fabs((double)b.hi.x)),
+                                          std::max(std::fabs((double)b.lo.y), std::fabs((double)b.hi.y))) +
+                         0.05;
+        lo[2 * i] = (double)b.lo.x - m;
+        lo[2 * i + 1] = (double)b.lo.y - m;
+        hi[2 * i] = (double)b.hi.x + m;
+        hi[2 * i + 1] = (double)b.hi.y + m;
+        size[i] = std::max(hi[2 * i] - lo[2 * i], hi[2 * i + 1] - lo[2 * i + 1]);
+        sizes.push_back(size[i]);
     }
-    std::vector<double> sorted = size;
-    std::nth_element(sorted.begin(), sorted.begin() + sorted.size() / 2, sorted.end());
-    double cell = (double)(float)(0.6 * sorted[sorted.size() / 2]);
+    std::nth_element(sizes.begin(), sizes.begin() + sizes.size() / 2, sizes.end());
+    double cell = (double)(float)(1.0 * sizes[sizes.size() / 2]);
     if (!(cell > 0)) return;
-    g.gridded.assign(n, 0);
+    double X0 = DBL_MAX, Y0 = DBL_MAX, X1 = -DBL_MAX, Y1 = -DBL_MAX;
+    float zmin = FLT_MAX, zmax = -FLT_MAX;
     for (uint32_t i = 0; i + 1 < n; ++i) {
         if (size[i] > 8.0 * cell) continue;  // oversized: global list
-        g.gridded[i] = 1;
+        gridded[i] = 1;
         X0 = std::min(X0, lo[2 * i]);
         Y0 = std::min(Y0, lo[2 * i + 1]);
         X1 = std::max(X1, hi[2 * i]);
         Y1 = std::max(Y1, hi[2 * i + 1]);
-        zmin = std::min(zmin, zr[2 * i]);
-        zmax = std::max(zmax, zr[2 * i + 1]);
+        zmin = std::min(zmin, s.prune[i].lo.z);
+        zmax = std::max(zmax, s.prune[i].hi.z);
     }
     if (!(X1 > X0) || !(Y1 > Y0)) return;
-    if (zmax - zmin > 0.25 * std::max(X1 - X0, Y1 - Y0)) return;  // not a thin layer
+    if ((double)zmax - (double)zmin > 0.25 * std::max(X1 - X0, Y1 - Y0)) return;  // not a thin layer
     double nxd = std::ceil((X1 - X0) / cell), nyd = std::ceil((Y1 - Y0) / cell);
     while (nxd * nyd > (double)kGridMaxCells) {
         cell = (double)(float)(cell * 1.5);
@@ -539,26 +526,30 @@ void build_grid(const csp_element* el, uint32_t n, const HostScene& s, HostGrid&
     g.inv_cell = 1.0f / g.cell;
     g.x1 = g.x0 + (float)g.nx * g.cell;
     g.y1 = g.y0 + (float)g.ny * g.cell;
-    // the float bounds must still cover every registered square
+    // the float bounds must still cover every registered box
     while ((double)g.x1 < X1 || (double)g.y1 < Y1 || (double)g.x0 > X0 || (double)g.y0 > Y0) {
         g.x0 = std::nextafter(g.x0, -FLT_MAX);
         g.y0 = std::nextafter(g.y0, -FLT_MAX);
         g.x1 = std::nextafter(g.x1, FLT_MAX);
         g.y1 = std::nextafter(g.y1, FLT_MAX);
     }
+    // the layer: every gridded surface lies in its pruning box
+    const float mz = 1e-5f * std::max(std::fabs(zmin), std::fabs(zmax)) + 0.01f;
+    g.zlo = std::nextafter(zmin - mz, -FLT_MAX);
+    g.zhi = std::nextafter(zmax + mz, FLT_MAX);
     auto cell_range = [&](uint32_t i, int& ax, int& ay, int& bx, int& by) {
         ax = std::max(0, std::min(g.nx - 1, (int)std::floor((lo[2 * i] - g.x0) / cell)));
         ay = std::max(0, std::min(g.ny - 1, (int)std::floor((lo[2 * i + 1] - g.y0) / cell)));
         bx = std::max(0, std::min(g.nx - 1, (int)std::floor((hi[2 * i] - g.x0) / cell)));
         by = std::max(0, std::min(g.ny - 1, (int)std::floor((hi[2 * i + 1] - g.y0) / cell)));
     };
-    std::vector<uint32_t> count((size_t)g.nx * g.ny + 1, 0);
+    std::vector<uint32_t> count((size_t)g.nx * g.ny, 0);
     for (uint32_t i = 0; i + 1 < n; ++i) {
-        if (!g.gridded[i]) continue;
+        if (!gridded[i]) continue;
         int ax, ay, bx, by;
         cell_range(i, ax, ay, bx, by);
         if ((bx - ax + 1) * (by - ay + 1) > kGridMaxCellsPerItem) {
-            g.gridded[i] = 0;
+            gridded[i] = 0;
             continue;
         }
         for (int y = ay; y <= by; ++y)
@@ -566,48 +557,46 @@ void build_grid(const csp_element* el, uint32_t n, const HostScene& s, HostGrid&
     }
     g.cell_start.assign((size_t)g.nx * g.ny + 1, 0);
     for (size_t c = 0; c < (size_t)g.nx * g.ny; ++c) g.cell_start[c + 1] = g.cell_start[c] + count[c];
-    g.items.assign(g.cell_start.back(), 0);
+    g.items.assign(g.cell_start.back(), Aabb{});
     std::vector<uint32_t> fill(g.cell_start.begin(), g.cell_start.end() - 1);
+    auto item = [&](uint32_t i) {
+        Aabb a = s.aabbs[i];
+        a.lo.w = u2f((s.types[i] << kTypeShift) | i);
+        a.hi.w = 0.f;
+        return a;
+    };
     for (uint32_t i = 0; i + 1 < n; ++i) {
-        if (!g.gridded[i]) continue;
+        if (!gridded[i]) continue;
         int ax, ay, bx, by;
         cell_range(i, ax, ay, bx, by);
-        const uint32_t w = (s.types[i] << kTypeShift) | i;
+        const Aabb a = item(i);
         for (int y = ay; y <= by; ++y)
-            for (int x = ax; x <= bx; ++x) g.items[fill[(size_t)y * g.nx + x]++] = w;
+            for (int x = ax; x <= bx; ++x) g.items[fill[(size_t)y * g.nx + x]++] = a;
     }
     for (uint32_t i = 0; i < n; ++i)
-        if (!g.gridded[i]) g.global.push_back((s.types[i] << kTypeShift) | i);
-    g.key.resize((size_t)kGridKey * n);
-    for (uint32_t i = 0; i < n; ++i) grid_key(el[i], &g.key[(size_t)kGridKey * i]);
+        if (!gridded[i]) g.global.push_back(item(i));
     g.valid = true;
 }
 
-bool grid_accepts(const HostGrid& g, const csp_element* el, uint32_t n) {
-    if (!g.valid || (size_t)kGridKey * n != g.key.size()) return false;
-    double k[kGridKey];
-    for (uint32_t i = 0; i < n; ++i) {
-        grid_key(el[i], k);
-        if (std::memcmp(k, &g.key[(size_t)kGridKey * i], sizeof k) != 0) return false;
-    }
-    return true;
-}
-
-void grid_layer(const HostGrid& g, const HostScene& s, float& zlo, float& zhi) {
-    float a = FLT_MAX, b = -FLT_MAX;
-    for (size_t i = 0; i < s.prune.size(); ++i) {
-        if (i < g.gridded.size() && g.gridded[i]) {
-            a = std::min(a, s.prune[i].lo.z);
-            b = std::max(b, s.prune[i].hi.z);
-        }
-    }
-    if (!(a <= b)) {
-        a = 0.f;
-        b = 0.f;
-    }
-    const float m = 1e-5f * std::max(std::fabs(a), std::fabs(b)) + 0.01f;
-    zlo = std::nextafter(a - m, -FLT_MAX);
-    zhi = std::nextafter(b + m, FLT_MAX);
+GridDesc grid_desc(const HostGrid& g, const uint32_t* cell_start, const Aabb* items, const Aabb* global) {
+    GridDesc d;
+    d.x0 = g.x0;
+    d.y0 = g.y0;
+    d.x1 = g.x1;
+    d.y1 = g.y1;
+    d.cell = g.cell;
+    d.inv_cell = g.inv_cell;
+    d.zlo = g.zlo;
+    d.zhi = g.zhi;
+    d.nx = g.nx;
+    d.ny = g.ny;
+    d.n_global = (int)g.global.size();
+    d.pad = 0;
+    d.cell_start = cell_start;
+    d.items = items;
+    d.global = global;
+    d.reserved = nullptr;
+    return d;
 }
 
 }  // namespace csp

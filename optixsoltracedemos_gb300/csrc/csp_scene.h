@@ -40,29 +40,26 @@ void refit_bvh(HostScene& s);
 // y, z axes in world space) and exact double AABB of one element.
 void element_frame(const csp_element& e, double euler[3], double G[9], double lo[3], double hi[3]);
 
-// Uniform 2D grid of a field-like scene (see GridDesc): the mirrors are registered in every cell
-// that the xy square of their orientation-independent bounding sphere (centre = origin, radius =
-// half aperture diagonal + paraboloid sag, plus a rounding margin) overlaps, so re-aimed poses keep
-// the grid valid; the last element (receiver) and oversized elements form the global list.
+// Uniform 2D grid of a field-like scene for one set of poses (see GridDesc): every mirror is
+// registered in each cell that its pruning box, widened by 2e-5 |coordinate| + 5 cm, overlaps in
+// xy; the last element (receiver) and oversized elements form the global list.  Items carry the
+// exact AABB (lo.w = element | type << kTypeShift).
 struct HostGrid {
     bool valid = false;
-    float x0 = 0, y0 = 0, x1 = 0, y1 = 0, cell = 1, inv_cell = 1;
+    float x0 = 0, y0 = 0, x1 = 0, y1 = 0, cell = 1, inv_cell = 1, zlo = 0, zhi = 0;
     int nx = 0, ny = 0;
     std::vector<uint32_t> cell_start;  // [nx * ny + 1]
-    std::vector<uint32_t> items;       // element | type << kTypeShift
-    std::vector<uint32_t> global;      // element | type << kTypeShift
-    std::vector<uint8_t> gridded;      // per element: registered in cells
-    std::vector<double> key;           // per element: origin (3), width, height, curv_x, curv_y
+    std::vector<Aabb> items;
+    std::vector<Aabb> global;
 };
 
-// Build the grid for a scene whose mirrors lie in a thin layer (layer thickness at most a quarter
-// of the field's horizontal extent) and that has more than kFlatListMax elements; otherwise leave
-// g.valid false (the BVH is used).
-void build_grid(const csp_element* el, uint32_t n, const HostScene& s, HostGrid& g);
-// Poses that keep every element's origin, size, curvature and surface: the grid stays valid.
-bool grid_accepts(const HostGrid& g, const csp_element* el, uint32_t n);
-// z range of the pruning boxes of the gridded elements (current poses), widened by a margin.
-void grid_layer(const HostGrid& g, const HostScene& s, float& zlo, float& zhi);
+// Build the grid of a scene with more than kFlatListMax elements whose mirrors lie in a thin layer
+// (at most a quarter of the field's horizontal extent); otherwise leave g.valid false (the BVH is
+// used).  Reads s.prune (registration, layer), s.aabbs (items) and s.types.
+void build_grid(const HostScene& s, HostGrid& g);
+
+// Device descriptor of a grid whose arrays live at the given device addresses.
+GridDesc grid_desc(const HostGrid& g, const uint32_t* cell_start, const Aabb* items, const Aabb* global);
 
 // Flux map target of a receiver element for an nx x ny grid (counts and stats pointers left null),
 // and the area of one bin in m^2 (flat: (w/nx)(h/ny); cylinder: (2 pi r/nx)(h/ny)).

@@ -51,14 +51,13 @@ struct SScene {
     int group = kAccelBvh;
     Node* d_topo = nullptr;
     uint32_t* d_cells = nullptr;
-    uint32_t* d_items = nullptr;
-    uint32_t* d_global = nullptr;
+    Aabb* d_items = nullptr;
+    Aabb* d_global = nullptr;
     // the scene's own element records, for requests without poses
     Prim* d_prims = nullptr;
     Optics* d_optics = nullptr;
     Aabb* d_aabbs = nullptr;
     Node* d_nodes = nullptr;
-    float zlo = 0.f, zhi = 0.f;
 };
 
 enum ReqState { kPending = 0, kActive = 1, kDone = 2, kFailed = 3 };
@@ -68,6 +67,8 @@ struct SRequest {
     uint32_t scene = 0;
     const SScene* sc = nullptr;  // set at submission (the scene list may grow meanwhile)
     std::vector<csp_element> poses;
+    HostScene hs;   // element records of the poses (built at submission)
+    HostGrid grid;  // grid of the poses (field-like scenes)
     double sun[3] = {0, 0, 1};
     int shape = CSP_SUN_PILLBOX;
     double param = 0;
@@ -80,7 +81,7 @@ struct SRequest {
     int group = kAccelBvh;
     size_t off = 0, bytes = 0;  // arena block
     size_t o_prims = 0, o_optics = 0, o_aabbs = 0, o_prune = 0, o_nodes = 0, o_sun = 0, o_grid = 0, o_counts = 0,
-           o_stats = 0;
+           o_stats = 0, o_cells = 0, o_items = 0, o_global = 0;
     bool own_records = false;
     int result_slot = -1;
     Clock::time_point t_submit, t_admit, t_done;
@@ -263,9 +264,8 @@ int Server::add_scene(const csp_element* el, uint32_t n, uint32_t* id) {
     int rc = build_elements(el, n, s->base, err);
     if (rc) return set_error(rc, err);
     build_bvh(s->base);
-    if (n > kFlatListMax) build_grid(el, n, s->base, s->grid);
+    if (n > kFlatListMax) build_grid(s->base, s->grid);
     s->group = n <= kFlatListMax ? kAccelFlat : (s->grid.valid ? kAccelGrid : kAccelBvh);
-    if (s->grid.valid) grid_layer(s->grid, s->base, s->zlo, s->zhi);
     auto put = [&](auto*& dptr, const auto& host, const char* what) {
         const size_t bytes = std::max<size_t>(1, host.size()) * sizeof(host[0]);
         int r = cuda_status(cudaMalloc((void**)&dptr, bytes), what);
@@ -296,33 +296,44 @@ size_t Server::request_bytes(const SRequest& r) const {
     if (!r.poses.empty()) {
         b += align256(n * sizeof(Prim)) + align256(n * sizeof(Optics)) + 2 * align256(n * sizeof(Aabb));
         if (r.group != kAccelGrid) b += align256(s.base.nodes.size() * sizeof(Node));
+        else
+            b += align256(r.grid.cell_start.size() * sizeof(uint32_t)) + align256(r.grid.items.size() * sizeof(Aabb)) +
+                 align256(std::max<size_t>(1, r.grid.global.size()) * sizeof(Aabb));
     }
     return b;
 }
 
 int Server::submit(const SRequest& in, uint64_t* id) {
-    std::lock_guard<std::mutex> lk(mu);
-    if (!fatal.empty()) return set_error(CSP_ERR_CUDA, "server stopped: " + fatal);
-    if (in.scene >= scenes.size()) return set_error(CSP_ERR_INVALID_ARGUMENT, "no such scene");
-    const SScene& s = *scenes[in.scene];
+    const SScene* sp = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (in.scene < scenes.size()) sp = scenes[in.scene].get();
+    }
+    if (!sp) return set_error(CSP_ERR_INVALID_ARGUMENT, "no such scene");
+    auto r = std::make_unique<SRequest>(in);
+    const SScene& s = *sp;
     if (!in.poses.empty()) {
         if (in.poses.size() != s.elements.size())
             return set_error(CSP_ERR_BAD_SCENE, "request poses must have the scene's element count");
         for (size_t k = 0; k < s.elements.size(); ++k)
             if (in.poses[k].surface != s.elements[k].surface || in.poses[k].aperture != s.elements[k].aperture)
                 return set_error(CSP_ERR_BAD_SCENE, "request pose " + std::to_string(k) + " changes the surface type");
+        // host work of the request, in the submitting thread: element records and grid of its poses
+        std::string err;
+        const int rc = build_elements(r->poses.data(), (uint32_t)r->poses.size(), r->hs, err);
+        if (rc) return set_error(rc, err);
+        if (s.group != kAccelFlat) build_grid(r->hs, r->grid);
     }
+    std::lock_guard<std::mutex> lk(mu);
+    if (!fatal.empty()) return set_error(CSP_ERR_CUDA, "server stopped: " + fatal);
     if (in.shape != CSP_SUN_PILLBOX && in.shape != CSP_SUN_GAUSSIAN)
         return set_error(CSP_ERR_INVALID_ARGUMENT, "unknown sun shape");
     if (!(in.param >= 0.0) || in.param > 0.5) return set_error(CSP_ERR_INVALID_ARGUMENT, "sun shape parameter out of range");
     if (in.rays == 0 || in.rays >= (1ull << 40)) return set_error(CSP_ERR_INVALID_ARGUMENT, "bad ray count");
-    auto r = std::make_unique<SRequest>(in);
     r->id = next_id++;
     r->sc = &s;
     r->group = s.group;
-    if (r->group == kAccelGrid && !r->poses.empty() &&
-        !grid_accepts(s.grid, r->poses.data(), (uint32_t)r->poses.size()))
-        r->group = kAccelBvh;  // poses move an origin or change a size: the scene's grid does not hold
+    if (r->group != kAccelFlat && !r->poses.empty()) r->group = r->grid.valid ? kAccelGrid : kAccelBvh;
     r->bytes = request_bytes(*r);
     if (r->bytes > budget) return set_error(CSP_ERR_OUT_OF_MEMORY, "request larger than the server memory budget");
     r->t_submit = Clock::now();
@@ -383,10 +394,21 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
             if (r.group != kAccelGrid) {
                 r.o_nodes = o;
                 o += align256(s.base.nodes.size() * sizeof(Node));
+            } else {
+                r.o_cells = o;
+                o += align256(r.grid.cell_start.size() * sizeof(uint32_t));
+                r.o_items = o;
+                o += align256(r.grid.items.size() * sizeof(Aabb));
+                r.o_global = o;
+                o += align256(std::max<size_t>(1, r.grid.global.size()) * sizeof(Aabb));
             }
         }
         stage_off[i] = stage;
-        if (r.own_records) stage += n * (sizeof(Prim) + sizeof(Optics) + 2 * sizeof(Aabb));
+        if (r.own_records) {
+            stage += n * (sizeof(Prim) + sizeof(Optics) + 2 * sizeof(Aabb));
+            if (r.group == kAccelGrid)
+                stage += r.grid.cell_start.size() * sizeof(uint32_t) + (r.grid.items.size() + r.grid.global.size()) * sizeof(Aabb);
+        }
         stage = align256(stage + sizeof(GridDesc));
     }
     const size_t refit_at = stage;
@@ -402,7 +424,6 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
         if (rc) return rc;
         adm_cap = stage;
     }
-    HostScene hs;
     RefitJob* refits = reinterpret_cast<RefitJob*>(h_adm + refit_at);
     SunJob* suns = reinterpret_cast<SunJob*>(h_adm + sun_at);
     int n_refit = 0, n_sun = 0, max_nodes = 0;
@@ -411,16 +432,9 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
         const SScene& s = *r.sc;
         const uint32_t n = (uint32_t)s.elements.size();
         unsigned char* h = h_adm + stage_off[i];
-        const HostScene* src = &s.base;
         const Aabb* d_aabbs = s.d_aabbs;
         if (r.own_records) {
-            int rc = build_elements(r.poses.data(), n, hs, err);
-            if (rc) {
-                r.state = kFailed;
-                r.error = err;
-                continue;
-            }
-            src = &hs;
+            const HostScene& hs = r.hs;
             const size_t bp = n * sizeof(Prim), bo = n * sizeof(Optics), ba = n * sizeof(Aabb);
             std::memcpy(h, hs.prims.data(), bp);
             std::memcpy(h + bp, hs.optics.data(), bo);
@@ -446,25 +460,27 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
         }
         if (r.group == kAccelGrid) {
             GridDesc g;
-            g.x0 = s.grid.x0;
-            g.y0 = s.grid.y0;
-            g.x1 = s.grid.x1;
-            g.y1 = s.grid.y1;
-            g.cell = s.grid.cell;
-            g.inv_cell = s.grid.inv_cell;
-            if (r.own_records) grid_layer(s.grid, *src, g.zlo, g.zhi);
-            else {
-                g.zlo = s.zlo;
-                g.zhi = s.zhi;
+            if (r.own_records) {
+                const HostGrid& hg = r.grid;
+                const size_t bc = hg.cell_start.size() * sizeof(uint32_t), bi = hg.items.size() * sizeof(Aabb),
+                             bg = hg.global.size() * sizeof(Aabb);
+                std::memcpy(h, hg.cell_start.data(), bc);
+                std::memcpy(h + bc, hg.items.data(), bi);
+                if (bg) std::memcpy(h + bc + bi, hg.global.data(), bg);
+                int rc2 = cuda_status(cudaMemcpyAsync(d_arena + r.o_cells, h, bc, cudaMemcpyHostToDevice, stream), "upload");
+                if (!rc2 && bi)
+                    rc2 = cuda_status(cudaMemcpyAsync(d_arena + r.o_items, h + bc, bi, cudaMemcpyHostToDevice, stream), "upload");
+                if (!rc2 && bg)
+                    rc2 = cuda_status(cudaMemcpyAsync(d_arena + r.o_global, h + bc + bi, bg, cudaMemcpyHostToDevice, stream),
+                                      "upload");
+                if (rc2) return rc2;
+                h += bc + bi + bg;
+                g = grid_desc(hg, reinterpret_cast<const uint32_t*>(d_arena + r.o_cells),
+                              reinterpret_cast<const Aabb*>(d_arena + r.o_items),
+                              reinterpret_cast<const Aabb*>(d_arena + r.o_global));
+            } else {
+                g = grid_desc(s.grid, s.d_cells, s.d_items, s.d_global);
             }
-            g.nx = s.grid.nx;
-            g.ny = s.grid.ny;
-            g.n_global = (int)s.grid.global.size();
-            g.pad = 0;
-            g.cell_start = s.d_cells;
-            g.items = s.d_items;
-            g.global = s.d_global;
-            g.aabbs = d_aabbs;
             std::memcpy(h, &g, sizeof g);
             int rc2 = cuda_status(cudaMemcpyAsync(d_arena + r.o_grid, h, sizeof g, cudaMemcpyHostToDevice, stream), "upload");
             if (rc2) return rc2;

@@ -40,10 +40,10 @@ struct System {
     float4* d_hits = nullptr;
     uint32_t* d_ids = nullptr;
     GridDesc* d_grid = nullptr;
-    GridDesc grid_desc{};  // host copy (source of the async upload)
+    GridDesc grid_host{};  // host copy of the descriptor (source of the async upload)
     uint32_t* d_cells = nullptr;
-    uint32_t* d_items = nullptr;
-    uint32_t* d_global = nullptr;
+    Aabb* d_items = nullptr;
+    Aabb* d_global = nullptr;
     size_t cap_cells = 0, cap_items = 0, cap_global = 0;
     uint32_t* d_flux = nullptr;              // csp_flux_map counts
     unsigned long long* d_fstats = nullptr;  // [4]

@@ -398,12 +398,12 @@ __device__ __forceinline__ int traverse(const Node* __restrict__ nodes, const Pr
     return best;
 }
 
-// Exact-AABB culling and intersection program of one candidate element (a BVH leaf's work).
-__device__ __forceinline__ void test_element(uint32_t w, const Prim* __restrict__ prims, const Aabb* __restrict__ aabbs,
-                                             float3 o, float3 d, float3 inv, float tmin, int& best, float& best_t,
-                                             uint32_t& best_type, float& prune) {
-    const uint32_t prim = w & kPrimMask;
-    const float4* q = reinterpret_cast<const float4*>(aabbs + prim);
+// Exact-AABB culling and intersection program of one grid candidate (a BVH leaf's work): `it` is
+// the element's exact AABB with lo.w = element | type << 28.
+__device__ __forceinline__ void test_item(const Aabb* __restrict__ it, const Prim* __restrict__ prims, float3 o,
+                                          float3 d, float3 inv, float tmin, int& best, float& best_t,
+                                          uint32_t& best_type, float& prune) {
+    const float4* q = reinterpret_cast<const float4*>(it);
     const float4 lo = __ldg(q), hi = __ldg(q + 1);
     const float t0x = (lo.x - o.x) * inv.x, t1x = (hi.x - o.x) * inv.x;
     const float t0y = (lo.y - o.y) * inv.y, t1y = (hi.y - o.y) * inv.y;
@@ -411,6 +411,8 @@ __device__ __forceinline__ void test_element(uint32_t w, const Prim* __restrict_
     const float tn = fmaxf(tmin, fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z)));
     const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
     if (!(tn <= fminf(kTmax, tf))) return;
+    const uint32_t w = __float_as_uint(lo.w);
+    const uint32_t prim = w & kPrimMask;
     const uint32_t type = (w >> kTypeShift) & 7u;
     float t;
     if (hit_prim(type, load_prim(prims, prim), o, d, tmin, t) && (t < best_t || (t == best_t && (int)prim < best))) {
@@ -437,10 +439,10 @@ __device__ __forceinline__ void clip_axis(float o, float d, float inv, float lo,
 }
 
 // Closest hit through the field grid: the global elements, then the cells of the xy path inside
-// the layer in ray order (2D DDA), each cell's candidates through test_element, until a cell is
+// the layer in ray order (2D DDA), each cell's candidates through test_item, until a cell is
 // entered beyond the pruning distance.  The result equals traverse()'s: every element whose
 // surface holds a hit point at t is registered in the cell the walk assigns to that point (the
-// registered squares exceed the surfaces by a margin far above the walk's rounding), that cell is
+// registered boxes exceed the surfaces by a margin far above the walk's rounding), that cell is
 // entered at or before t, and the walk only stops beyond best_t + best_t 1e-3 + 1e-3.
 __device__ __forceinline__ int traverse_grid(const GridDesc& G, const Prim* __restrict__ prims, float3 o, float3 d,
                                              float tmin, float& best_t, uint32_t& best_type) {
@@ -460,11 +462,11 @@ __device__ __forceinline__ int traverse_grid(const GridDesc& G, const Prim* __re
     const float inf = __int_as_float(0x7f800000);
     float tc = ta;
     // candidate lists in order: the global elements, then the cells of the walk (one test site)
-    const uint32_t* list = G.global;
+    const Aabb* list = G.global;
     uint32_t j = 0, e = (uint32_t)G.n_global;
     int step = -1;
     for (;;) {
-        for (; j < e; ++j) test_element(__ldg(list + j), prims, G.aabbs, o, d, inv, tmin, best, best_t, best_type, prune);
+        for (; j < e; ++j) test_item(list + j, prims, o, d, inv, tmin, best, best_t, best_type, prune);
         if (step >= 0) {
             // next cell: parameters of the next x and y cell boundaries, from the cell index
             const float tnx = (d.x != 0.0f) ? (G.x0 + (float)(ix + (sx > 0)) * G.cell - o.x) * inv.x : inf;

@@ -71,20 +71,21 @@ struct alignas(16) SunFrame {
 };
 
 // Uniform 2D grid over a planar heliostat field (the alternative to the BVH for field-like
-// scenes).  Cells of size `cell` cover [x0, x1] x [y0, y1]; the items of cell (ix, iy) are
-// items[cell_start[iy * nx + ix] .. cell_start[iy * nx + ix + 1]), each element | type << 28, an
-// element being registered in every cell its orientation-independent bounding box overlaps.  Rays
-// walk the cells their xy path crosses inside the layer [zlo, zhi] (which holds every gridded
-// surface); the global items (the receiver, oversized elements) are tested by every ray.  Every
-// candidate still passes the exact AABB test before its intersection program runs.
+// scenes), built for one set of poses.  Cells of size `cell` cover [x0, x1] x [y0, y1]; the items of
+// cell (ix, iy) are items[cell_start[iy * nx + ix] .. cell_start[iy * nx + ix + 1]), one per element
+// whose pruning box (widened by a margin) overlaps the cell in xy: the element's exact AABB with
+// lo.w = element | type << 28 (bits).  Rays walk the cells their xy path crosses inside the layer
+// [zlo, zhi], which holds every gridded surface; the global items (the receiver, oversized
+// elements) are tested by every ray.  Every candidate passes the exact AABB test before its
+// intersection program runs.
 struct alignas(16) GridDesc {
     float x0, y0, x1, y1;
     float cell, inv_cell, zlo, zhi;
     int nx, ny, n_global, pad;
     const uint32_t* cell_start;
-    const uint32_t* items;
-    const uint32_t* global;
-    const Aabb* aabbs;  // exact element AABBs
+    const Aabb* items;
+    const Aabb* global;
+    const void* reserved;
 };
 
 // Receiver flux map target (scripts/post_processing/flux_map_calculator.py:135-179 binning, in

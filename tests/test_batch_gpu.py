@@ -116,8 +116,8 @@ def test_batch_instances_equal_plain_runs(gpu):
 
 
 def test_batch_groups(gpu):
-    """Re-aimed field instances run in the grid group; an instance whose poses move a heliostat
-    runs in the BVH group; both equal plain runs."""
+    """Field instances with their own poses (re-aimed, and one with a moved heliostat) run in the grid
+    group, each with the grid of its poses; both equal plain runs."""
     from optixsoltracedemos_gb300 import native
     b = native.Batch(0)
     try:
