@@ -496,7 +496,7 @@ void build_grid(const HostScene& s, HostGrid& g) {
         sizes.push_back(size[i]);
     }
     std::nth_element(sizes.begin(), sizes.begin() + sizes.size() / 2, sizes.end());
-    double cell = (double)(float)(1.0 * sizes[sizes.size() / 2]);
+    double cell = (double)(float)(1.4 * sizes[sizes.size() / 2]);
     if (!(cell > 0)) return;
     double X0 = DBL_MAX, Y0 = DBL_MAX, X1 = -DBL_MAX, Y1 = -DBL_MAX;
     float zmin = FLT_MAX, zmax = -FLT_MAX;
