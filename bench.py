@@ -16,6 +16,12 @@ the dense 16M x 5 float4 hit buffer (1.34 GB, larger than L2, so no flush is nee
   roofline   HBM: algorithmic bytes = 80 B per ray (the dense hit records) / per-launch time.
   cpu_baseline  the oracle port of the reference algorithm on all host cores, bounded sample.
 
+The default line also carries `batched` (256 sun positions of the 10,000-heliostat field, one
+csp_batch run, against the plain per-scene loop through the drop-in handle) and `served` (300
+requests over fields of 3 / 1,000 / 10,000 heliostats through csp_server, at saturation and with
+Poisson arrivals at 200/s: p50 / p99 latency, against the plain loop); `--workload batched|served`
+prints those lines in full, `--no-systems` leaves them out.
+
 --impl reference times the reference algorithm's CPU implementation (the oracle port: the
 reference's own programs cannot run this workload's Gaussian sun and slope error) on all host
 cores, on the same workload and metric.
@@ -61,6 +67,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-accuracy", action="store_true")
+    p.add_argument("--no-systems", action="store_true",
+                   help="default line without the batched and served summaries")
     p.add_argument("--tuning", type=str, default="", help="batched workload: block,ctas_per_sm,chunk (default: autotune)")
     p.add_argument("--requests", type=int, default=300, help="served workload: number of requests")
     p.add_argument("--rate", type=float, default=200.0, help="served workload: Poisson arrival rate (1/s)")
@@ -331,6 +339,28 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds, sc)
     tr.close()
+    if world == 1 and not args.no_systems and args.workload == "single_parabolic" and args.rays is None:
+        # the batched and served workloads against the plain per-scene loop (flux maps identical)
+        sys_args = argparse.Namespace(**vars(args))
+        sys_args.steps, sys_args.warmup = 3, 2
+        b = measure_batched(sys_args, local, world)
+        line["batched"] = {
+            "workload": b["config"]["workload"], "rays": b["config"]["rays_total"],
+            "rays_per_s_device": b["value"], "rays_per_s_wall": b["batched_wall_rays_per_s"],
+            "plain_loop_rays_per_s": b["plain_loop"]["rays_per_s"], "speedup_vs_plain_loop": b["speedup_vs_plain_loop"],
+            "flux_counts_mismatching_plain": b["plain_loop"]["flux_counts_mismatching_batched"],
+            "tuning_grid": b["config"]["tuning_grid"]}
+        v = measure_served(sys_args, local, world)
+        line["served"] = {
+            "workload": v["config"]["workload"], "requests": v["config"]["requests"], "rays": v["config"]["rays_total"],
+            "saturation_rays_per_s": v["served_saturation"]["rays_per_s"],
+            "plain_loop_saturation_rays_per_s": v["plain_loop_saturation"]["rays_per_s"],
+            "speedup_vs_plain_loop": v["speedup_vs_plain_loop"],
+            "poisson_rate_per_s": v["config"]["arrival_rate_per_s"],
+            "poisson_p50_s": v["served_poisson"]["p50_s"], "poisson_p99_s": v["served_poisson"]["p99_s"],
+            "plain_loop_poisson_p50_s": v["plain_loop_poisson"]["p50_s"],
+            "plain_loop_poisson_p99_s": v["plain_loop_poisson"]["p99_s"],
+            "flux_counts_mismatching_plain": v["plain_loop_saturation"]["flux_counts_mismatching_served"]}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if pg:
@@ -349,13 +379,19 @@ def batched_workload(n_instances, n_heliostats):
 
 
 def run_batched(args):
+    rank, world, local = dist_env()
+    line = measure_batched(args, local, world)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def measure_batched(args, local, world):
     """Batched workload: one csp_batch run (host element builds, upload, device refit, sun planes,
     one persistent trace launch, flux maps back) against the plain per-scene loop through the
     drop-in handle (per instance: new poses and sun, update, run, device flux map)."""
     import numpy as np
     import torch
 
-    rank, world, local = dist_env()
     torch.cuda.set_device(local)
     from optixsoltracedemos_gb300 import build as nbuild
     nbuild.build()
@@ -430,8 +466,8 @@ def run_batched(args):
         "gpu_launches": 1 + 1 + 1,
         "clocks": clocks,
     }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    b.close()
+    return line
 
 
 def served_workload(n_requests, rate):
@@ -463,6 +499,13 @@ def served_workload(n_requests, rate):
 
 
 def run_served(args):
+    rank, world, local = dist_env()
+    line = measure_served(args, local, world)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def measure_served(args, local, world):
     """Serving workload through csp_server (continuous batching) against the plain per-scene loop
     (one drop-in handle per scene: update, run, device flux map per request, in arrival order), at
     saturation (all requests queued at once) and with real-time Poisson arrivals."""
@@ -470,7 +513,6 @@ def run_served(args):
     import numpy as np
     import torch
 
-    rank, world, local = dist_env()
     torch.cuda.set_device(local)
     from optixsoltracedemos_gb300 import build as nbuild
     nbuild.build()
@@ -572,8 +614,7 @@ def run_served(args):
         "gpu_launches": None,
         "clocks": clocks,
     }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    return line
 
 
 def main():
