@@ -181,6 +181,25 @@ def test_batch_rerun_and_relayout(gpu):
         b.close()
 
 
+def test_batch_empty_instances(gpu):
+    """Instances with no rays trace nothing and leave empty flux maps; the others are unaffected."""
+    from optixsoltracedemos_gb300 import native
+    th = scenes.three_heliostats()
+    b = native.Batch(0)
+    try:
+        sid = b.add_scene(th.elements)
+        b.add_instance(sid, th.sun_dir, th.sun_shape, th.sun_param, 0, seed=1, instance=0)
+        b.add_instance(sid, th.sun_dir, th.sun_shape, th.sun_param, 77777, seed=1, instance=1)
+        b.add_instance(sid, th.sun_dir, th.sun_shape, th.sun_param, 0, seed=1, instance=2)
+        b.run()
+        assert b.counts(0).sum() == 0 and b.counts(2).sum() == 0
+        assert list(b.stats(0)) == [0, 0, 0, 0]
+        counts, _, _ = _plain_counts(native, th.elements, th.sun_dir, th.sun_shape, th.sun_param, 77777, 1, 1)
+        np.testing.assert_array_equal(b.counts(1), counts)
+    finally:
+        b.close()
+
+
 def test_batch_rejects_bad_instances(gpu):
     from optixsoltracedemos_gb300 import native
     b = native.Batch(0)

@@ -149,3 +149,32 @@ def test_server_rejects_bad_requests(gpu):
             srv.submit(sid2, th.sun_dir, 0, 4.65e-3, 1000, poses=big)
     finally:
         srv.close()
+
+
+def test_server_ray_indices_beyond_32_bits(gpu):
+    """A request of 5e9 rays (ray indices past 2^32, sliced over many server steps) bins exactly
+    what one batch launch of the same rays bins; an impatient wait times out and a later wait still
+    gets the result."""
+    from optixsoltracedemos_gb300 import native
+    th = scenes.three_heliostats()
+    rays = 5_000_000_000
+    srv = native.Server(0, memory_budget=64 << 20, max_active=4, step_rays=1 << 30)
+    try:
+        sid = srv.add_scene(th.elements)
+        rid = srv.submit(sid, th.sun_dir, th.sun_shape, th.sun_param, rays, seed=3, instance=1)
+        with pytest.raises(native.CspError):
+            srv.wait(rid, timeout=0.0)
+        c_srv, st_srv, _ = srv.wait(rid, timeout=300)
+        assert srv.stats()["steps"] >= 5
+    finally:
+        srv.close()
+    b = native.Batch(0)
+    try:
+        sid = b.add_scene(th.elements)
+        b.add_instance(sid, th.sun_dir, th.sun_shape, th.sun_param, rays, seed=3, instance=1)
+        b.run()
+        np.testing.assert_array_equal(b.counts(0), c_srv)
+        np.testing.assert_array_equal(b.stats(0), st_srv)
+        assert st_srv[0] == rays and st_srv[3] > 0.02 * rays
+    finally:
+        b.close()
