@@ -262,6 +262,10 @@ CSP_API int csp_server_add_scene(csp_server s, const csp_element* elements, uint
 CSP_API int csp_server_submit(csp_server s, uint32_t scene_id, const csp_element* poses, const double* sun_dir,
                               int sun_shape, double sun_param, uint64_t num_rays, uint64_t seed, uint32_t instance,
                               uint64_t* request_id);
+/* hold != 0: admit no further requests (they stay queued; active ones run to completion);
+ * hold == 0: resume admission, admitting the queued requests together.  Destroying a held server
+ * drops its queued requests. */
+CSP_API int csp_server_hold(csp_server s, int hold);
 /* Block until the request is done (timeout_s < 0: no limit; CSP_ERR_TIMEOUT otherwise), then hand
  * out its results and forget it: counts[100 * 100] (bin (i, j) at i * 100 + j, as csp_flux_map),
  * stats[4] (rays, mirror records, receiver records, binned records), latency_s[2] (submission to

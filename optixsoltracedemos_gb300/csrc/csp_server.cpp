@@ -170,6 +170,7 @@ struct Server {
     std::condition_variable cv_work, cv_done;
     std::thread worker;
     bool stopping = false;
+    bool hold = false;  // admission paused (requests queue; active ones finish)
     std::string fatal;
 
     // statistics
@@ -353,7 +354,8 @@ int Server::submit(const SRequest& in, uint64_t* id) {
 int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
     {
         std::lock_guard<std::mutex> lk(mu);
-        while (!pending.empty() && (int)(active.size() + admitted.size()) < max_active && !free_res_slots.empty()) {
+        while (!hold && !pending.empty() && (int)(active.size() + admitted.size()) < max_active &&
+               !free_res_slots.empty()) {
             SRequest* r = pending.front();
             size_t off = 0;
             if (!arena.alloc(r->bytes, off)) break;  // wait for completions to free memory
@@ -605,8 +607,8 @@ void Server::run_worker() {
     for (;;) {
         {
             std::unique_lock<std::mutex> lk(mu);
-            cv_work.wait(lk, [&] { return stopping || !pending.empty() || !active.empty(); });
-            if (stopping && pending.empty() && active.empty()) break;
+            cv_work.wait(lk, [&] { return stopping || (!pending.empty() && !hold) || !active.empty(); });
+            if (stopping && active.empty() && (pending.empty() || hold)) break;
         }
         uint64_t rays = 0;
         std::string err;
@@ -740,6 +742,17 @@ int csp_server_submit(csp_server sh, uint32_t scene, const csp_element* poses, c
     r.seed = seed;
     r.instance = instance;
     return s->submit(r, request);
+}
+
+int csp_server_hold(csp_server sh, int hold) {
+    CSP_SGUARD(sh);
+    Server* s = reinterpret_cast<Server*>(sh);
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->hold = hold != 0;
+    }
+    s->cv_work.notify_all();
+    return CSP_OK;
 }
 
 int csp_server_wait(csp_server sh, uint64_t request, double timeout_s, uint32_t* counts, uint64_t* stats,

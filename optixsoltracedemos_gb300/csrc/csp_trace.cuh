@@ -649,6 +649,11 @@ __device__ __forceinline__ Segment generate(const TraceArgs& A, const SunFrame& 
     return Segment{pos, dir, kTminSun, 0};
 }
 
+// Queue entries of BVH/grid launches carry the depth of their pending mirror hit in the top bits of
+// the ray index (ray indices stay below 2^56).
+constexpr int kDepthShift = 56;
+constexpr uint64_t kRayMask = (1ull << kDepthShift) - 1u;
+
 // Shared memory of one CTA: the ray queue, the Halton table, the sun frame and the kFlat scene.
 template <int kB>
 struct CoreSmem {
@@ -796,16 +801,39 @@ __device__ void drain(const TraceArgs& A, const Sink& k, CoreSmem<C::kB>& sm, bo
         if (threadIdx.x == 0) sm.qsize = base;
         __syncthreads();
         if (have) {
-            const Segment g{o, d, kTminSun, 0};
-            Hit h;
             if (C::kFlat) {
                 // first segment from the sun: intersection programs of the candidate elements
+                const Segment g{o, d, kTminSun, 0};
+                Hit h;
                 h.best = closest_in(sm.flat, w, o, d, kTminSun, h.t, h.type);
-            } else {
-                // pending mirror hit of the first segment: its record was emitted in phase A
-                h = Hit{(int)(w & kPrimMask), t, w >> kTypeShift};
+                finish_path<C>(A, k, sm, ray, g, h, false);
             }
-            finish_path<C>(A, k, sm, ray, g, h, !C::kFlat);
+        }
+        if (!C::kFlat) {
+            // one bounce per batch: shade the pending mirror hit (its record is out), find the next
+            // hit, record it, and queue it again when it is another mirror below the depth limit
+            bool again = false;
+            Segment next{f3(0.f, 0.f, 0.f), f3(0.f, 0.f, 1.f), 0.f, 0};
+            Hit h2{-1, 0.f, 0u};
+            const uint64_t r = ray & kRayMask;
+            if (have) {
+                const int depth = (int)(ray >> kDepthShift);
+                const Segment g{o, d, depth == 0 ? kTminSun : kTminBounce, depth};
+                const Hit h{(int)(w & kPrimMask), t, w >> kTypeShift};
+                const Prim p = load_prim(A.prims, (uint32_t)h.best);
+                if (shade_mirror(A, r, p, A.optics[h.best], g, h, next)) {
+                    h2.best = find_closest<C>(A, sm, next.o, next.d, next.tmin, h2.t, h2.type);
+                    if (h2.best >= 0) {
+                        const Prim p2 = load_prim(A.prims, (uint32_t)h2.best);
+                        float4 rec;
+                        int slot;
+                        again = classify(p2, next, h2, rec, slot);
+                        if (slot >= 0) emit<C>(A, k, r, slot, rec, (uint32_t)h2.best);
+                    }
+                }
+            }
+            push<C::kB>(sm, again, r | ((uint64_t)next.depth << kDepthShift), next.o, next.d, h2.t,
+                        (uint32_t)h2.best | (h2.type << kTypeShift));
         }
         __syncthreads();
         qs = sm.qsize;

@@ -93,6 +93,7 @@ SIGNATURES = {
     "csp_server_submit": (ctypes.c_int, [_H, ctypes.c_uint32, _P, _P, ctypes.c_int, ctypes.c_double, ctypes.c_uint64,
                                          ctypes.c_uint64, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)]),
     "csp_server_wait": (ctypes.c_int, [_H, ctypes.c_uint64, ctypes.c_double, _P, _P, _P]),
+    "csp_server_hold": (ctypes.c_int, [_H, ctypes.c_int]),
     "csp_server_stats": (ctypes.c_int, [_H, _P]),
 }
 STINPUT_APPLY_OPTICS = 1
@@ -403,6 +404,10 @@ class Server:
         _check(self.lib.csp_server_submit(self.h, int(scene), _ptr(p), _ptr(sd), int(sun_shape), float(sun_param),
                                           int(num_rays), int(seed), int(instance), ctypes.byref(rid)))
         return rid.value
+
+    def hold(self, on: bool = True):
+        """Pause (True) or resume (False) admission of queued requests."""
+        _check(self.lib.csp_server_hold(self.h, 1 if on else 0))
 
     def wait(self, request: int, timeout: float = -1.0):
         """(counts [100, 100] uint32, stats [4] uint64, (latency s, queueing s))."""

@@ -71,8 +71,10 @@ def test_server_results_same_alone_and_in_mix(gpu):
             c, st, lat = srv.wait(rid, timeout=120)
             alone.append((c, st))
             assert lat[0] >= lat[1] >= 0
-        # the mix: all requests submitted at once from four threads
+        # the mix: all requests submitted from four threads while admission is held, then admitted
+        # together (8 slots for 10 requests: the last two join while the first ones run)
         ids = [None] * len(reqs)
+        srv.hold(True)
 
         def sub(k):
             for i in range(k, len(reqs), 4):
@@ -82,6 +84,7 @@ def test_server_results_same_alone_and_in_mix(gpu):
             t.start()
         for t in th:
             t.join()
+        srv.hold(False)
         for i, rid in enumerate(ids):
             c, st, _ = srv.wait(rid, timeout=120)
             np.testing.assert_array_equal(c, alone[i][0], err_msg=f"request {i}")
