@@ -97,8 +97,16 @@ __device__ __forceinline__ void finish_instance(BatchSmem<C::kB>& sm, const Sink
     __syncthreads();
 }
 
+// Resident threads per SM the register budget is cut for: 1024 for the field kernels (64
+// registers: more warps to hide the grid walk's load latency), 768 for the element-list kernel
+// (which would spill at 64).
+template <int kAccel>
+constexpr int batch_threads_per_sm() {
+    return kAccel == kAccelFlat ? 768 : 1024;
+}
+
 template <int kB, int kAccel>
-__global__ void __launch_bounds__(kB, 768 / kB) batch_kernel(const BatchLaunch L) {
+__global__ void __launch_bounds__(kB, batch_threads_per_sm<kAccel>() / kB) batch_kernel(const BatchLaunch L) {
     using C = Cfg<kB, kAccel, false, true>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BatchSmem<kB>& sm = *reinterpret_cast<BatchSmem<kB>*>(smem_raw);
