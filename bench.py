@@ -143,6 +143,17 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(seconds: float, pg, device: str) -> float:
+    """Replica timing: the largest of every rank's seconds (the job ends with its slowest replica);
+    the value itself when there is no process group."""
+    if pg is None:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], device=device, dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
 def cpu_baseline(seconds: float, sc):
     """Oracle port of the reference algorithm on all host cores over a bounded sample."""
     from oracle import oracle
@@ -268,7 +279,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     e0.record(stream)
     for k in range(args.steps):
-        tr.set_seed(1000 + k)
+        tr.set_seed(1000 + k, rank)  # each replica traces its own rays (Philox instance = rank)
         starts[k].record(stream)
         tr.trace_async(sp)
         ends[k].record(stream)
@@ -277,10 +288,7 @@ def run_ours(args):
     clocks = clk.stop()
     total_s = e0.elapsed_time(e1) * 1e-3
     launch_s = statistics.mean(s.elapsed_time(e) for s, e in zip(starts, ends)) * 1e-3
-    if pg:
-        t = torch.tensor([total_s], device=f"cuda:{local}", dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        total_s = float(t.item())
+    total_s = max_over_ranks(total_s, pg, f"cuda:{local}")
     value = world * N * args.steps / total_s
 
     # end to end through the C ABI with host buffers
@@ -294,15 +302,12 @@ def run_ours(args):
         pg.barrier()
     t0 = time.perf_counter()
     for k in range(args.e2e_steps):
-        tr.set_seed(5000 + k)
+        tr.set_seed(5000 + k, rank)
         tr.set_elements(elements)
         tr.update()
         tr.run_to_host_ptr(host.data_ptr())
     e2e_s = (time.perf_counter() - t0) / args.e2e_steps
-    if pg:
-        t = torch.tensor([e2e_s], device=f"cuda:{local}", dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, pg, f"cuda:{local}")
 
     peak, peak_kind = peaks()
     achieved = BYTES_PER_RAY * N / launch_s / 1e9
