@@ -30,6 +30,7 @@
 #include <thread>
 #include <tuple>
 
+#include "csp_math.cuh"
 #include "csp_system.h"
 
 namespace csp {
@@ -85,6 +86,7 @@ int Batch::ensure_stream() {
     if (stream) return CSP_OK;
     int rc = cuda_status(cudaSetDevice(device), "cudaSetDevice");
     if (rc) return rc;
+    h3t12 = halton3_table();
     if ((rc = cuda_status(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate"))) return rc;
     if ((rc = cuda_status(cudaEventCreate(&ev0), "cudaEventCreate"))) return rc;
     return cuda_status(cudaEventCreate(&ev1), "cudaEventCreate");
@@ -346,6 +348,7 @@ void Batch::fill_descs(const int* block, double sample, std::vector<InstanceDesc
         d.args.instance = b.instance;
         d.args.pad = 0;
         d.args.grid = nullptr;
+        d.args.h3t12 = h3t12;
         if (g == kAccelGrid) {
             const bool own = !b.poses.empty();
             const BScene& bs = scenes[b.scene];

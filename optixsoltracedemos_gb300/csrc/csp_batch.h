@@ -52,6 +52,7 @@ struct Batch {
     int device = -1;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    const float* h3t12 = nullptr;  // Halton table of the device
     uint32_t nx = 100, ny = 100;
     std::vector<BScene> scenes;
     std::vector<BInst> inst;

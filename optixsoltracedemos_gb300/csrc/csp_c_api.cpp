@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include "csp_kernels.cuh"
+#include "csp_math.cuh"
 #include "csp_scene.h"
 #include "csp_system.h"
 
@@ -177,6 +178,7 @@ int System::initialize() {
     const auto t0 = std::chrono::steady_clock::now();
     int rc = ensure_streams();
     if (rc) return rc;
+    h3t12 = halton3_table();
     std::string err;
     if ((rc = build_elements(elements.data(), (uint32_t)elements.size(), scene, err))) return fail(rc, err);
     build_bvh(scene);
@@ -228,6 +230,7 @@ TraceArgs System::args(uint64_t begin, uint64_t count) const {
     a.instance = instance;
     a.pad = 0;
     a.grid = grid.valid ? d_grid : nullptr;
+    a.h3t12 = h3t12;
     return a;
 }
 

@@ -15,6 +15,7 @@
 //                        (scripts/post_processing/flux_map_calculator.py:135-179)
 // The device functions of the path live in csp_trace.cuh.
 #include <algorithm>
+#include <mutex>
 
 #include "csp_kernels.cuh"
 #include "csp_trace.cuh"
@@ -43,7 +44,7 @@ struct TraceSmem {
 
 // Persistent kernel over the tiles of one launch (static round robin); dense records out.
 template <int kAccel>
-__global__ void __launch_bounds__(kTraceBlock, 6) trace_kernel(const TraceArgs A) {
+__global__ void __launch_bounds__(kTraceBlock, 6) trace_kernel(const typename PlainCfg<kAccel>::Args A) {
     using C = PlainCfg<kAccel>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TraceSmem& sm = *reinterpret_cast<TraceSmem*>(smem_raw);
@@ -73,9 +74,12 @@ cudaError_t launch_trace_t(const TraceArgs& args, cudaStream_t stream) {
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel<kAccel>, kTraceBlock,
                                                           sizeof(TraceSmem));
     if (e != cudaSuccess) return e;
-    const uint64_t tiles = (args.count + kTraceBlock - 1) / kTraceBlock;
+    const uint64_t tiles = (args.count + kTraceBlock - 1) / kTraceBlock;  // CTAs that have work
     const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)std::max(1, sms * std::max(1, per_sm)));
-    trace_kernel<kAccel><<<(unsigned)grid, kTraceBlock, sizeof(TraceSmem), stream>>>(args);
+    typename PlainCfg<kAccel>::Args a;
+    static_cast<TraceArgs&>(a) = args;
+    if constexpr (PlainCfg<kAccel>::kSched) philox_keys(args.seed, a.keys);
+    trace_kernel<kAccel><<<(unsigned)grid, kTraceBlock, sizeof(TraceSmem), stream>>>(a);
     return cudaGetLastError();
 }
 
@@ -96,7 +100,36 @@ __global__ void __launch_bounds__(kFluxBlock) flux_records_kernel(const float4* 
     if (threadIdx.x < 4 && threadIdx.x > 0 && stat[threadIdx.x]) atomicAdd(F.stats + threadIdx.x, stat[threadIdx.x]);
 }
 
+__global__ void __launch_bounds__(256) halton3_table_kernel(float* __restrict__ t) {
+    const uint32_t m = blockIdx.x * 256u + threadIdx.x;
+    if (m < kH3T12) t[m] = halton3(m);
+}
+
 }  // namespace
+
+const float* halton3_table() {
+    constexpr int kMaxDevices = 64;
+    static std::mutex mu;
+    static float* tables[kMaxDevices] = {};
+    static bool tried[kMaxDevices] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    if (!tried[dev]) {
+        tried[dev] = true;
+        float* t = nullptr;
+        if (cudaMalloc((void**)&t, kH3T12 * sizeof(float)) == cudaSuccess) {
+            halton3_table_kernel<<<(kH3T12 + 255) / 256, 256>>>(t);
+            if (cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess) tables[dev] = t;
+            else cudaFree(t);
+        }
+        cudaGetLastError();  // a failed table only means the loop path
+    }
+    return tables[dev];
+}
 
 cudaError_t launch_prepare_sun(const Aabb* aabbs, int n, float sx, float sy, float sz, float tan_pad, int shape,
                                float param, SunFrame* out, cudaStream_t stream) {

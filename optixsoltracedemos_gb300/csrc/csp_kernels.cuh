@@ -25,7 +25,19 @@ struct TraceArgs {
     uint32_t instance;
     int pad;
     const GridDesc* grid;  // field grid of the scene, nullptr: BVH (or element list) traversal
+    const float* h3t12;    // Halton base-3 partial sums after 12 digits (halton3_table), or nullptr
 };
+
+// Arguments of the single-scene element-list kernel: TraceArgs plus the Philox key schedule of
+// `seed` (philox_keys), read as kernel parameters.
+struct TraceArgsK : TraceArgs {
+    uint32_t keys[20];
+};
+
+// Device table of the base-3 Halton fold after its first 12 digits, t[m] = the reference loop's
+// sum for m < 3^12 (2.1 MB, filled once per device by the same loop), or nullptr if it could not be
+// made.  Thread-safe; the calling thread's current device.
+const float* halton3_table();
 
 // Sun-plane distance and parallelogram (lib/geometry_manager.cpp:97-148 with the reductions of
 // lib/sun_utils.cu:53-179) plus the per-launch cone frame (cuda/sun.cu:76-79), one block.

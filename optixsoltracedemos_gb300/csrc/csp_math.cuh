@@ -87,6 +87,35 @@ CSP_HD u32x4 philox4x32_10(u32x4 c, uint32_t k0, uint32_t k1) {
     return c;
 }
 
+// The same rounds with the key schedule precomputed: keys[2r], keys[2r + 1] = the key of round r.
+CSP_HD u32x4 philox4x32_10_sched(u32x4 c, const uint32_t* keys) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c.x, p1 = (uint64_t)0xCD9E8D57u * c.z;
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        c = u32x4{hi1 ^ c.y ^ keys[2 * r], lo1, hi0 ^ c.w ^ keys[2 * r + 1], lo0};
+    }
+    return c;
+}
+
+// Key schedule of a seed for philox4x32_10_sched.
+CSP_HD void philox_keys(uint64_t seed, uint32_t* keys) {
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    for (int r = 0; r < 10; ++r) {
+        keys[2 * r] = k0;
+        keys[2 * r + 1] = k1;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+// Draw block for (ray, bounce, draw, instance) under the key schedule of the seed.
+CSP_HD u32x4 draw_block_sched(uint64_t ray, uint32_t bounce, uint32_t draw, uint32_t instance, const uint32_t* keys) {
+    return philox4x32_10_sched(u32x4{(uint32_t)ray, (uint32_t)(ray >> 32), (bounce << 4) | (draw & 15u), instance},
+                               keys);
+}
+
 // Draw block for (ray, bounce, draw, instance) under key = seed.  bounce 0 = sun sample,
 // bounce k >= 1 = k-th surface interaction; draw selects one of up to 16 blocks per bounce.
 CSP_HD u32x4 draw_block(uint64_t ray, uint32_t bounce, uint32_t draw, uint32_t instance, uint64_t seed) {

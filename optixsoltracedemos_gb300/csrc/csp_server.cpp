@@ -34,6 +34,7 @@
 
 #include "csp_c_api.h"
 #include "csp_kernels.cuh"
+#include "csp_math.cuh"
 #include "csp_scene.h"
 #include "csp_system.h"
 
@@ -165,6 +166,7 @@ struct Server {
     size_t res_slot_bytes = 0;
     std::vector<int> free_res_slots;
     unsigned long long* d_counter = nullptr;
+    const float* h3t12 = nullptr;  // Halton table of the device
 
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -234,6 +236,7 @@ int Server::start(int dev, size_t budget_bytes, int max_act, uint64_t step_targe
     step_rays = std::max<uint64_t>(step_target, 1u << 20);
     int rc = cuda_status(cudaSetDevice(device), "cudaSetDevice");
     if (rc) return rc;
+    h3t12 = halton3_table();
     if ((rc = cuda_status(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate"))) return rc;
     size_t free_b = 0, total_b = 0;
     if ((rc = cuda_status(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo"))) return rc;
@@ -551,6 +554,7 @@ int Server::step_launch(std::vector<SRequest*>& finishing, uint64_t& rays) {
         d.args.instance = r->instance;
         d.args.pad = 0;
         d.args.grid = g == kAccelGrid ? reinterpret_cast<const GridDesc*>(d_arena + r->o_grid) : nullptr;
+        d.args.h3t12 = h3t12;
         const csp_element& rcv = (r->poses.empty() ? s.elements : r->poses).back();
         flux_target(rcv, nx, ny, d.flux);
         d.flux.counts = reinterpret_cast<uint32_t*>(d_arena + r->o_counts);

@@ -40,6 +40,7 @@ struct System {
     float4* d_hits = nullptr;
     uint32_t* d_ids = nullptr;
     GridDesc* d_grid = nullptr;
+    const float* h3t12 = nullptr;  // Halton table of the device (halton3_table)
     GridDesc grid_host{};  // host copy of the descriptor (source of the async upload)
     uint32_t* d_cells = nullptr;
     Aabb* d_items = nullptr;

@@ -33,6 +33,7 @@
 #pragma once
 
 #include <cfloat>
+#include <type_traits>
 
 #include "csp_kernels.cuh"
 #include "csp_math.cuh"
@@ -55,6 +56,11 @@ struct Cfg {
     static constexpr bool kFlux = kFlux_;
     // grid and BVH launches give each warp 32 rays whose sun-plane points are close together
     static constexpr bool kCoherent = kAccel_ != kAccelFlat;
+    // Philox from the precomputed key schedule: the single-scene element-list kernel only (the field
+    // kernels would lose a resident CTA to the extra registers, the batch kernel reads its
+    // arguments from shared memory)
+    static constexpr bool kSched = kAccel_ == kAccelFlat && kDense_;
+    using Args = std::conditional_t<kSched, TraceArgsK, TraceArgs>;
 };
 
 // Coherent ray order: position kk of a launch of `count` rays -> ray offset.  Rays come in blocks
@@ -210,18 +216,30 @@ __device__ __forceinline__ float halton3(uint64_t i) {
     return r;
 }
 
-// Same fold with its first six steps looked up: t6[m] = halton3(m) for m < 3^6.  For larger i the
-// reference loop continues from exactly that partial sum with the seventh digit (a zero digit adds
-// +0, which leaves the sum unchanged), so the result is identical bit for bit.
-__device__ __forceinline__ float halton3_tab(uint64_t i, const float* __restrict__ t6) {
+// Same fold with its first steps looked up: t6[m] = halton3(m) for m < 3^6 (shared memory) or
+// t12[m] = halton3(m) for m < 3^12 (global table, when present).  The partial sum of the reference
+// loop after k digits depends only on i mod 3^k and equals halton3(i mod 3^k) (a zero digit adds +0,
+// which leaves the sum unchanged); for larger i the loop continues from exactly that sum with digit
+// k + 1, so the result is identical bit for bit.
+constexpr uint32_t kH3T12Digits = 12, kH3T12 = 531441;
+__device__ __forceinline__ float halton3_tab(uint64_t i, const float* __restrict__ t6, const float* __restrict__ t12) {
     if (i >= (1ull << 32)) return halton3(i);
     uint32_t j = (uint32_t)i;
-    uint32_t q = j / kH3Tab;
-    float r = t6[j - kH3Tab * q];
-    int k = kH3TabDigits;
-    j = q;
+    float r;
+    int k;
+    if (t12) {
+        const uint32_t q = j / kH3T12;
+        r = __ldg(t12 + (j - kH3T12 * q));
+        k = kH3T12Digits;
+        j = q;
+    } else {
+        const uint32_t q = j / kH3Tab;
+        r = t6[j - kH3Tab * q];
+        k = kH3TabDigits;
+        j = q;
+    }
     while (j > 0) {
-        q = j / 3u;
+        const uint32_t q = j / 3u;
         r = r + c_halton3_f[k++] * (float)(j - 3u * q);
         j = q;
     }
@@ -599,7 +617,17 @@ __device__ __forceinline__ bool classify(const Prim& p, const Segment& g, const 
 // as the intersection program reports it, faced against the ray, ideal reflection; plus the
 // extensions (Gaussian slope and specularity error, absorption with probability 1 - reflectivity).
 // Returns false when the ray is absorbed.
-__device__ __forceinline__ bool shade_mirror(const TraceArgs& A, uint64_t ray, const Prim& p, const Optics& op,
+// C::kSched: draws use the precomputed key schedule A.keys (kernel parameters, free operands in the
+// single-scene element-list kernel); otherwise the schedule is derived from A.seed per draw.
+template <class C>
+__device__ __forceinline__ u32x4 draw(const typename C::Args& A, uint64_t ray, uint32_t bounce,
+                                      uint32_t draw_index) {
+    if constexpr (C::kSched) return draw_block_sched(ray, bounce, draw_index, A.instance, A.keys);
+    else return draw_block(ray, bounce, draw_index, A.instance, A.seed);
+}
+
+template <class C>
+__device__ __forceinline__ bool shade_mirror(const typename C::Args& A, uint64_t ray, const Prim& p, const Optics& op,
                                              const Segment& g, const Hit& h, Segment& next) {
     const int nd = g.depth + 1;
     const float3 hit = add(g.o, scale(h.t, g.d));
@@ -607,7 +635,7 @@ __device__ __forceinline__ bool shade_mirror(const TraceArgs& A, uint64_t ray, c
     float3 ffn = (dot(neg(g.d), wn) >= 0.0f) ? wn : neg(wn);
     const bool need_rng = (op.slope > 0.0f) || (op.spec > 0.0f) || !(op.reflectivity >= 1.0f);
     u32x4 ra = {0u, 0u, 0u, 0u};
-    if (need_rng) ra = draw_block(ray, (uint32_t)nd, 0, A.instance, A.seed);
+    if (need_rng) ra = draw<C>(A, ray, (uint32_t)nd, 0);
     if (op.slope > 0.0f) {
         float g1, g2;
         box_muller(u01(ra.y), u01(ra.z), g1, g2);
@@ -615,7 +643,7 @@ __device__ __forceinline__ bool shade_mirror(const TraceArgs& A, uint64_t ray, c
     }
     float3 rd = reflect(g.d, ffn);
     if (op.spec > 0.0f) {
-        const u32x4 rb = draw_block(ray, (uint32_t)nd, 1, A.instance, A.seed);
+        const u32x4 rb = draw<C>(A, ray, (uint32_t)nd, 1);
         float g1, g2;
         box_muller(u01(rb.x), u01(rb.y), g1, g2);
         rd = perturb(normalize(rd), op.spec, g1, g2);
@@ -627,10 +655,12 @@ __device__ __forceinline__ bool shade_mirror(const TraceArgs& A, uint64_t ray, c
 
 // Ray generation: cuda/sun.cu:28-38 (Halton point on the sun parallelogram) and :72-91, :106
 // (direction in the sun cone; Gaussian sun as an extension).
-__device__ __forceinline__ Segment generate(const TraceArgs& A, const SunFrame& S, uint64_t ray, const float* t6) {
-    const float hu = halton2(ray), hv = halton3_tab(ray, t6);
+template <class C>
+__device__ __forceinline__ Segment generate(const typename C::Args& A, const SunFrame& S, uint64_t ray,
+                                           const float* t6) {
+    const float hu = halton2(ray), hv = halton3_tab(ray, t6, A.h3t12);
     const float3 pos = add(add(xyz(S.v0), scale(hu, xyz(S.e1))), scale(hv, xyz(S.e2)));
-    const u32x4 r0 = draw_block(ray, 0, 0, A.instance, A.seed);
+    const u32x4 r0 = draw<C>(A, ray, 0, 0);
     const float3 w = xyz(S.w), cu = xyz(S.u), cv = xyz(S.v);
     float3 dir;
     if (S.shape == 1) {
@@ -669,7 +699,7 @@ struct CoreSmem {
 
 // Closest hit of a segment in a BVH or grid launch.
 template <class C>
-__device__ __forceinline__ int find_closest(const TraceArgs& A, const CoreSmem<C::kB>& sm, float3 o, float3 d,
+__device__ __forceinline__ int find_closest(const typename C::Args& A, const CoreSmem<C::kB>& sm, float3 o, float3 d,
                                             float tmin, float& t, uint32_t& type) {
     if constexpr (C::kAccel == kAccelGrid) return traverse_grid(sm.grid, A.prims, o, d, tmin, t, type);
     else return traverse(A.nodes, A.prims, o, d, tmin, t, type);
@@ -716,7 +746,7 @@ __device__ __forceinline__ void store_record(const TraceArgs& A, uint64_t ray, i
 }
 
 template <class C>
-__device__ __forceinline__ void emit(const TraceArgs& A, const Sink& k, uint64_t ray, int slot, float4 rec,
+__device__ __forceinline__ void emit(const typename C::Args& A, const Sink& k, uint64_t ray, int slot, float4 rec,
                                      uint32_t id) {
     if constexpr (C::kDense) store_record(A, ray, slot, rec, id);
     if constexpr (C::kFlux) flux_record(k, rec);
@@ -750,7 +780,7 @@ __device__ __forceinline__ void push(CoreSmem<kB>& sm, bool want, uint64_t ray, 
 // segment, until the ray misses, is absorbed, ends on the receiver or reaches the depth limit.
 // pending: `h` is a mirror hit whose record was already emitted (phase A), shading comes next.
 template <class C>
-__device__ void finish_path(const TraceArgs& A, const Sink& k, const CoreSmem<C::kB>& sm, uint64_t ray, Segment g,
+__device__ void finish_path(const typename C::Args& A, const Sink& k, const CoreSmem<C::kB>& sm, uint64_t ray, Segment g,
                             Hit h, bool pending) {
     for (;;) {
         if (h.best < 0) return;  // __miss__ms, cuda/materials.cu:236-253
@@ -765,7 +795,7 @@ __device__ void finish_path(const TraceArgs& A, const Sink& k, const CoreSmem<C:
         pending = false;
         const Optics op = C::kFlat ? sm.flat.optics[h.best] : A.optics[h.best];
         Segment next;
-        if (!shade_mirror(A, ray, p, op, g, h, next)) return;
+        if (!shade_mirror<C>(A, ray, p, op, g, h, next)) return;
         g = next;
         if (C::kFlat) {
             const uint32_t m = candidates(sm.flat, g.o, g.d, g.tmin);
@@ -778,7 +808,7 @@ __device__ void finish_path(const TraceArgs& A, const Sink& k, const CoreSmem<C:
 
 // Phase B: run full batches of kB queued rays (all = also the remainder).
 template <class C>
-__device__ void drain(const TraceArgs& A, const Sink& k, CoreSmem<C::kB>& sm, bool all) {
+__device__ void drain(const typename C::Args& A, const Sink& k, CoreSmem<C::kB>& sm, bool all) {
     __syncthreads();
     int qs = sm.qsize;
     while (qs >= C::kB || (all && qs > 0)) {
@@ -821,7 +851,7 @@ __device__ void drain(const TraceArgs& A, const Sink& k, CoreSmem<C::kB>& sm, bo
                 const Segment g{o, d, depth == 0 ? kTminSun : kTminBounce, depth};
                 const Hit h{(int)(w & kPrimMask), t, w >> kTypeShift};
                 const Prim p = load_prim(A.prims, (uint32_t)h.best);
-                if (shade_mirror(A, r, p, A.optics[h.best], g, h, next)) {
+                if (shade_mirror<C>(A, r, p, A.optics[h.best], g, h, next)) {
                     h2.best = find_closest<C>(A, sm, next.o, next.d, next.tmin, h2.t, h2.type);
                     if (h2.best >= 0) {
                         const Prim p2 = load_prim(A.prims, (uint32_t)h2.best);
@@ -843,7 +873,7 @@ __device__ void drain(const TraceArgs& A, const Sink& k, CoreSmem<C::kB>& sm, bo
 // Per-CTA setup of an instance: sun frame and (kFlat) the element list into shared memory.
 // Callers synchronise before the first use.
 template <class C>
-__device__ __forceinline__ void load_instance_smem(const TraceArgs& A, CoreSmem<C::kB>& sm) {
+__device__ __forceinline__ void load_instance_smem(const typename C::Args& A, CoreSmem<C::kB>& sm) {
     if (threadIdx.x < sizeof(SunFrame) / 4)
         reinterpret_cast<uint32_t*>(&sm.sun)[threadIdx.x] = reinterpret_cast<const uint32_t*>(A.sun)[threadIdx.x];
     if (C::kFlat && threadIdx.x < kFlatMax) {
@@ -867,7 +897,7 @@ __device__ __forceinline__ void load_instance_smem(const TraceArgs& A, CoreSmem<
 // Phase A of one tile (rays A.ray_begin + tile * kB ...) followed by phase B on full batches.
 // `stage` is the kDense staging area (unused otherwise).
 template <class C>
-__device__ __forceinline__ void trace_tile(const TraceArgs& A, const Sink& k, CoreSmem<C::kB>& sm,
+__device__ __forceinline__ void trace_tile(const typename C::Args& A, const Sink& k, CoreSmem<C::kB>& sm,
                                            StageSmem<C::kB>* stage, uint64_t tile) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float4* wh = nullptr;
@@ -897,7 +927,7 @@ __device__ __forceinline__ void trace_tile(const TraceArgs& A, const Sink& k, Co
     float qt = 0.f;
     uint32_t qw = 0;
     if (kk < A.count) {
-        g = generate(A, sm.sun, ray, sm.t6);
+        g = generate<C>(A, sm.sun, ray, sm.t6);
         if constexpr (C::kDense) slot[0] = make_float4(0.0f, g.o.x, g.o.y, g.o.z);
         if (C::kFlat) {
             qw = candidates(sm.flat, g.o, g.d, g.tmin);
