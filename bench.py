@@ -46,9 +46,9 @@ sys.path.insert(0, ROOT)
 METRIC = "rays/s on 1 GB300 (batched/served vs plain trace) at flux L2<=1%; p50/p99 latency"
 BYTES_PER_RAY = 80  # 5 float4 hit records per ray, fully rewritten by every trace
 # dram__bytes_read.sum + dram__bytes_write.sum of one full-size trace_kernel launch of this workload
-# (14,810,368 + 1,313,165,056 bytes), from the ncu capture summarised in
+# (34,487,552 + 1,318,957,568 bytes), from the ncu capture summarised in
 # profiles/trace_kernel_single_parabolic.md
-NCU_TRAFFIC_PER_LAUNCH = 1327975424
+NCU_TRAFFIC_PER_LAUNCH = 1353445120
 
 
 def parse():
