@@ -75,9 +75,9 @@ __global__ void __launch_bounds__(kPrepBlock) prepare_sun_batch_kernel(const Sun
     sun_frame_block(J.aabbs, J.n, make_float3(J.sx, J.sy, J.sz), J.tan_pad, J.shape, J.param, J.out, scratch);
 }
 
-template <int kB>
+template <int kB, int kAccel>
 struct BatchSmem {
-    CoreSmem<kB> core;
+    typename Cfg<kB, kAccel, false, true>::Core core;
     TraceArgs A;
     FluxTarget F;
     unsigned long long stat[4];
@@ -87,7 +87,7 @@ struct BatchSmem {
 
 // Drain the queue of the current instance and add its record counters to the instance's totals.
 template <class C>
-__device__ __forceinline__ void finish_instance(BatchSmem<C::kB>& sm, const Sink& k) {
+__device__ __forceinline__ void finish_instance(BatchSmem<C::kB, C::kAccel>& sm, const Sink& k) {
     drain<C>(sm.A, k, sm.core, true);  // ends with a barrier
     if (threadIdx.x > 0 && threadIdx.x < 4) {
         const unsigned long long v = sm.stat[threadIdx.x];
@@ -109,11 +109,12 @@ template <int kB, int kAccel>
 __global__ void __launch_bounds__(kB, batch_threads_per_sm<kAccel>() / kB) batch_kernel(const BatchLaunch L) {
     using C = Cfg<kB, kAccel, false, true>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    BatchSmem<kB>& sm = *reinterpret_cast<BatchSmem<kB>*>(smem_raw);
+    BatchSmem<kB, kAccel>& sm = *reinterpret_cast<BatchSmem<kB, kAccel>*>(smem_raw);
     for (uint32_t m = threadIdx.x; m < kH3Tab; m += kB) sm.core.t6[m] = halton3(m);
     if (threadIdx.x < 4) sm.stat[threadIdx.x] = 0;
     if (threadIdx.x == 0) {
         sm.core.qsize = 0;
+        sm.core.gsize = 0;
         sm.grab = 0;
     }
     const Sink k{&sm.F, sm.stat};
@@ -163,9 +164,9 @@ __global__ void __launch_bounds__(kB, batch_threads_per_sm<kAccel>() / kB) batch
     if (have) finish_instance<C>(sm, k);
 }
 
-template <int kB>
+template <int kB, int kAccel>
 constexpr size_t batch_smem() {
-    return sizeof(BatchSmem<kB>);
+    return sizeof(BatchSmem<kB, kAccel>);
 }
 
 template <int kB, int kAccel>
@@ -173,10 +174,10 @@ int occupancy_t() {
     static int cached = -1;
     if (cached >= 0) return cached;
     if (cudaFuncSetAttribute(batch_kernel<kB, kAccel>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)batch_smem<kB>()) != cudaSuccess)
+                             (int)batch_smem<kB, kAccel>()) != cudaSuccess)
         return 0;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<kB, kAccel>, kB, batch_smem<kB>()) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<kB, kAccel>, kB, batch_smem<kB, kAccel>()) !=
         cudaSuccess)
         return 0;
     cached = per_sm;
@@ -193,7 +194,7 @@ cudaError_t launch_t(const BatchLaunch& L, const BatchTuning& t, cudaStream_t st
     if (occ <= 0) return cudaErrorInvalidConfiguration;
     const int per_sm = std::max(1, std::min(occ, t.ctas_per_sm > 0 ? t.ctas_per_sm : occ));
     const uint64_t grid = std::min<uint64_t>(std::max<uint64_t>(L.total_tiles, 1), (uint64_t)sms * per_sm);
-    batch_kernel<kB, kAccel><<<(unsigned)grid, kB, batch_smem<kB>(), stream>>>(L);
+    batch_kernel<kB, kAccel><<<(unsigned)grid, kB, batch_smem<kB, kAccel>(), stream>>>(L);
     return cudaGetLastError();
 }
 

@@ -37,9 +37,10 @@ __global__ void __launch_bounds__(kPrepBlock) prepare_sun_kernel(const Aabb* __r
 template <int kAccel>
 using PlainCfg = Cfg<kTraceBlock, kAccel, true, false>;
 
+template <int kAccel>
 struct TraceSmem {
-    StageSmem<kTraceBlock> stage;
-    CoreSmem<kTraceBlock> core;
+    typename PlainCfg<kAccel>::Stage stage;
+    typename PlainCfg<kAccel>::Core core;
 };
 
 // Persistent kernel over the tiles of one launch (static round robin); dense records out.
@@ -47,10 +48,13 @@ template <int kAccel>
 __global__ void __launch_bounds__(kTraceBlock, 6) trace_kernel(const typename PlainCfg<kAccel>::Args A) {
     using C = PlainCfg<kAccel>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    TraceSmem& sm = *reinterpret_cast<TraceSmem*>(smem_raw);
+    TraceSmem<kAccel>& sm = *reinterpret_cast<TraceSmem<kAccel>*>(smem_raw);
     load_instance_smem<C>(A, sm.core);
     for (uint32_t m = threadIdx.x; m < kH3Tab; m += kTraceBlock) sm.core.t6[m] = halton3(m);
-    if (threadIdx.x == 0) sm.core.qsize = 0;
+    if (threadIdx.x == 0) {
+        sm.core.qsize = 0;
+        sm.core.gsize = 0;
+    }
     __syncthreads();
     const Sink none{nullptr, nullptr};
     const uint64_t tiles = (A.count + kTraceBlock - 1) / kTraceBlock;
@@ -67,19 +71,19 @@ cudaError_t launch_trace_t(const TraceArgs& args, cudaStream_t stream) {
     static bool attr_set = false;  // per process; the attribute belongs to the function
     if (e == cudaSuccess && !attr_set) {
         e = cudaFuncSetAttribute(trace_kernel<kAccel>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)sizeof(TraceSmem));
+                                 (int)sizeof(TraceSmem<kAccel>));
         attr_set = (e == cudaSuccess);
     }
     if (e == cudaSuccess)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel<kAccel>, kTraceBlock,
-                                                          sizeof(TraceSmem));
+                                                          sizeof(TraceSmem<kAccel>));
     if (e != cudaSuccess) return e;
     const uint64_t tiles = (args.count + kTraceBlock - 1) / kTraceBlock;  // CTAs that have work
     const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)std::max(1, sms * std::max(1, per_sm)));
     typename PlainCfg<kAccel>::Args a;
     static_cast<TraceArgs&>(a) = args;
     if constexpr (PlainCfg<kAccel>::kSched) philox_keys(args.seed, a.keys);
-    trace_kernel<kAccel><<<(unsigned)grid, kTraceBlock, sizeof(TraceSmem), stream>>>(a);
+    trace_kernel<kAccel><<<(unsigned)grid, kTraceBlock, sizeof(TraceSmem<kAccel>), stream>>>(a);
     return cudaGetLastError();
 }
 

@@ -46,6 +46,13 @@ constexpr float kTwoPiF = 0x1.921fb6p+2f;                  // fl32(2 pi), flux a
 constexpr int kFlatMax = 8;
 constexpr uint32_t kH3TabDigits = 6, kH3Tab = 729;
 
+template <int kB, bool kGen>
+struct CoreSmem;
+template <int kB>
+struct StageSmem;
+template <int kB>
+struct FlatStageSmem;
+
 template <int kB_, int kAccel_, bool kDense_, bool kFlux_>
 struct Cfg {
     static constexpr int kB = kB_;        // CTA size = tile size (rays)
@@ -61,6 +68,11 @@ struct Cfg {
     // arguments from shared memory)
     static constexpr bool kSched = kAccel_ == kAccelFlat && kDense_;
     using Args = std::conditional_t<kSched, TraceArgsK, TraceArgs>;
+    // element-list launches defer the direction of sun rays whose sun-plane point may reach an
+    // element box to full batches (the generation queue); the other rays provably miss
+    using Core = CoreSmem<kB_, kFlat>;
+    // phase A record staging of dense launches
+    using Stage = std::conditional_t<kFlat, FlatStageSmem<kB_>, StageSmem<kB_>>;
 };
 
 // Coherent ray order: position kk of a launch of `count` rays -> ray offset.  Rays come in blocks
@@ -655,11 +667,12 @@ __device__ __forceinline__ bool shade_mirror(const typename C::Args& A, uint64_t
 
 // Ray generation: cuda/sun.cu:28-38 (Halton point on the sun parallelogram) and :72-91, :106
 // (direction in the sun cone; Gaussian sun as an extension).
+__device__ __forceinline__ float3 sun_point(const SunFrame& S, float hu, float hv) {
+    return add(add(xyz(S.v0), scale(hu, xyz(S.e1))), scale(hv, xyz(S.e2)));
+}
+
 template <class C>
-__device__ __forceinline__ Segment generate(const typename C::Args& A, const SunFrame& S, uint64_t ray,
-                                           const float* t6) {
-    const float hu = halton2(ray), hv = halton3_tab(ray, t6, A.h3t12);
-    const float3 pos = add(add(xyz(S.v0), scale(hu, xyz(S.e1))), scale(hv, xyz(S.e2)));
+__device__ __forceinline__ float3 sun_direction(const typename C::Args& A, const SunFrame& S, uint64_t ray) {
     const u32x4 r0 = draw<C>(A, ray, 0, 0);
     const float3 w = xyz(S.w), cu = xyz(S.u), cv = xyz(S.v);
     float3 dir;
@@ -676,7 +689,59 @@ __device__ __forceinline__ Segment generate(const typename C::Args& A, const Sun
         det_sincos(phi, sp, cp);
         dir = normalize(add(scale(r, add(scale(cp, cu), scale(sp, cv))), scale(z, w)));
     }
-    return Segment{pos, dir, kTminSun, 0};
+    return dir;
+}
+
+template <class C>
+__device__ __forceinline__ Segment generate(const typename C::Args& A, const SunFrame& S, uint64_t ray,
+                                           const float* t6) {
+    const float hu = halton2(ray), hv = halton3_tab(ray, t6, A.h3t12);
+    return Segment{sun_point(S, hu, hv), sun_direction<C>(A, S, ray), kTminSun, 0};
+}
+
+// Reach rectangle of one element box: Halton coordinates (u in [x, y], v in [z, w]) outside which
+// no sun ray can meet the box.  A ray leaves the sun plane at o = v0 + u e1 + v e2 with a direction
+// at most a from the cone axis w; at depth h below the plane it has moved at most h tan a across
+// it, and every point of the box lies at depth <= H (its deepest corner).  So o projects within
+// H tan a of the box's projection; in Halton units that is the corners' range of
+// ((c - v0).e1 / |e1|^2, (c - v0).e2 / |e2|^2) widened by H tan a / |e1|, H tan a / |e2|.
+// tan a: pillbox tan(half angle); Gaussian sigma |(g1, g2)| with |(g1, g2)| <= sqrt(-2 ln 2^-24)
+// = 5.77 (the smallest uniform is 2^-24).  Margins: 1 % on tan a, 1e-4 of the scene's extent plus
+// 1 mm on the distance, 1e-5 in Halton units, far above the float rounding of the ray's origin,
+// direction and box test, so a ray outside every rectangle fails the exact box test of every
+// element.  Degenerate frames give the whole plane.
+__device__ __forceinline__ float4 reach_rect(const SunFrame& S, float4 lo, float4 hi) {
+    const float3 v0 = xyz(S.v0), e1 = xyz(S.e1), e2 = xyz(S.e2), w = xyz(S.w);
+    const float l1 = dot(e1, e1), l2 = dot(e2, e2);
+    float tan_a;
+    if (S.shape == 1) {
+        tan_a = 5.8f * S.sigma;
+    } else {
+        const float c = S.cos_theta;
+        tan_a = c > 0.2f ? sqrtf(fmaxf(0.0f, 1.0f - c * c)) / c : __int_as_float(0x7f800000);
+    }
+    tan_a = tan_a * 1.01f + 1e-6f;
+    float umin = __int_as_float(0x7f800000), umax = -umin, vmin = umin, vmax = -umin, hmax = 0.0f;
+    const Aabb b{lo, hi};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const float3 r = sub(corner(b, k), v0);
+        const float du = dot(r, e1) / l1, dv = dot(r, e2) / l2;
+        umin = fminf(umin, du);
+        umax = fmaxf(umax, du);
+        vmin = fminf(vmin, dv);
+        vmax = fmaxf(vmax, dv);
+        hmax = fmaxf(hmax, dot(r, w));
+    }
+    const float n1 = sqrtf(l1), n2 = sqrtf(l2);
+    const float rad = hmax * tan_a + 1e-4f * (length(v0) + n1 + n2 + hmax) + 1e-3f;
+    const float ru = rad / n1 + 1e-5f, rv = rad / n2 + 1e-5f;
+    float4 r = make_float4(umin - ru, umax + ru, vmin - rv, vmax + rv);
+    if (!(l1 > 0.0f && l2 > 0.0f && r.x <= r.y && r.z <= r.w)) {
+        const float inf = __int_as_float(0x7f800000);
+        r = make_float4(-inf, inf, -inf, inf);
+    }
+    return r;
 }
 
 // Queue entries of BVH/grid launches carry the depth of their pending mirror hit in the top bits of
@@ -684,22 +749,29 @@ __device__ __forceinline__ Segment generate(const typename C::Args& A, const Sun
 constexpr int kDepthShift = 56;
 constexpr uint64_t kRayMask = (1ull << kDepthShift) - 1u;
 
-// Shared memory of one CTA: the ray queue, the Halton table, the sun frame and the kFlat scene.
-template <int kB>
+// Shared memory of one CTA: the ray queue, the Halton table, the sun frame and the kFlat scene;
+// with kGen also the generation queue (sun rays waiting for their direction) and the reach
+// rectangles of the elements.
+template <int kB, bool kGen>
 struct CoreSmem {
+    static constexpr int kG = kGen ? 2 * kB : 1;
     float qo[3][2 * kB], qd[3][2 * kB], qt[2 * kB];
     uint32_t qw[2 * kB];  // kFlat: candidate mask; BVH: element | type << 28 of the pending mirror hit
     uint64_t qray[2 * kB];
+    float go[3][kG];
+    uint64_t gray[kG];
+    float4 reach[kGen ? kFlatMax : 1];
     float t6[kH3Tab];
     FlatScene flat;
     SunFrame sun;
     GridDesc grid;
     int qsize;
+    int gsize;
 };
 
 // Closest hit of a segment in a BVH or grid launch.
 template <class C>
-__device__ __forceinline__ int find_closest(const typename C::Args& A, const CoreSmem<C::kB>& sm, float3 o, float3 d,
+__device__ __forceinline__ int find_closest(const typename C::Args& A, const typename C::Core& sm, float3 o, float3 d,
                                             float tmin, float& t, uint32_t& type) {
     if constexpr (C::kAccel == kAccelGrid) return traverse_grid(sm.grid, A.prims, o, d, tmin, t, type);
     else return traverse(A.nodes, A.prims, o, d, tmin, t, type);
@@ -710,6 +782,13 @@ template <int kB>
 struct StageSmem {
     float4 hits[kB * kMaxDepth];
     uint32_t ids[kB * kMaxDepth];
+};
+
+// kFlat launches: phase A produces slot 0 of each row only (the sun-plane record); the other slots
+// are empty until phase B writes them straight to global memory.
+template <int kB>
+struct FlatStageSmem {
+    float4 rec0[kB];
 };
 
 // Where kFlux records go: the instance's flux target and the CTA's record counters.
@@ -752,9 +831,28 @@ __device__ __forceinline__ void emit(const typename C::Args& A, const Sink& k, u
     if constexpr (C::kFlux) flux_record(k, rec);
 }
 
+// warp-aggregated append of the lanes with `want` set to the generation queue; every lane of the
+// warp must call it
+template <class Core>
+__device__ __forceinline__ void push_gen(Core& sm, bool want, uint64_t ray, float3 o) {
+    const unsigned mask = __ballot_sync(0xffffffffu, want);
+    if (mask == 0u) return;
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == __ffs(mask) - 1) base = atomicAdd(&sm.gsize, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
+    if (want) {
+        const int k = base + __popc(mask & ((1u << lane) - 1u));
+        sm.go[0][k] = o.x;
+        sm.go[1][k] = o.y;
+        sm.go[2][k] = o.z;
+        sm.gray[k] = ray;
+    }
+}
+
 // warp-aggregated append of the lanes with `want` set; every lane of the warp must call it
-template <int kB>
-__device__ __forceinline__ void push(CoreSmem<kB>& sm, bool want, uint64_t ray, float3 o, float3 d, float t,
+template <class Core>
+__device__ __forceinline__ void push(Core& sm, bool want, uint64_t ray, float3 o, float3 d, float t,
                                      uint32_t w) {
     const unsigned mask = __ballot_sync(0xffffffffu, want);
     if (mask == 0u) return;
@@ -780,7 +878,7 @@ __device__ __forceinline__ void push(CoreSmem<kB>& sm, bool want, uint64_t ray, 
 // segment, until the ray misses, is absorbed, ends on the receiver or reaches the depth limit.
 // pending: `h` is a mirror hit whose record was already emitted (phase A), shading comes next.
 template <class C>
-__device__ void finish_path(const typename C::Args& A, const Sink& k, const CoreSmem<C::kB>& sm, uint64_t ray, Segment g,
+__device__ void finish_path(const typename C::Args& A, const Sink& k, const typename C::Core& sm, uint64_t ray, Segment g,
                             Hit h, bool pending) {
     for (;;) {
         if (h.best < 0) return;  // __miss__ms, cuda/materials.cu:236-253
@@ -806,12 +904,11 @@ __device__ void finish_path(const typename C::Args& A, const Sink& k, const Core
     }
 }
 
-// Phase B: run full batches of kB queued rays (all = also the remainder).
+// One batch of up to kB rays from the top of the bounce queue (qs entries): kFlat launches finish
+// their paths, BVH/grid launches advance them by one bounce.  Ends with a barrier.
 template <class C>
-__device__ void drain(const typename C::Args& A, const Sink& k, CoreSmem<C::kB>& sm, bool all) {
-    __syncthreads();
-    int qs = sm.qsize;
-    while (qs >= C::kB || (all && qs > 0)) {
+__device__ __forceinline__ void bounce_batch(const typename C::Args& A, const Sink& k, typename C::Core& sm, int qs) {
+    {
         const int n = min(qs, C::kB);
         const int base = qs - n;
         const bool have = (int)threadIdx.x < n;
@@ -862,18 +959,66 @@ __device__ void drain(const typename C::Args& A, const Sink& k, CoreSmem<C::kB>&
                     }
                 }
             }
-            push<C::kB>(sm, again, r | ((uint64_t)next.depth << kDepthShift), next.o, next.d, h2.t,
-                        (uint32_t)h2.best | (h2.type << kTypeShift));
+            push(sm, again, r | ((uint64_t)next.depth << kDepthShift), next.o, next.d, h2.t,
+                 (uint32_t)h2.best | (h2.type << kTypeShift));
         }
         __syncthreads();
-        qs = sm.qsize;
+    }
+}
+
+// One batch of up to kB rays from the top of the generation queue (gs entries, kFlat launches):
+// sun direction and box tests; the rays that meet a box go to the bounce queue with their
+// candidate mask.  The bounce queue holds fewer than kB entries on entry.  Ends with a barrier.
+template <class C>
+__device__ __forceinline__ void gen_batch(const typename C::Args& A, typename C::Core& sm, int gs) {
+    const int n = min(gs, C::kB);
+    const int base = gs - n;
+    const bool have = (int)threadIdx.x < n;
+    float3 o = f3(0.f, 0.f, 0.f), d = f3(0.f, 0.f, 1.f);
+    uint64_t ray = 0;
+    if (have) {
+        const int q = base + threadIdx.x;
+        o = f3(sm.go[0][q], sm.go[1][q], sm.go[2][q]);
+        ray = sm.gray[q];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) sm.gsize = base;
+    uint32_t m = 0;
+    if (have) {
+        d = sun_direction<C>(A, sm.sun, ray);
+        m = candidates(sm.flat, o, d, kTminSun);
+    }
+    push(sm, m != 0u, ray, o, d, 0.0f, m);
+    __syncthreads();
+}
+
+// Phase B: run full batches of queued rays (all = also the remainders).  kFlat launches keep the
+// bounce queue below kB before each generation batch, so neither queue exceeds 2 kB.
+template <class C>
+__device__ void drain(const typename C::Args& A, const Sink& k, typename C::Core& sm, bool all) {
+    __syncthreads();
+    int qs = sm.qsize;
+    if constexpr (C::kFlat) {
+        int gs = sm.gsize;
+        for (;;) {
+            if (qs >= C::kB || (all && qs > 0 && gs == 0)) bounce_batch<C>(A, k, sm, qs);
+            else if (gs >= C::kB || (all && gs > 0)) gen_batch<C>(A, sm, gs);
+            else break;
+            qs = sm.qsize;
+            gs = sm.gsize;
+        }
+    } else {
+        while (qs >= C::kB || (all && qs > 0)) {
+            bounce_batch<C>(A, k, sm, qs);
+            qs = sm.qsize;
+        }
     }
 }
 
 // Per-CTA setup of an instance: sun frame and (kFlat) the element list into shared memory.
 // Callers synchronise before the first use.
 template <class C>
-__device__ __forceinline__ void load_instance_smem(const typename C::Args& A, CoreSmem<C::kB>& sm) {
+__device__ __forceinline__ void load_instance_smem(const typename C::Args& A, typename C::Core& sm) {
     if (threadIdx.x < sizeof(SunFrame) / 4)
         reinterpret_cast<uint32_t*>(&sm.sun)[threadIdx.x] = reinterpret_cast<const uint32_t*>(A.sun)[threadIdx.x];
     if (C::kFlat && threadIdx.x < kFlatMax) {
@@ -887,6 +1032,7 @@ __device__ __forceinline__ void load_instance_smem(const typename C::Args& A, Co
             sm.flat.box[k].lo = nd.lo;
             sm.flat.box[k].hi = nd.hi;
             sm.flat.type[k] = (__float_as_uint(nd.lo.w) >> kTypeShift) & 7u;
+            sm.reach[k] = reach_rect(*A.sun, nd.lo, nd.hi);
         }
         if (k == 0) sm.flat.n = min(nprim, kFlatMax);
     }
@@ -897,14 +1043,16 @@ __device__ __forceinline__ void load_instance_smem(const typename C::Args& A, Co
 // Phase A of one tile (rays A.ray_begin + tile * kB ...) followed by phase B on full batches.
 // `stage` is the kDense staging area (unused otherwise).
 template <class C>
-__device__ __forceinline__ void trace_tile(const typename C::Args& A, const Sink& k, CoreSmem<C::kB>& sm,
-                                           StageSmem<C::kB>* stage, uint64_t tile) {
+__device__ __forceinline__ void trace_tile(const typename C::Args& A, const Sink& k, typename C::Core& sm,
+                                           typename C::Stage* stage, uint64_t tile) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float4* wh = nullptr;
     uint32_t* wi = nullptr;
     float4* slot = nullptr;
     uint32_t* id = nullptr;
-    if constexpr (C::kDense) {
+    if constexpr (C::kDense && C::kFlat) {
+        wh = stage->rec0 + warp * 32;
+    } else if constexpr (C::kDense) {
         wh = stage->hits + warp * 32 * kMaxDepth;
         wi = stage->ids + warp * 32 * kMaxDepth;
         slot = wh + lane * kMaxDepth;
@@ -914,7 +1062,7 @@ __device__ __forceinline__ void trace_tile(const typename C::Args& A, const Sink
     uint64_t pos = kk;
     if constexpr (C::kCoherent) pos = coherent_order(kk, A.count);
     const uint64_t ray = A.ray_begin + pos;
-    if constexpr (C::kDense) {
+    if constexpr (C::kDense && !C::kFlat) {
 #pragma unroll
         for (int s = 0; s < kMaxDepth; ++s) slot[s] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (A.ids) {
@@ -927,12 +1075,22 @@ __device__ __forceinline__ void trace_tile(const typename C::Args& A, const Sink
     float qt = 0.f;
     uint32_t qw = 0;
     if (kk < A.count) {
-        g = generate<C>(A, sm.sun, ray, sm.t6);
-        if constexpr (C::kDense) slot[0] = make_float4(0.0f, g.o.x, g.o.y, g.o.z);
-        if (C::kFlat) {
-            qw = candidates(sm.flat, g.o, g.d, g.tmin);
-            want = qw != 0u;
+        if constexpr (C::kFlat) {
+            // sun-plane point; the direction waits in the generation queue unless the point lies
+            // outside every reach rectangle (then the ray meets no element box)
+            const float hu = halton2(ray), hv = halton3_tab(ray, sm.t6, A.h3t12);
+            g.o = sun_point(sm.sun, hu, hv);
+            if constexpr (C::kDense) wh[lane] = make_float4(0.0f, g.o.x, g.o.y, g.o.z);
+            const int nr = sm.flat.n;
+#pragma unroll
+            for (int e = 0; e < kFlatMax; ++e) {
+                if (e >= nr) break;
+                const float4 r = sm.reach[e];
+                want |= (hu >= r.x) & (hu <= r.y) & (hv >= r.z) & (hv <= r.w);
+            }
         } else {
+            g = generate<C>(A, sm.sun, ray, sm.t6);
+            if constexpr (C::kDense) slot[0] = make_float4(0.0f, g.o.x, g.o.y, g.o.z);
             Hit h;
             h.best = find_closest<C>(A, sm, g.o, g.d, g.tmin, h.t, h.type);
             if (h.best >= 0) {
@@ -953,7 +1111,8 @@ __device__ __forceinline__ void trace_tile(const typename C::Args& A, const Sink
         }
     }
     __syncwarp();
-    push<C::kB>(sm, want, ray, g.o, g.d, qt, qw);
+    if constexpr (C::kFlat) push_gen(sm, want, ray, g.o);
+    else push(sm, want, ray, g.o, g.d, qt, qw);
     if constexpr (C::kDense && C::kCoherent) {
         // each lane writes its own ray's 80 B row
         if (kk < A.count) {
@@ -964,6 +1123,28 @@ __device__ __forceinline__ void trace_tile(const typename C::Args& A, const Sink
                 uint32_t* gi = A.ids + pos * kMaxDepth;
 #pragma unroll
                 for (int s = 0; s < kMaxDepth; ++s) gi[s] = id[s];
+            }
+        }
+    } else if constexpr (C::kDense && C::kFlat) {
+        // the warp's 32 x 80 B of records leave as 5 fully coalesced 512-byte rows: record e of the
+        // warp is slot e mod 5 of ray e / 5, the staged sun-plane record for slot 0, else empty
+        const uint64_t warp_first = tile * C::kB + (uint64_t)warp * 32;
+        if (warp_first < A.count) {
+            const uint32_t n_rec = (uint32_t)min((uint64_t)32, A.count - warp_first) * kMaxDepth;
+            float4* gh = A.hits + warp_first * kMaxDepth;
+#pragma unroll
+            for (int s = 0; s < kMaxDepth; ++s) {
+                const uint32_t e = (uint32_t)(s * 32 + lane);
+                const uint32_t r = e / kMaxDepth;
+                if (e < n_rec) gh[e] = (e == r * kMaxDepth) ? wh[r] : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            if (A.ids) {
+                uint32_t* gi = A.ids + warp_first * kMaxDepth;
+#pragma unroll
+                for (int s = 0; s < kMaxDepth; ++s) {
+                    const uint32_t e = (uint32_t)(s * 32 + lane);
+                    if (e < n_rec) gi[e] = kNoElement;
+                }
             }
         }
     } else if constexpr (C::kDense) {

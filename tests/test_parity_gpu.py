@@ -62,6 +62,34 @@ def test_gpu_matches_oracle_bit_exact(gpu, oracle32, name):
             np.testing.assert_array_equal(hits, oh.astype(np.float32))
 
 
+def _reach_edge_configs():
+    """Element-list scenes at the edges of the sun-plane reach test (rays whose sun-plane point lies
+    outside every element's reach rectangle skip their direction): wide and very wide pillbox cones
+    (the latter disables the test), a wide Gaussian sun, a collimated zenith sun (axis-parallel
+    rays: infinite slab reciprocals), and a sun 2 degrees above the horizon."""
+    wide = scenes.single_parabolic(sun_shape=0, sun_sigma=0.3)
+    very_wide = scenes.three_heliostats(sun_angle=1.45)
+    gauss = scenes.single_parabolic(sun_sigma=30e-3)
+    zenith = scenes.three_heliostats(sun_angle=0.0)
+    zenith.sun_dir = np.array([0.0, 0.0, 1.0])
+    low = scenes.three_heliostats()
+    low.sun_dir = scenes.sun_vector(2.0, 10.0)
+    return {"pillbox_0.3rad": wide, "pillbox_1.45rad": very_wide, "gaussian_30mrad": gauss,
+            "collimated_zenith": zenith, "sun_2deg": low}
+
+
+@pytest.mark.parametrize("name", list(_reach_edge_configs()))
+def test_reach_pretest_edges_bit_exact(gpu, oracle32, name):
+    sc = _reach_edge_configs()[name]
+    n = 60000
+    for seed, inst in ((3, 0), (55, 2)):
+        oh, oi = oracle32.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, count=n, seed=seed, instance=inst)
+        hits, ids = gpu_trace(sc, n, seed=seed, instance=inst)
+        np.testing.assert_array_equal(ids, oi)
+        np.testing.assert_array_equal(hits, oh.astype(np.float32))
+        assert (oh[:, 1:, 0] != 0).any()
+
+
 @pytest.mark.parametrize("accel", [native.ACCEL_BVH, native.ACCEL_GRID], ids=["bvh", "grid"])
 def test_gpu_large_field_bit_exact(gpu, oracle32, accel):
     """2000 flat heliostats, cylinder receiver, through the BVH and through the field grid: a window
