@@ -48,7 +48,7 @@ BYTES_PER_RAY = 80  # 5 float4 hit records per ray, fully rewritten by every tra
 # dram__bytes_read.sum + dram__bytes_write.sum of one full-size trace_kernel launch of this workload
 # (34,487,552 + 1,318,957,568 bytes), from the ncu capture summarised in
 # profiles/trace_kernel_single_parabolic.md
-NCU_TRAFFIC_PER_LAUNCH = 1353445120
+NCU_TRAFFIC_PER_LAUNCH = 1371278592
 
 
 def parse():

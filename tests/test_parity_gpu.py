@@ -64,17 +64,17 @@ def test_gpu_matches_oracle_bit_exact(gpu, oracle32, name):
 
 def _reach_edge_configs():
     """Element-list scenes at the edges of the sun-plane reach test (rays whose sun-plane point lies
-    outside every element's reach rectangle skip their direction): wide and very wide pillbox cones
-    (the latter disables the test), a wide Gaussian sun, a collimated zenith sun (axis-parallel
-    rays: infinite slab reciprocals), and a sun 2 degrees above the horizon."""
+    outside every element's reach rectangle skip their direction): wide pillbox cones up to the
+    largest half angle the API accepts (0.5 rad), a wide Gaussian sun, a collimated zenith sun
+    (axis-parallel rays: infinite slab reciprocals), and a sun 2 degrees above the horizon."""
     wide = scenes.single_parabolic(sun_shape=0, sun_sigma=0.3)
-    very_wide = scenes.three_heliostats(sun_angle=1.45)
+    very_wide = scenes.three_heliostats(sun_angle=0.5)
     gauss = scenes.single_parabolic(sun_sigma=30e-3)
     zenith = scenes.three_heliostats(sun_angle=0.0)
     zenith.sun_dir = np.array([0.0, 0.0, 1.0])
     low = scenes.three_heliostats()
     low.sun_dir = scenes.sun_vector(2.0, 10.0)
-    return {"pillbox_0.3rad": wide, "pillbox_1.45rad": very_wide, "gaussian_30mrad": gauss,
+    return {"pillbox_0.3rad": wide, "pillbox_0.5rad": very_wide, "gaussian_30mrad": gauss,
             "collimated_zenith": zenith, "sun_2deg": low}
 
 
