@@ -352,8 +352,11 @@ def run_ours(args):
         line["batched"] = {
             "workload": b["config"]["workload"], "rays": b["config"]["rays_total"],
             "rays_per_s_device": b["value"], "rays_per_s_wall": b["batched_wall_rays_per_s"],
+            "rays_per_s_pipelined": b["batched_pipelined_rays_per_s"],
             "plain_loop_rays_per_s": b["plain_loop"]["rays_per_s"], "speedup_vs_plain_loop": b["speedup_vs_plain_loop"],
-            "flux_counts_mismatching_plain": b["plain_loop"]["flux_counts_mismatching_batched"],
+            "speedup_vs_plain_loop_single_run": b["speedup_vs_plain_loop_single_run"],
+            "flux_counts_mismatching_plain": b["plain_loop"]["flux_counts_mismatching_batched"]
+            + b["pipelined_flux_counts_mismatching"],
             "tuning_grid": b["config"]["tuning_grid"]}
         v = measure_served(sys_args, local, world)
         line["served"] = {
@@ -393,7 +396,10 @@ def run_batched(args):
 def measure_batched(args, local, world):
     """Batched workload: one csp_batch run (host element builds, upload, device refit, sun planes,
     one persistent trace launch, flux maps back) against the plain per-scene loop through the
-    drop-in handle (per instance: new poses and sun, update, run, device flux map)."""
+    drop-in handle (per instance: new poses and sun, update, run, device flux map).  Reported three
+    ways: device time, wall time of one synchronous run, and the completion interval of pipelined
+    runs (run_async / wait: the host builds of a run overlap the device work of the previous one),
+    the headline and the `e2e` value."""
     import numpy as np
     import torch
 
@@ -424,8 +430,22 @@ def measure_batched(args, local, world):
         b.run()
         wall.append(time.perf_counter() - t0)
         dev.append(b.timing()[1])
-    clocks = clk.stop()
     batch_counts = [b.counts(i).copy() for i in range(len(suns))]
+    # pipelined: the host builds of run k + 1 overlap the device work of run k; per-run time =
+    # interval between completions
+    b.run_async()
+    piped = []
+    t_prev = None
+    for _ in range(args.steps + 1):
+        b.run_async()
+        b.wait()
+        t = time.perf_counter()
+        if t_prev is not None:
+            piped.append(t - t_prev)
+        t_prev = t
+    b.wait()
+    clocks = clk.stop()
+    piped_mismatch = sum(int(not np.array_equal(b.counts(i), batch_counts[i])) for i in range(len(suns)))
 
     # plain per-scene loop through the drop-in handle
     tr = native.Tracer(local, int(counts.max()))
@@ -461,11 +481,15 @@ def measure_batched(args, local, world):
                    "l2_policy": "per-instance scenes and flux maps; no per-ray buffers"},
         "batched_wall_rays_per_s": total / statistics.median(wall),
         "batched_wall_ms": statistics.median(wall) * 1e3,
+        "batched_pipelined_rays_per_s": total / statistics.median(piped),
+        "batched_pipelined_ms": statistics.median(piped) * 1e3,
+        "pipelined_flux_counts_mismatching": piped_mismatch,
         "first_run_s": first_s,
         "plain_loop": {"rays_per_s": plain_rays / plain_s, "instances": n_plain, "seconds": plain_s,
                        "flux_counts_mismatching_batched": mismatches},
-        "speedup_vs_plain_loop": (total / statistics.median(wall)) / (plain_rays / plain_s),
-        "e2e": {"value": total / statistics.median(wall), "unit": "rays/s",
+        "speedup_vs_plain_loop": (total / statistics.median(piped)) / (plain_rays / plain_s),
+        "speedup_vs_plain_loop_single_run": (total / statistics.median(wall)) / (plain_rays / plain_s),
+        "e2e": {"value": total / statistics.median(piped), "unit": "rays/s",
                 "h2d_bytes_per_step": int(sum(p.nbytes for p in poses)),
                 "d2h_bytes_per_step": int(len(suns) * 100 * 100 * 4)},
         "gpu_launches": 1 + 1 + 1,

@@ -214,7 +214,7 @@ CSP_API int csp_flux_target(const csp_element* receiver, uint32_t nx, uint32_t n
 typedef struct csp_batch_s* csp_batch;
 CSP_API int csp_batch_create(csp_batch* out, int device);
 CSP_API int csp_batch_destroy(csp_batch b);
-/* Flux map grid of every instance (default 100 x 100); resets the instances' results. */
+/* Flux map grid of every instance (default 100 x 100), from the next run on. */
 CSP_API int csp_batch_set_flux_grid(csp_batch b, uint32_t nx, uint32_t ny);
 CSP_API int csp_batch_add_scene(csp_batch b, const csp_element* elements, uint32_t count, uint32_t* scene_id);
 /* poses: NULL (the scene's own elements) or count elements matching the scene's surfaces. */
@@ -232,8 +232,17 @@ CSP_API int csp_batch_set_tuning(csp_batch b, int block, int ctas_per_sm, int ch
  * size leaves its scene's grid for the BVH). */
 CSP_API int csp_batch_get_tuning(csp_batch b, int group, int* block, int* ctas_per_sm, int* chunk);
 CSP_API int csp_batch_run(csp_batch b);
-/* Results of the last run: counts / flux as csp_flux_map; stats[4] = rays, mirror records,
- * receiver records, binned receiver records. */
+/* Pipelined runs.  csp_batch_run_async builds the current instances on the host and queues their
+ * device work behind the run in flight (at most two runs in flight, else CSP_ERR_STATE), so the
+ * host work of one run overlaps the device work of the previous one; csp_batch_wait completes the
+ * oldest run in flight and makes its results the current ones (CSP_ERR_STATE when none is in
+ * flight).  csp_batch_run waits for every run in flight, then runs and waits.  Instances and the
+ * flux grid may change while runs are in flight: each run keeps what its results need.  The
+ * current results stay valid until the next csp_batch_run or csp_batch_run_async. */
+CSP_API int csp_batch_run_async(csp_batch b);
+CSP_API int csp_batch_wait(csp_batch b);
+/* Results of the last completed run: counts / flux as csp_flux_map; stats[4] = rays, mirror
+ * records, receiver records, binned receiver records. */
 CSP_API int csp_batch_get_flux(csp_batch b, uint32_t index, uint32_t* counts, double dni, double* flux);
 CSP_API int csp_batch_get_stats(csp_batch b, uint32_t index, uint64_t* stats);
 /* out[16] as csp_get_sun_plane, for one instance. */

@@ -9,7 +9,9 @@
 //           (prepare_sun_batch_kernel), trace the small-scene instances and the BVH instances
 //           (one persistent batch_kernel launch each), copy flux maps, counters and sun frames back
 // The graph is captured once per batch layout (instances, element counts, ray counts, tuning) and
-// re-launched while the layout is unchanged.
+// re-launched while the layout is unchanged.  Runs are pipelined over two slots (pinned staging and
+// result buffers, graph, events): run_async builds the next run on the host while the previous one
+// executes, wait completes the oldest run in flight.
 //
 // Arena layout (one cudaMalloc, offsets 16-byte aligned):
 //   upload  [per instance: prims | optics | aabbs | prune] [descs flat | descs bvh]
@@ -57,8 +59,22 @@ Batch::~Batch() { release(); }
 
 void Batch::release() {
     if (device >= 0) cudaSetDevice(device);
-    if (graph) cudaGraphExecDestroy(graph);
-    graph = nullptr;
+    if (stream) cudaStreamSynchronize(stream);  // runs in flight read the arena and the slots
+    flight.clear();
+    cur = -1;
+    for (RunSlot& S : slot) {
+        if (S.graph) cudaGraphExecDestroy(S.graph);
+        S.graph = nullptr;
+        if (S.h_stage) cudaFreeHost(S.h_stage);
+        if (S.h_result) cudaFreeHost(S.h_result);
+        S.h_stage = S.h_result = nullptr;
+        S.stage_cap = S.result_cap = 0;
+        if (S.ev0) cudaEventDestroy(S.ev0);
+        if (S.ev1) cudaEventDestroy(S.ev1);
+        if (S.done) cudaEventDestroy(S.done);
+        S.ev0 = S.ev1 = S.done = nullptr;
+    }
+    h_stage = nullptr;
     for (BScene& s : scenes) {
         cudaFree(s.d_topo);
         cudaFree(s.d_cells);
@@ -71,10 +87,6 @@ void Batch::release() {
     cudaFree(d_arena);
     d_arena = nullptr;
     arena_cap = 0;
-    if (h_stage) cudaFreeHost(h_stage);
-    if (h_result) cudaFreeHost(h_result);
-    h_stage = h_result = nullptr;
-    stage_cap = result_cap = 0;
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (stream) cudaStreamDestroy(stream);
@@ -89,7 +101,13 @@ int Batch::ensure_stream() {
     h3t12 = halton3_table();
     if ((rc = cuda_status(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate"))) return rc;
     if ((rc = cuda_status(cudaEventCreate(&ev0), "cudaEventCreate"))) return rc;
-    return cuda_status(cudaEventCreate(&ev1), "cudaEventCreate");
+    if ((rc = cuda_status(cudaEventCreate(&ev1), "cudaEventCreate"))) return rc;
+    for (RunSlot& S : slot) {
+        if ((rc = cuda_status(cudaEventCreate(&S.ev0), "cudaEventCreate"))) return rc;
+        if ((rc = cuda_status(cudaEventCreate(&S.ev1), "cudaEventCreate"))) return rc;
+        if ((rc = cuda_status(cudaEventCreateWithFlags(&S.done, cudaEventDisableTiming), "cudaEventCreate"))) return rc;
+    }
+    return CSP_OK;
 }
 
 int Batch::add_scene(const csp_element* el, uint32_t n, uint32_t* id) {
@@ -141,7 +159,6 @@ int Batch::add_instance(const BInst& bi, uint32_t* index) {
     if (bi.rays >= (1ull << 40)) return set_error(CSP_ERR_INVALID_ARGUMENT, "too many rays for one instance");
     inst.push_back(bi);
     if (index) *index = (uint32_t)(inst.size() - 1);
-    ran = false;
     return CSP_OK;
 }
 
@@ -152,7 +169,7 @@ const csp_element* Batch::elements_of(size_t i) const {
 uint32_t Batch::count_of(size_t i) const { return (uint32_t)scenes[inst[i].scene].elements.size(); }
 
 // Offsets of every region; grows the arena and the pinned buffers when needed.
-int Batch::layout() {
+int Batch::layout(int si) {
     const size_t n = inst.size();
     place.assign(n, Place{});
     for (int g = 0; g < kBatchGroups; ++g) n_group[g] = 0;
@@ -222,9 +239,14 @@ int Batch::layout() {
     const size_t total = std::max<size_t>(off, 16);
 
     int rc;
+    RunSlot& S = slot[si];
     if (total > arena_cap) {
-        if (graph) cudaGraphExecDestroy(graph);
-        graph = nullptr;
+        // the runs in flight read the arena: let them finish (their results stay in their slots)
+        if (!flight.empty() && (rc = cuda_status(cudaStreamSynchronize(stream), "batch run"))) return rc;
+        for (RunSlot& o : slot) {
+            if (o.graph) cudaGraphExecDestroy(o.graph);
+            o.graph = nullptr;
+        }
         cudaFree(d_arena);
         d_arena = nullptr;
         arena_cap = 0;
@@ -234,27 +256,30 @@ int Batch::layout() {
         if ((rc = cuda_status(cudaMalloc((void**)&d_arena, total), "cudaMalloc batch arena"))) return rc;
         arena_cap = total;
     }
-    if (up_bytes > stage_cap) {
-        if (graph) cudaGraphExecDestroy(graph);
-        graph = nullptr;
-        if (h_stage) cudaFreeHost(h_stage);
-        h_stage = nullptr;
-        stage_cap = 0;
-        if ((rc = cuda_status(cudaHostAlloc((void**)&h_stage, up_bytes, cudaHostAllocDefault), "cudaHostAlloc staging")))
-            return rc;
-        stage_cap = up_bytes;
+    // the slot is not in flight; if it holds the current results, this run replaces them
+    if (up_bytes > S.stage_cap || res_bytes > S.result_cap) {
+        if (S.graph) cudaGraphExecDestroy(S.graph);
+        S.graph = nullptr;
+        if (si == cur) cur = -1;
     }
-    if (res_bytes > result_cap) {
-        if (graph) cudaGraphExecDestroy(graph);
-        graph = nullptr;
-        if (h_result) cudaFreeHost(h_result);
-        h_result = nullptr;
-        result_cap = 0;
-        if ((rc = cuda_status(cudaHostAlloc((void**)&h_result, std::max<size_t>(res_bytes, 16), cudaHostAllocDefault),
+    if (up_bytes > S.stage_cap) {
+        if (S.h_stage) cudaFreeHost(S.h_stage);
+        S.h_stage = nullptr;
+        S.stage_cap = 0;
+        if ((rc = cuda_status(cudaHostAlloc((void**)&S.h_stage, up_bytes, cudaHostAllocDefault), "cudaHostAlloc staging")))
+            return rc;
+        S.stage_cap = up_bytes;
+    }
+    if (res_bytes > S.result_cap) {
+        if (S.h_result) cudaFreeHost(S.h_result);
+        S.h_result = nullptr;
+        S.result_cap = 0;
+        if ((rc = cuda_status(cudaHostAlloc((void**)&S.h_result, std::max<size_t>(res_bytes, 16), cudaHostAllocDefault),
                               "cudaHostAlloc results")))
             return rc;
-        result_cap = res_bytes;
+        S.result_cap = res_bytes;
     }
+    h_stage = S.h_stage;
     return CSP_OK;
 }
 
@@ -499,11 +524,16 @@ int Batch::resolve_tuning() {
     return CSP_OK;
 }
 
-int Batch::run() {
+int Batch::run_async() {
     if (inst.empty()) return set_error(CSP_ERR_STATE, "batch has no instances");
+    if (flight.size() >= 2) return set_error(CSP_ERR_STATE, "two runs in flight: wait for one first");
     const auto t0 = std::chrono::steady_clock::now();
     int rc = ensure_stream();
     if (rc) return rc;
+    // the slot not in flight (with none in flight, the one without the current results)
+    const int si = flight.empty() ? (cur == 0 ? 1 : 0) : 1 - flight.front();
+    if (si == cur) cur = -1;  // this run's download replaces those results
+    RunSlot& S = slot[si];
 
     // host builds of the instances with their own poses, then the copies into the staging image,
     // both parallel over instances
@@ -536,7 +566,7 @@ int Batch::run() {
         return (int)CSP_OK;
     };
     if ((rc = parallel([&](size_t i, std::string& err) { return build_instance(i, err); }))) return rc;
-    if ((rc = layout())) return rc;
+    if ((rc = layout(si))) return rc;
     if ((rc = parallel([&](size_t i, std::string&) {
              fill_instance(i);
              return (int)CSP_OK;
@@ -556,8 +586,8 @@ int Batch::run() {
     for (int g = 0; g < kBatchGroups; ++g) tiles[g] = tb[g][n_group[g]];
 
     // graph signature: everything the captured launches depend on besides the staged contents
-    std::vector<uint64_t> sig = {(uint64_t)(uintptr_t)d_arena, (uint64_t)(uintptr_t)h_stage,
-                                 (uint64_t)(uintptr_t)h_result, up_bytes, zero_bytes, res_bytes, n, nx, ny,
+    std::vector<uint64_t> sig = {(uint64_t)(uintptr_t)d_arena, (uint64_t)(uintptr_t)S.h_stage,
+                                 (uint64_t)(uintptr_t)S.h_result, up_bytes, zero_bytes, res_bytes, n, nx, ny,
                                  desc_off[0], zero_off, res_off};
     for (int g = 0; g < kBatchGroups; ++g) {
         sig.push_back(tiles[g]);
@@ -566,50 +596,83 @@ int Batch::run() {
         sig.push_back((uint64_t)used[g].ctas_per_sm);
         sig.push_back((uint64_t)used[g].chunk);
     }
-    if (!graph || sig != graph_sig) {
-        if (graph) cudaGraphExecDestroy(graph);
-        graph = nullptr;
+    if (!S.graph || sig != S.graph_sig) {
+        if (S.graph) cudaGraphExecDestroy(S.graph);
+        S.graph = nullptr;
         cudaGraph_t g = nullptr;
         if ((rc = cuda_status(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture")))
             return rc;
         int crc = enqueue_prefix(stream);
-        if (!crc) crc = cuda_status(cudaEventRecordWithFlags(ev0, stream, cudaEventRecordExternal), "event");
+        if (!crc) crc = cuda_status(cudaEventRecordWithFlags(S.ev0, stream, cudaEventRecordExternal), "event");
         if (!crc) crc = enqueue_scene_setup(stream);
         for (int gi = 0; gi < kBatchGroups && !crc; ++gi)
             if (n_group[gi] > 0)
                 crc = cuda_status(launch_trace_batch(launch_of(gi, tiles[gi], used[gi].chunk), gi, used[gi], stream),
                                   "batch_kernel");
-        if (!crc) crc = cuda_status(cudaEventRecordWithFlags(ev1, stream, cudaEventRecordExternal), "event");
+        if (!crc) crc = cuda_status(cudaEventRecordWithFlags(S.ev1, stream, cudaEventRecordExternal), "event");
         if (!crc)
             crc = cuda_status(
-                cudaMemcpyAsync(h_result, d_arena + res_off, res_bytes, cudaMemcpyDeviceToHost, stream), "download");
+                cudaMemcpyAsync(S.h_result, d_arena + res_off, res_bytes, cudaMemcpyDeviceToHost, stream), "download");
         const int erc = cuda_status(cudaStreamEndCapture(stream, &g), "end capture");
         if (crc || erc) {
             if (g) cudaGraphDestroy(g);
             return crc ? crc : erc;
         }
-        rc = cuda_status(cudaGraphInstantiate(&graph, g, 0), "cudaGraphInstantiate");
+        rc = cuda_status(cudaGraphInstantiate(&S.graph, g, 0), "cudaGraphInstantiate");
         cudaGraphDestroy(g);
         if (rc) return rc;
-        graph_sig = sig;
+        S.graph_sig = sig;
     }
-    time_setup = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    if ((rc = cuda_status(cudaGraphLaunch(graph, stream), "cudaGraphLaunch"))) return rc;
-    if ((rc = cuda_status(cudaStreamSynchronize(stream), "batch run"))) return rc;
-    float ms = 0.f;
-    if ((rc = cuda_status(cudaEventElapsedTime(&ms, ev0, ev1), "batch timing"))) return rc;
-    time_trace = ms * 1e-3;
-    ran = true;
+    // what the results of this run need, whatever the instance list holds by then
+    S.place = place;
+    S.rays.resize(n);
+    S.receiver.resize(n);
+    for (size_t i = 0; i < n; ++i) {
+        S.rays[i] = inst[i].rays;
+        S.receiver[i] = elements_of(i)[count_of(i) - 1];
+    }
+    S.res_off = res_off;
+    S.nx = nx;
+    S.ny = ny;
+    S.time_setup = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if ((rc = cuda_status(cudaGraphLaunch(S.graph, stream), "cudaGraphLaunch"))) return rc;
+    if ((rc = cuda_status(cudaEventRecord(S.done, stream), "cudaEventRecord"))) return rc;
+    flight.push_back(si);
     return CSP_OK;
 }
 
+int Batch::wait() {
+    if (flight.empty()) return set_error(CSP_ERR_STATE, "no batch run in flight");
+    const int si = flight.front();
+    flight.pop_front();
+    RunSlot& S = slot[si];
+    int rc = cuda_status(cudaEventSynchronize(S.done), "batch run");
+    if (rc) return rc;
+    float ms = 0.f;
+    if ((rc = cuda_status(cudaEventElapsedTime(&ms, S.ev0, S.ev1), "batch timing"))) return rc;
+    time_trace = ms * 1e-3;
+    time_setup = S.time_setup;
+    cur = si;
+    return CSP_OK;
+}
+
+int Batch::run() {
+    while (!flight.empty()) {
+        const int rc = wait();
+        if (rc) return rc;
+    }
+    const int rc = run_async();
+    return rc ? rc : wait();
+}
+
 int Batch::result(uint32_t index, const uint32_t** counts, const unsigned long long** stats, const SunFrame** sun) const {
-    if (!ran) return set_error(CSP_ERR_STATE, "no results: run the batch first");
-    if (index >= inst.size()) return set_error(CSP_ERR_INVALID_ARGUMENT, "no such instance");
-    const Place& p = place[index];
-    if (counts) *counts = reinterpret_cast<const uint32_t*>(h_result + (p.counts - res_off));
-    if (stats) *stats = reinterpret_cast<const unsigned long long*>(h_result + (p.stats - res_off));
-    if (sun) *sun = reinterpret_cast<const SunFrame*>(h_result + (p.sun - res_off));
+    if (cur < 0) return set_error(CSP_ERR_STATE, "no results: run the batch first");
+    const RunSlot& S = slot[cur];
+    if (index >= S.place.size()) return set_error(CSP_ERR_INVALID_ARGUMENT, "no such instance");
+    const Place& p = S.place[index];
+    if (counts) *counts = reinterpret_cast<const uint32_t*>(S.h_result + (p.counts - S.res_off));
+    if (stats) *stats = reinterpret_cast<const unsigned long long*>(S.h_result + (p.stats - S.res_off));
+    if (sun) *sun = reinterpret_cast<const SunFrame*>(S.h_result + (p.sun - S.res_off));
     return CSP_OK;
 }
 
@@ -650,7 +713,6 @@ int csp_batch_set_flux_grid(csp_batch bh, uint32_t nx, uint32_t ny) {
     Batch* b = reinterpret_cast<Batch*>(bh);
     b->nx = nx;
     b->ny = ny;
-    b->ran = false;
     return CSP_OK;
 }
 
@@ -683,7 +745,6 @@ int csp_batch_clear_instances(csp_batch bh) {
     CSP_BGUARD(bh);
     Batch* b = reinterpret_cast<Batch*>(bh);
     b->inst.clear();
-    b->ran = false;
     return CSP_OK;
 }
 
@@ -719,6 +780,16 @@ int csp_batch_run(csp_batch bh) {
     return reinterpret_cast<Batch*>(bh)->run();
 }
 
+int csp_batch_run_async(csp_batch bh) {
+    CSP_BGUARD(bh);
+    return reinterpret_cast<Batch*>(bh)->run_async();
+}
+
+int csp_batch_wait(csp_batch bh) {
+    CSP_BGUARD(bh);
+    return reinterpret_cast<Batch*>(bh)->wait();
+}
+
 int csp_batch_get_flux(csp_batch bh, uint32_t index, uint32_t* counts, double dni, double* flux) {
     CSP_BGUARD(bh);
     const Batch* b = reinterpret_cast<Batch*>(bh);
@@ -726,13 +797,12 @@ int csp_batch_get_flux(csp_batch bh, uint32_t index, uint32_t* counts, double dn
     const csp::SunFrame* f = nullptr;
     int rc = b->result(index, &c, nullptr, &f);
     if (rc) return rc;
-    const size_t nb = (size_t)b->nx * b->ny;
+    const csp::RunSlot& S = b->slot[b->cur];
+    const size_t nb = (size_t)S.nx * S.ny;
     if (counts) std::memcpy(counts, c, nb * sizeof(uint32_t));
-    if (flux) {
-        const csp_element& rcv = b->elements_of(index)[b->count_of(index) - 1];
-        csp::counts_to_flux(c, nb, dni, csp::sun_plane_area(*f), b->inst[index].rays,
-                            csp::flux_bin_area(rcv, b->nx, b->ny), flux);
-    }
+    if (flux)
+        csp::counts_to_flux(c, nb, dni, csp::sun_plane_area(*f), S.rays[index],
+                            csp::flux_bin_area(S.receiver[index], S.nx, S.ny), flux);
     return CSP_OK;
 }
 
@@ -743,7 +813,7 @@ int csp_batch_get_stats(csp_batch bh, uint32_t index, uint64_t* stats) {
     const unsigned long long* s = nullptr;
     int rc = b->result(index, nullptr, &s, nullptr);
     if (rc) return rc;
-    stats[0] = b->inst[index].rays;
+    stats[0] = b->slot[b->cur].rays[index];
     for (int k = 1; k < 4; ++k) stats[k] = s[k];
     return CSP_OK;
 }

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <deque>
 #include <string>
 #include <vector>
 
@@ -48,10 +49,29 @@ struct Place {
     int slot = 0;   // index within the group
 };
 
+// One run of the pipeline: its pinned buffers and graph, and what its results need (the layout and
+// inputs of its instances), so the instance list can change while the run is in flight.  The host
+// builds run k + 1 into one slot while run k executes from the other.
+struct RunSlot {
+    unsigned char* h_stage = nullptr;  // pinned image of the upload region
+    size_t stage_cap = 0;
+    unsigned char* h_result = nullptr;  // pinned copy of the download region
+    size_t result_cap = 0;
+    cudaGraphExec_t graph = nullptr;
+    std::vector<uint64_t> graph_sig;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, done = nullptr;
+    std::vector<Place> place;
+    std::vector<uint64_t> rays;
+    std::vector<csp_element> receiver;
+    size_t res_off = 0;
+    uint32_t nx = 0, ny = 0;
+    double time_setup = 0.0;
+};
+
 struct Batch {
     int device = -1;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // autotuner timing
     const float* h3t12 = nullptr;  // Halton table of the device
     uint32_t nx = 100, ny = 100;
     std::vector<BScene> scenes;
@@ -61,10 +81,10 @@ struct Batch {
 
     unsigned char* d_arena = nullptr;
     size_t arena_cap = 0;
-    unsigned char* h_stage = nullptr;  // pinned image of the upload region
-    size_t stage_cap = 0;
-    unsigned char* h_result = nullptr;  // pinned copy of the download region
-    size_t result_cap = 0;
+    RunSlot slot[2];
+    std::deque<int> flight;            // slots of the runs in flight, oldest first
+    int cur = -1;                      // slot of the last completed run (its results), -1: none
+    unsigned char* h_stage = nullptr;  // staging image of the run being built
 
     std::vector<Place> place;
     size_t up_bytes = 0, zero_off = 0, zero_bytes = 0, res_off = 0, res_bytes = 0;
@@ -73,10 +93,7 @@ struct Batch {
     std::vector<InstBuild> builds;  // per instance, during a run (instances with poses)
     int max_nodes = 0;
 
-    cudaGraphExec_t graph = nullptr;
-    std::vector<uint64_t> graph_sig;
-    bool ran = false;
-    double time_setup = 0.0, time_trace = 0.0;
+    double time_setup = 0.0, time_trace = 0.0;  // of the last completed run
 
     ~Batch();
     void release();
@@ -85,7 +102,7 @@ struct Batch {
     int add_instance(const BInst& bi, uint32_t* index);
     const csp_element* elements_of(size_t i) const;
     uint32_t count_of(size_t i) const;
-    int layout();
+    int layout(int s);
     int build_instance(size_t i, std::string& err);
     const HostScene& scene_of(size_t i) const;
     const HostGrid& grid_of(size_t i) const;
@@ -97,6 +114,8 @@ struct Batch {
     int enqueue_scene_setup(cudaStream_t st);
     int autotune(int g, BatchTuning& best);
     int resolve_tuning();
+    int run_async();
+    int wait();
     int run();
     int result(uint32_t index, const uint32_t** counts, const unsigned long long** stats, const SunFrame** sun) const;
 };

@@ -82,6 +82,8 @@ SIGNATURES = {
     "csp_batch_get_tuning": (ctypes.c_int, [_H, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                             ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "csp_batch_run": (ctypes.c_int, [_H]),
+    "csp_batch_run_async": (ctypes.c_int, [_H]),
+    "csp_batch_wait": (ctypes.c_int, [_H]),
     "csp_batch_get_flux": (ctypes.c_int, [_H, ctypes.c_uint32, _P, ctypes.c_double, _P]),
     "csp_batch_get_stats": (ctypes.c_int, [_H, ctypes.c_uint32, _P]),
     "csp_batch_get_sun_plane": (ctypes.c_int, [_H, ctypes.c_uint32, _P]),
@@ -330,6 +332,14 @@ class Batch:
 
     def run(self):
         _check(self.lib.csp_batch_run(self.h))
+
+    def run_async(self):
+        """Build the current instances and queue their run behind the one in flight (at most two)."""
+        _check(self.lib.csp_batch_run_async(self.h))
+
+    def wait(self):
+        """Complete the oldest run in flight; its results become the current ones."""
+        _check(self.lib.csp_batch_wait(self.h))
 
     def counts(self, index: int) -> np.ndarray:
         out = np.zeros((self.nx, self.ny), np.uint32)

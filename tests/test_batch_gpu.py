@@ -5,7 +5,8 @@
   * every instance of a batch (one persistent launch, flux binned in the shading stage, per-instance
     BVH refit on the device) equals a plain single-scene run of the same scene, sun, rays, seed and
     instance id, count for count, whatever the launch parameters;
-  * re-running a batch (CUDA graph replay) reproduces it, and a changed layout re-captures.
+  * re-running a batch (CUDA graph replay) reproduces it, and a changed layout re-captures;
+  * pipelined runs (run_async / wait, two in flight) give each run its own instances' results.
 """
 import numpy as np
 import pytest
@@ -177,6 +178,48 @@ def test_batch_rerun_and_relayout(gpu):
         b.run()
         counts, _, _ = _plain_counts(native, th.elements, th.sun_dir, th.sun_shape, th.sun_param, 400000, 4, 2)
         np.testing.assert_array_equal(b.counts(0), counts)
+    finally:
+        b.close()
+
+
+def test_batch_pipelined_runs(gpu):
+    """run_async / wait: two runs in flight with different instance sets (the second built while
+    the first executes) give each set's own results, equal to synchronous runs; a third run_async
+    and a wait with nothing in flight are refused; results survive a change of the instance list."""
+    from optixsoltracedemos_gb300 import native
+    b, jobs, scene_el = _mixed_batch(native)
+    th = scenes.three_heliostats()
+    try:
+        b.run()
+        ref_a = [b.counts(i).copy() for i in range(len(jobs))]
+        ref_a_stats = [b.stats(i).copy() for i in range(len(jobs))]
+        counts_b, _, _ = _plain_counts(native, th.elements, th.sun_dir, th.sun_shape, th.sun_param, 400000, 4, 2)
+        for _ in range(2):
+            b.run_async()  # set A
+            b.clear_instances()
+            b.add_instance(0, th.sun_dir, th.sun_shape, th.sun_param, 400000, seed=4, instance=2)
+            b.run_async()  # set B, built while A runs
+            with pytest.raises(native.CspError):
+                b.run_async()
+            b.wait()
+            assert len(b) == 1
+            for i in range(len(jobs)):
+                np.testing.assert_array_equal(b.counts(i), ref_a[i])
+                np.testing.assert_array_equal(b.stats(i), ref_a_stats[i])
+            b.wait()
+            np.testing.assert_array_equal(b.counts(0), counts_b)
+            with pytest.raises(native.CspError):
+                b.counts(1)  # set B has one instance
+            with pytest.raises(native.CspError):
+                b.wait()
+            b.clear_instances()
+            for j in jobs:
+                b.add_instance(j[0], j[2], j[3], j[4], j[5], seed=j[6], instance=j[7], poses=j[1])
+        # synchronous run after pipelined ones, and a run_async left in flight at close
+        b.run()
+        for i in range(len(jobs)):
+            np.testing.assert_array_equal(b.counts(i), ref_a[i])
+        b.run_async()
     finally:
         b.close()
 
