@@ -428,13 +428,13 @@ __device__ __forceinline__ int traverse(const Node* __restrict__ nodes, const Pr
     return best;
 }
 
-// Exact-AABB culling and intersection program of one grid candidate (a BVH leaf's work): `it` is
-// the element's exact AABB with lo.w = element | type << 28.
-__device__ __forceinline__ void test_item(const Aabb* __restrict__ it, const Prim* __restrict__ prims, float3 o,
-                                          float3 d, float3 inv, float tmin, int& best, float& best_t,
-                                          uint32_t& best_type, float& prune) {
-    const float4* q = reinterpret_cast<const float4*>(it);
-    const float4 lo = __ldg(q), hi = __ldg(q + 1);
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
+// Exact-AABB culling and intersection program of one grid candidate (a BVH leaf's work): the
+// element's exact AABB lo, hi with lo.w = element | type << 28.
+__device__ __forceinline__ void test_box(float4 lo, float4 hi, const Prim* __restrict__ prims, float3 o, float3 d,
+                                         float3 inv, float tmin, int& best, float& best_t, uint32_t& best_type,
+                                         float& prune) {
     const float t0x = (lo.x - o.x) * inv.x, t1x = (hi.x - o.x) * inv.x;
     const float t0y = (lo.y - o.y) * inv.y, t1y = (hi.y - o.y) * inv.y;
     const float t0z = (lo.z - o.z) * inv.z, t1z = (hi.z - o.z) * inv.z;
@@ -451,6 +451,14 @@ __device__ __forceinline__ void test_item(const Aabb* __restrict__ it, const Pri
         best_type = type;
         prune = fminf(kTmax, best_t + best_t * 1e-3f + 1e-3f);
     }
+}
+
+// The same for the candidate stored at `it`.
+__device__ __forceinline__ void test_item(const Aabb* __restrict__ it, const Prim* __restrict__ prims, float3 o,
+                                          float3 d, float3 inv, float tmin, int& best, float& best_t,
+                                          uint32_t& best_type, float& prune) {
+    const float4* q = reinterpret_cast<const float4*>(it);
+    test_box(__ldg(q), __ldg(q + 1), prims, o, d, inv, tmin, best, best_t, best_type, prune);
 }
 
 // Restrict [ta, tb] to the parameters where coordinate o + t d lies in [lo, hi] (an empty range
@@ -490,34 +498,37 @@ __device__ __forceinline__ int traverse_grid(const GridDesc& G, const Prim* __re
     int iy = (int)fminf(fmaxf(floorf((py - G.y0) * G.inv_cell), 0.0f), (float)(G.ny - 1));
     const int sx = d.x > 0.0f ? 1 : -1, sy = d.y > 0.0f ? 1 : -1;
     const float inf = __int_as_float(0x7f800000);
-    float tc = ta;
-    // candidate lists in order: the global elements, then the cells of the walk (one test site)
+    // candidate lists in order: the global elements, then the cells of the walk (one test site).
+    // (ix, iy) is the next cell of the walk, entered at ctc: it does not depend on the tests, so its
+    // item range is prefetched into L1 before the current list is tested; it is entered only if
+    // ctc lies within the segment and the pruning distance the tests leave.
     const Aabb* list = G.global;
     uint32_t j = 0, e = (uint32_t)G.n_global;
-    int step = -1;
+    bool next = walk;
+    float ctc = ta;
+    if (next) prefetch_l1(G.cell_start + (iy * G.nx + ix));
+    int step = 0;
     for (;;) {
         for (; j < e; ++j) test_item(list + j, prims, o, d, inv, tmin, best, best_t, best_type, prune);
-        if (step >= 0) {
-            // next cell: parameters of the next x and y cell boundaries, from the cell index
-            const float tnx = (d.x != 0.0f) ? (G.x0 + (float)(ix + (sx > 0)) * G.cell - o.x) * inv.x : inf;
-            const float tny = (d.y != 0.0f) ? (G.y0 + (float)(iy + (sy > 0)) * G.cell - o.y) * inv.y : inf;
-            if (tnx < tny) {
-                tc = fmaxf(tc, tnx);
-                ix += sx;
-                if (ix < 0 || ix >= G.nx) break;
-            } else {
-                tc = fmaxf(tc, tny);
-                iy += sy;
-                if (iy < 0 || iy >= G.ny) break;
-            }
-        } else if (!walk) {
-            break;
-        }
-        if (tc > tb || tc > prune || ++step > G.nx + G.ny) break;
+        if (!next || ctc > tb || ctc > prune || step > G.nx + G.ny) break;
         const int c = iy * G.nx + ix;
         list = G.items;
         j = __ldg(G.cell_start + c);
         e = __ldg(G.cell_start + c + 1);
+        ++step;
+        // the cell after it: parameters of the next x and y cell boundaries, from the cell index
+        const float tnx = (d.x != 0.0f) ? (G.x0 + (float)(ix + (sx > 0)) * G.cell - o.x) * inv.x : inf;
+        const float tny = (d.y != 0.0f) ? (G.y0 + (float)(iy + (sy > 0)) * G.cell - o.y) * inv.y : inf;
+        if (tnx < tny) {
+            ctc = fmaxf(ctc, tnx);
+            ix += sx;
+            next = ix >= 0 && ix < G.nx;
+        } else {
+            ctc = fmaxf(ctc, tny);
+            iy += sy;
+            next = iy >= 0 && iy < G.ny;
+        }
+        if (next) prefetch_l1(G.cell_start + (iy * G.nx + ix));
     }
     return best;
 }
