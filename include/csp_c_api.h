@@ -182,6 +182,14 @@ CSP_API int csp_read_stinput(csp_handle h, const char* path, int flags);
 CSP_API int csp_write_hits_csv(const float* hits, uint64_t num_rays, const char* path);
 /* Copy the hit buffer to the host and write it as CSV (write_output). */
 CSP_API int csp_write_output(csp_handle h, const char* path);
+/* Staged results (SolTrace's stage order: the receiver sees only light from the mirrors): rays
+ * whose first interaction is the receiver -- straight from the sun -- are left out.  The CSV then
+ * equals the reference's file after scripts/post_processing/clean_direct_sun.py:6-18 (rows of
+ * those rays dropped, the other rays keep their numbers); flux maps and batch flux maps do not
+ * count their receiver records. */
+#define CSP_OUT_STAGED 1
+CSP_API int csp_write_hits_csv_ex(const float* hits, uint64_t num_rays, const char* path, int flags);
+CSP_API int csp_write_output_ex(csp_handle h, const char* path, int flags);
 /* out[16]: sun vector (3), v0 (3), v1 (3), v2 (3), v3 (3), plane distance (1). */
 CSP_API int csp_get_sun_plane(csp_handle h, float* out);
 
@@ -193,6 +201,9 @@ CSP_API int csp_get_sun_plane(csp_handle h, float* out);
  * [i * ny + j].  counts (may be NULL) receives hit counts; flux (may be NULL) receives W/m^2 =
  * counts * dni * sun-plane area / rays / bin area. */
 CSP_API int csp_flux_map(csp_handle h, uint32_t nx, uint32_t ny, uint32_t* counts, double dni, double* flux);
+/* The same with flags (CSP_OUT_STAGED). */
+CSP_API int csp_flux_map_ex(csp_handle h, uint32_t nx, uint32_t ny, int flags, uint32_t* counts, double dni,
+                            double* flux);
 /* Host-only (no GPU): the float binning parameters the device uses for a receiver element.
  * out[20]: origin (3), local x, y, z axes (9), hx, hy, kx, ky, keep, kind (0 flat, 1 cylinder),
  * bin area (m^2), 0.  A record at p lands in bx = floor((lx + hx) kx) (flat) or
@@ -216,6 +227,8 @@ CSP_API int csp_batch_create(csp_batch* out, int device);
 CSP_API int csp_batch_destroy(csp_batch b);
 /* Flux map grid of every instance (default 100 x 100), from the next run on. */
 CSP_API int csp_batch_set_flux_grid(csp_batch b, uint32_t nx, uint32_t ny);
+/* Output flags of the instances' flux maps (CSP_OUT_STAGED or 0, default 0), from the next run on. */
+CSP_API int csp_batch_set_output(csp_batch b, int flags);
 CSP_API int csp_batch_add_scene(csp_batch b, const csp_element* elements, uint32_t count, uint32_t* scene_id);
 /* poses: NULL (the scene's own elements) or count elements matching the scene's surfaces. */
 CSP_API int csp_batch_add_instance(csp_batch b, uint32_t scene_id, const csp_element* poses, const double* sun_dir,

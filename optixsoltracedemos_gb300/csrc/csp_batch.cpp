@@ -384,6 +384,7 @@ void Batch::fill_descs(const int* block, double sample, std::vector<InstanceDesc
                                                             offsetof(InstanceDesc, grid));
         }
         flux_target(elements_of(i)[count_of(i) - 1], nx, ny, d.flux);
+        d.flux.staged = (out_flags & CSP_OUT_STAGED) ? 1 : 0;
         d.flux.counts = reinterpret_cast<uint32_t*>(d_arena + p.counts);
         d.flux.stats = reinterpret_cast<unsigned long long*>(d_arena + p.stats);
         d.tile_begin = tiles[g];
@@ -713,6 +714,13 @@ int csp_batch_set_flux_grid(csp_batch bh, uint32_t nx, uint32_t ny) {
     Batch* b = reinterpret_cast<Batch*>(bh);
     b->nx = nx;
     b->ny = ny;
+    return CSP_OK;
+}
+
+int csp_batch_set_output(csp_batch bh, int flags) {
+    CSP_BGUARD(bh);
+    if (flags & ~CSP_OUT_STAGED) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "unknown output flags");
+    reinterpret_cast<Batch*>(bh)->out_flags = flags;
     return CSP_OK;
 }
 

@@ -74,6 +74,7 @@ struct Batch {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // autotuner timing
     const float* h3t12 = nullptr;  // Halton table of the device
     uint32_t nx = 100, ny = 100;
+    int out_flags = 0;  // CSP_OUT_* of the instances' flux maps
     std::vector<BScene> scenes;
     std::vector<BInst> inst;
     BatchTuning user{0, 0, 0};  // block 0: autotune

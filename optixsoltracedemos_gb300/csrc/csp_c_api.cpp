@@ -304,7 +304,7 @@ void counts_to_flux(const uint32_t* counts, size_t n, double dni, double sun_are
     for (size_t i = 0; i < n; ++i) flux[i] = counts[i] * per;
 }
 
-int System::flux_map(uint32_t nx, uint32_t ny, uint32_t* counts, double dni, double* flux) {
+int System::flux_map(uint32_t nx, uint32_t ny, uint32_t* counts, double dni, double* flux, bool staged) {
     if (!initialized || !d_hits) return fail(CSP_ERR_STATE, "flux map before initialize()/run()");
     if (nx == 0 || ny == 0 || (uint64_t)nx * ny > (1u << 26)) return fail(CSP_ERR_INVALID_ARGUMENT, "bad flux grid");
     const size_t nb = (size_t)nx * ny;
@@ -322,6 +322,7 @@ int System::flux_map(uint32_t nx, uint32_t ny, uint32_t* counts, double dni, dou
     flux_target(elements.back(), nx, ny, F);
     F.counts = d_flux;
     F.stats = d_fstats;
+    F.staged = staged ? 1 : 0;
     if ((rc = cuda_status(cudaMemsetAsync(d_flux, 0, nb * sizeof(uint32_t), stream), "memset flux"))) return rc;
     if ((rc = cuda_status(cudaMemsetAsync(d_fstats, 0, 4 * sizeof(unsigned long long), stream), "memset"))) return rc;
     if ((rc = cuda_status(launch_flux_records(d_hits, num_rays * kMaxDepth, F, stream), "flux_records_kernel")))
@@ -556,6 +557,12 @@ int csp_element_frame(const csp_element* e, double* euler, double* g2l, double* 
 int csp_flux_map(csp_handle h, uint32_t nx, uint32_t ny, uint32_t* counts, double dni, double* flux) {
     CSP_GUARD(h);
     return reinterpret_cast<System*>(h)->flux_map(nx, ny, counts, dni, flux);
+}
+
+int csp_flux_map_ex(csp_handle h, uint32_t nx, uint32_t ny, int flags, uint32_t* counts, double dni, double* flux) {
+    CSP_GUARD(h);
+    if (flags & ~CSP_OUT_STAGED) return fail(CSP_ERR_INVALID_ARGUMENT, "unknown output flags");
+    return reinterpret_cast<System*>(h)->flux_map(nx, ny, counts, dni, flux, (flags & CSP_OUT_STAGED) != 0);
 }
 
 int csp_flux_target(const csp_element* rcv, uint32_t nx, uint32_t ny, float* out) {

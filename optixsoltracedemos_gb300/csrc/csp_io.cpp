@@ -18,6 +18,8 @@
 //   a marker that ends the current ray, rays are numbered from 1 in order, values printed as the
 //   C++ stream prints floats (6 significant digits, %g style).  Blocks of rays are formatted in
 //   parallel threads starting from the writer state of their first ray, then written in order.
+//   CSP_OUT_STAGED leaves out the rows of rays that reach the receiver straight from the sun, as
+//   scripts/post_processing/clean_direct_sun.py does to the written file.
 #include <algorithm>
 #include <charconv>
 #include <cmath>
@@ -266,7 +268,14 @@ inline void put_u64(std::string& out, uint64_t v) {
     out.append(buf, res.ptr);
 }
 
-void format(const float* hits, uint64_t b, uint64_t e, WriterState st, std::string& out) {
+// A ray whose first interaction is the receiver (a stage-2 record in slot 1): light straight from
+// the sun, which a staged SolTrace run never records (scripts/post_processing/clean_direct_sun.py:
+// 6-18 drops the rows of every ray number with a stage-2 row and no stage-1 row; a ray's rows are
+// its stage-0 sun point, its mirror interactions, then at most one receiver record, so that is a
+// stage-2 record in slot 1).
+inline bool direct_sun(const float* hits, uint64_t ray) { return hits[4 * (ray * kMaxDepth + 1)] == 2.0f; }
+
+void format(const float* hits, uint64_t b, uint64_t e, WriterState st, bool staged, std::string& out) {
     out.clear();
     out.reserve((e - b) * 64);
     for (uint64_t k = b * kMaxDepth; k < e * kMaxDepth; ++k) {
@@ -282,6 +291,11 @@ void format(const float* hits, uint64_t b, uint64_t e, WriterState st, std::stri
             st.current++;
             st.stage = 0;
         }
+        if (staged && direct_sun(hits, k / kMaxDepth)) {
+            // the rows are dropped, the ray keeps its number (the state advances as if written)
+            st.stage++;
+            continue;
+        }
         put_u64(out, st.current);
         for (int c = 0; c < 4; ++c) {
             out.push_back(',');
@@ -294,7 +308,7 @@ void format(const float* hits, uint64_t b, uint64_t e, WriterState st, std::stri
 
 }  // namespace
 
-int write_hits_csv(const float* hits, uint64_t n, const char* path, std::string& err) {
+int write_hits_csv(const float* hits, uint64_t n, const char* path, bool staged, std::string& err) {
     FILE* fp = std::fopen(path, "wb");
     if (!fp) {
         err = std::string("could not open ") + path + " for writing";
@@ -317,7 +331,7 @@ int write_hits_csv(const float* hits, uint64_t n, const char* path, std::string&
         }
         std::vector<std::thread> th;
         for (unsigned t = 0; t < nt; ++t)
-            if (bb[t] < ee[t]) th.emplace_back(format, hits, bb[t], ee[t], starts[t], std::ref(bufs[t]));
+            if (bb[t] < ee[t]) th.emplace_back(format, hits, bb[t], ee[t], starts[t], staged, std::ref(bufs[t]));
         for (auto& x : th) x.join();
         for (unsigned t = 0; t < nt; ++t)
             if (bb[t] < ee[t] && std::fwrite(bufs[t].data(), 1, bufs[t].size(), fp) != bufs[t].size()) {
@@ -386,14 +400,21 @@ int csp_read_stinput(csp_handle h, const char* path, int flags) {
     return CSP_OK;
 }
 
-int csp_write_hits_csv(const float* hits, uint64_t num_rays, const char* path) {
+int csp_write_hits_csv_ex(const float* hits, uint64_t num_rays, const char* path, int flags) {
     if (!path || (!hits && num_rays)) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "null argument");
+    if (flags & ~CSP_OUT_STAGED) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "unknown output flags");
     std::string err;
-    const int rc = csp::write_hits_csv(hits, num_rays, path, err);
+    const int rc = csp::write_hits_csv(hits, num_rays, path, (flags & CSP_OUT_STAGED) != 0, err);
     return rc ? csp::set_error(rc, err) : CSP_OK;
 }
 
-int csp_write_output(csp_handle h, const char* path) {
+int csp_write_hits_csv(const float* hits, uint64_t num_rays, const char* path) {
+    return csp_write_hits_csv_ex(hits, num_rays, path, 0);
+}
+
+int csp_write_output(csp_handle h, const char* path) { return csp_write_output_ex(h, path, 0); }
+
+int csp_write_output_ex(csp_handle h, const char* path, int flags) {
     if (!h) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "null handle");
     csp::System* s = reinterpret_cast<csp::System*>(h);
     if (!s->initialized) return csp::set_error(CSP_ERR_STATE, "write_output before initialize()");
@@ -405,7 +426,7 @@ int csp_write_output(csp_handle h, const char* path) {
     }
     int rc = csp_copy_hits(h, host.data(), nullptr, 0, s->num_rays);
     if (rc) return rc;
-    return csp_write_hits_csv(host.data(), s->num_rays, path);
+    return csp_write_hits_csv_ex(host.data(), s->num_rays, path, flags);
 }
 
 }  // extern "C"

@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(kFluxBlock) flux_records_kernel(const float4* 
     for (uint64_t i = blockIdx.x * (uint64_t)kFluxBlock + threadIdx.x; i < n_records;
          i += (uint64_t)gridDim.x * kFluxBlock) {
         const float4 r = __ldg(hits + i);
-        if (r.x == 1.0f || r.x == 2.0f) flux_record(k, r);
+        if (r.x == 1.0f || r.x == 2.0f) flux_record(k, r, (int)(i % kMaxDepth));
     }
     __syncthreads();
     if (threadIdx.x < 4 && threadIdx.x > 0 && stat[threadIdx.x]) atomicAdd(F.stats + threadIdx.x, stat[threadIdx.x]);

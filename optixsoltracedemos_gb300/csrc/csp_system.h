@@ -74,7 +74,7 @@ struct System {
     int trace_async(cudaStream_t st);
     int run();
     int run_to_host(float* dst, uint32_t* ids);
-    int flux_map(uint32_t nx, uint32_t ny, uint32_t* counts, double dni, double* flux);
+    int flux_map(uint32_t nx, uint32_t ny, uint32_t* counts, double dni, double* flux, bool staged = false);
 };
 
 // |(v1 - v0) x (v3 - v0)| of a sun frame, in double

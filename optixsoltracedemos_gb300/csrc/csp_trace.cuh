@@ -816,11 +816,12 @@ __device__ __forceinline__ void warp_count(unsigned long long* s) {
 
 // Out of line: one copy serves every emit site (the phase A and phase B paths), which keeps the
 // flux kernels' instruction footprint close to the dense ones'.
-__device__ __noinline__ void flux_record(const Sink& k, float4 rec) {
+__device__ __noinline__ void flux_record(const Sink& k, float4 rec, int slot) {
     if (rec.x == 1.0f) {
         warp_count(k.stat + 1);
         return;
     }
+    if (slot == 1 && k.F->staged) return;  // direct sun on the receiver: not a staged result
     warp_count(k.stat + 2);
     const int b = flux_bin(*k.F, make_float3(rec.y, rec.z, rec.w));
     if (b >= 0) {
@@ -839,7 +840,7 @@ template <class C>
 __device__ __forceinline__ void emit(const typename C::Args& A, const Sink& k, uint64_t ray, int slot, float4 rec,
                                      uint32_t id) {
     if constexpr (C::kDense) store_record(A, ray, slot, rec, id);
-    if constexpr (C::kFlux) flux_record(k, rec);
+    if constexpr (C::kFlux) flux_record(k, rec, slot);
 }
 
 // warp-aggregated append of the lanes with `want` set to the generation queue; every lane of the
@@ -1114,7 +1115,7 @@ __device__ __forceinline__ void trace_tile(const typename C::Args& A, const Sink
                         slot[s] = rec;
                         if (A.ids) id[s] = (uint32_t)h.best;
                     }
-                    if constexpr (C::kFlux) flux_record(k, rec);
+                    if constexpr (C::kFlux) flux_record(k, rec, s);
                 }
                 qt = h.t;
                 qw = (uint32_t)h.best | (h.type << kTypeShift);

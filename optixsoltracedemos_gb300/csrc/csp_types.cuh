@@ -104,6 +104,10 @@ struct alignas(16) FluxTarget {
     int kind, nx, ny;
     uint32_t* counts;           // [nx * ny]
     unsigned long long* stats;  // [4]: rays, mirror records, receiver records, binned records
+    // staged results (SolTrace's stage order: the receiver only sees light from the mirrors): a
+    // receiver record in slot 1, i.e. straight from the sun, is dropped with its ray
+    // (scripts/post_processing/clean_direct_sun.py:6-18)
+    int staged;
 };
 
 // Halton base-3 digit weights: f_k = fl(f_{k-1} / 3), f_0 = 1 (the float sequence cuda/sun.cu:19

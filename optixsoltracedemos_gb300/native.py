@@ -60,6 +60,8 @@ SIGNATURES = {
     "csp_read_stinput": (ctypes.c_int, [_H, ctypes.c_char_p, ctypes.c_int]),
     "csp_write_hits_csv": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.c_char_p]),
     "csp_write_output": (ctypes.c_int, [_H, ctypes.c_char_p]),
+    "csp_write_hits_csv_ex": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.c_char_p, ctypes.c_int]),
+    "csp_write_output_ex": (ctypes.c_int, [_H, ctypes.c_char_p, ctypes.c_int]),
     "csp_element_frame": (ctypes.c_int, [_P, _P, _P, _P, _P]),
     "csp_trace_into": (ctypes.c_int, [_H, _P, _P, ctypes.c_uint64, ctypes.c_uint64, _P]),
     "csp_trace_noalloc": (ctypes.c_int, [ctypes.c_int, _P, ctypes.c_uint32, _P, ctypes.c_int, ctypes.c_double,
@@ -68,6 +70,8 @@ SIGNATURES = {
     "csp_set_accel": (ctypes.c_int, [_H, ctypes.c_int]),
     "csp_get_accel": (ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_int)]),
     "csp_flux_map": (ctypes.c_int, [_H, ctypes.c_uint32, ctypes.c_uint32, _P, ctypes.c_double, _P]),
+    "csp_flux_map_ex": (ctypes.c_int, [_H, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, _P, ctypes.c_double, _P]),
+    "csp_batch_set_output": (ctypes.c_int, [_H, ctypes.c_int]),
     "csp_flux_target": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_uint32, _P]),
     "csp_batch_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]),
     "csp_batch_destroy": (ctypes.c_int, [_H]),
@@ -99,6 +103,7 @@ SIGNATURES = {
     "csp_server_stats": (ctypes.c_int, [_H, _P]),
 }
 STINPUT_APPLY_OPTICS = 1
+OUT_STAGED = 1  # staged results: rays straight from the sun to the receiver left out
 ACCEL_AUTO, ACCEL_BVH, ACCEL_GRID, ACCEL_LIST = 0, 1, 2, 3
 GROUP_LIST, GROUP_BVH, GROUP_GRID = 0, 1, 2  # batch kernel groups
 
@@ -248,18 +253,22 @@ class Tracer:
         _check(self.lib.csp_get_sun_plane(self.h, _ptr(out)))
         return out
 
-    def flux_map(self, nx: int = 100, ny: int = 100, dni: float = 1000.0):
-        """(counts [nx, ny] uint32, flux [nx, ny] W/m^2) of the last run, binned on the device."""
+    def flux_map(self, nx: int = 100, ny: int = 100, dni: float = 1000.0, staged: bool = False):
+        """(counts [nx, ny] uint32, flux [nx, ny] W/m^2) of the last run, binned on the device;
+        staged: without the receiver records of rays straight from the sun."""
         counts = np.zeros((nx, ny), np.uint32)
         flux = np.zeros((nx, ny), np.float64)
-        _check(self.lib.csp_flux_map(self.h, int(nx), int(ny), _ptr(counts), float(dni), _ptr(flux)))
+        _check(self.lib.csp_flux_map_ex(self.h, int(nx), int(ny), OUT_STAGED if staged else 0, _ptr(counts),
+                                        float(dni), _ptr(flux)))
         return counts, flux
 
     def read_stinput(self, path: str, apply_optics: bool = False):
         _check(self.lib.csp_read_stinput(self.h, path.encode(), STINPUT_APPLY_OPTICS if apply_optics else 0))
 
-    def write_output(self, path: str):
-        _check(self.lib.csp_write_output(self.h, path.encode()))
+    def write_output(self, path: str, staged: bool = False):
+        """The reference's CSV of the last run; staged: without the rows of rays straight from the
+        sun to the receiver (clean_direct_sun.py's output)."""
+        _check(self.lib.csp_write_output_ex(self.h, path.encode(), OUT_STAGED if staged else 0))
 
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:
@@ -332,6 +341,10 @@ class Batch:
 
     def run(self):
         _check(self.lib.csp_batch_run(self.h))
+
+    def set_output(self, staged: bool = False):
+        """Staged flux maps (no receiver records of rays straight from the sun) from the next run on."""
+        _check(self.lib.csp_batch_set_output(self.h, OUT_STAGED if staged else 0))
 
     def run_async(self):
         """Build the current instances and queue their run behind the one in flight (at most two)."""
@@ -488,10 +501,11 @@ def trace_noalloc(elements: np.ndarray, sun_dir, sun_shape: int, sun_param: floa
                                     ctypes.c_void_p(stream or 0)))
 
 
-def write_hits_csv(hits: np.ndarray, path: str) -> None:
-    """Host-only CSV writer of [N, 5, 4] float32 hit records (the reference's write_output format)."""
+def write_hits_csv(hits: np.ndarray, path: str, staged: bool = False) -> None:
+    """Host-only CSV writer of [N, 5, 4] float32 hit records (the reference's write_output format);
+    staged: without the rows of rays straight from the sun to the receiver."""
     h = np.ascontiguousarray(hits, np.float32)
-    _check(load().csp_write_hits_csv(_ptr(h), h.shape[0], path.encode()))
+    _check(load().csp_write_hits_csv_ex(_ptr(h), h.shape[0], path.encode(), OUT_STAGED if staged else 0))
 
 
 def tracer_for(scene, device: int = 0, seed: int = 0, instance: int = 0, record_ids: bool = True,
