@@ -90,6 +90,30 @@ def test_reach_pretest_edges_bit_exact(gpu, oracle32, name):
         assert (oh[:, 1:, 0] != 0).any()
 
 
+@pytest.mark.parametrize("first", [(1 << 32) - 5000, (1 << 40) + 12345], ids=["2^32-5000", "2^40+12345"])
+def test_ray_indices_beyond_32_bits(gpu, oracle32, first):
+    """Ray windows starting near and far beyond 2^32 (csp_trace_into with a first ray): the Halton
+    loops past their tables, the 64-bit Philox counter and, for the field, the coherent order of
+    a 400k-ray window offset by the first ray, against the oracle."""
+    import torch
+    cases = [(scenes.three_heliostats(), 60000), (scenes.single_parabolic(), 60000),
+             (scenes.large_field(n_heliostats=300, sun=scenes.sun_vector(40.0, 30.0)), 400000)]
+    for sc, n in cases:
+        t = native.tracer_for(sc, seed=2, instance=1, num_rays=1024)
+        try:
+            hits = torch.zeros(n * 5 * 4, dtype=torch.float32, device="cuda")
+            ids = torch.zeros(n * 5, dtype=torch.int32, device="cuda")
+            t.trace_into(hits.data_ptr(), ids.data_ptr(), first, n)
+            torch.cuda.synchronize()
+        finally:
+            t.close()
+        oh, oi = oracle32.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, first_ray=first, count=n, seed=2,
+                                instance=1)
+        np.testing.assert_array_equal(ids.cpu().numpy().view(np.uint32).reshape(n, 5), oi, err_msg=sc.name)
+        np.testing.assert_array_equal(hits.cpu().numpy().reshape(n, 5, 4), oh.astype(np.float32), err_msg=sc.name)
+        assert (oh[:, 1:, 0] != 0).any()
+
+
 @pytest.mark.parametrize("accel", [native.ACCEL_BVH, native.ACCEL_GRID], ids=["bvh", "grid"])
 def test_gpu_large_field_bit_exact(gpu, oracle32, accel):
     """2000 flat heliostats, cylinder receiver, through the BVH and through the field grid: a window
