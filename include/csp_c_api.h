@@ -284,6 +284,8 @@ CSP_API int csp_server_add_scene(csp_server s, const csp_element* elements, uint
 CSP_API int csp_server_submit(csp_server s, uint32_t scene_id, const csp_element* poses, const double* sun_dir,
                               int sun_shape, double sun_param, uint64_t num_rays, uint64_t seed, uint32_t instance,
                               uint64_t* request_id);
+/* Output flags (CSP_OUT_STAGED or 0, default 0) of the requests submitted from now on. */
+CSP_API int csp_server_set_output(csp_server s, int flags);
 /* hold != 0: admit no further requests (they stay queued; active ones run to completion);
  * hold == 0: resume admission, admitting the queued requests together.  Destroying a held server
  * drops its queued requests. */

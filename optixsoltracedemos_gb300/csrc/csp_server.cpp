@@ -75,6 +75,7 @@ struct SRequest {
     double param = 0;
     uint64_t rays = 0, seed = 0;
     uint32_t instance = 0;
+    int out_flags = 0;  // CSP_OUT_* of its flux map (the server's setting at submission)
 
     ReqState state = kPending;
     std::string error;
@@ -139,6 +140,7 @@ struct Server {
     int device = -1;
     cudaStream_t stream = nullptr;
     uint32_t nx = 100, ny = 100;
+    int out_flags = 0;  // CSP_OUT_* given to requests at submission
     int max_active = 64;
     uint64_t step_rays = 64ull << 20;  // rays per step across all active requests (target)
     size_t budget = 0;
@@ -335,6 +337,7 @@ int Server::submit(const SRequest& in, uint64_t* id) {
     if (!(in.param >= 0.0) || in.param > 0.5) return set_error(CSP_ERR_INVALID_ARGUMENT, "sun shape parameter out of range");
     if (in.rays == 0 || in.rays >= (1ull << 40)) return set_error(CSP_ERR_INVALID_ARGUMENT, "bad ray count");
     r->id = next_id++;
+    r->out_flags = out_flags;
     r->sc = &s;
     r->group = s.group;
     if (r->group != kAccelFlat && !r->poses.empty()) r->group = r->grid.valid ? kAccelGrid : kAccelBvh;
@@ -557,6 +560,7 @@ int Server::step_launch(std::vector<SRequest*>& finishing, uint64_t& rays) {
         d.args.h3t12 = h3t12;
         const csp_element& rcv = (r->poses.empty() ? s.elements : r->poses).back();
         flux_target(rcv, nx, ny, d.flux);
+        d.flux.staged = (r->out_flags & CSP_OUT_STAGED) ? 1 : 0;
         d.flux.counts = reinterpret_cast<uint32_t*>(d_arena + r->o_counts);
         d.flux.stats = reinterpret_cast<unsigned long long*>(d_arena + r->o_stats);
         d.tile_begin = tiles[g];
@@ -746,6 +750,15 @@ int csp_server_submit(csp_server sh, uint32_t scene, const csp_element* poses, c
     r.seed = seed;
     r.instance = instance;
     return s->submit(r, request);
+}
+
+int csp_server_set_output(csp_server sh, int flags) {
+    CSP_SGUARD(sh);
+    if (flags & ~CSP_OUT_STAGED) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "unknown output flags");
+    Server* s = reinterpret_cast<Server*>(sh);
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->out_flags = flags;
+    return CSP_OK;
 }
 
 int csp_server_hold(csp_server sh, int hold) {

@@ -72,6 +72,7 @@ SIGNATURES = {
     "csp_flux_map": (ctypes.c_int, [_H, ctypes.c_uint32, ctypes.c_uint32, _P, ctypes.c_double, _P]),
     "csp_flux_map_ex": (ctypes.c_int, [_H, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, _P, ctypes.c_double, _P]),
     "csp_batch_set_output": (ctypes.c_int, [_H, ctypes.c_int]),
+    "csp_server_set_output": (ctypes.c_int, [_H, ctypes.c_int]),
     "csp_flux_target": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_uint32, _P]),
     "csp_batch_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]),
     "csp_batch_destroy": (ctypes.c_int, [_H]),
@@ -431,6 +432,10 @@ class Server:
     def hold(self, on: bool = True):
         """Pause (True) or resume (False) admission of queued requests."""
         _check(self.lib.csp_server_hold(self.h, 1 if on else 0))
+
+    def set_output(self, staged: bool = False):
+        """Staged flux maps for the requests submitted from now on."""
+        _check(self.lib.csp_server_set_output(self.h, OUT_STAGED if staged else 0))
 
     def wait(self, request: int, timeout: float = -1.0):
         """(counts [100, 100] uint32, stats [4] uint64, (latency s, queueing s))."""

@@ -7,7 +7,7 @@ sun), the staged CSV writer equals the plain CSV after `clean_receiver_direct_su
 byte, and the ray numbers it keeps are those of the script's group rule (a number is kept if its
 rows include stage 1 or exclude stage 2), restated here from the records.
 GPU: staged device flux maps equal the oracle's binning of the kept rays; the staged write_output
-equals the cleaned plain one; staged batch flux maps equal staged plain ones.
+equals the cleaned plain one; staged batch and served flux maps equal staged plain ones.
 """
 import os
 
@@ -95,3 +95,15 @@ def test_staged_device_outputs(gpu, oracle32, tmp_path):
         np.testing.assert_array_equal(b.counts(0), want_plain)
     finally:
         b.close()
+    # served requests: the setting at submission applies
+    srv = native.Server(0, memory_budget=1 << 30, max_active=8)
+    try:
+        sid = srv.add_scene(sc.elements)
+        srv.set_output(staged=True)
+        a = srv.submit(sid, sc.sun_dir, sc.sun_shape, sc.sun_param, n, seed=3, instance=0)
+        srv.set_output(staged=False)
+        c = srv.submit(sid, sc.sun_dir, sc.sun_shape, sc.sun_param, n, seed=3, instance=0)
+        np.testing.assert_array_equal(srv.wait(a)[0], want_staged)
+        np.testing.assert_array_equal(srv.wait(c)[0], want_plain)
+    finally:
+        srv.close()
