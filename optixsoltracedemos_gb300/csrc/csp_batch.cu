@@ -98,11 +98,12 @@ __device__ __forceinline__ void finish_instance(BatchSmem<C::kB, C::kAccel>& sm,
 }
 
 // Resident threads per SM the register budget is cut for: 1024 for the field kernels (64
-// registers: more warps to hide the grid walk's load latency), 768 for the element-list kernel
-// (which would spill at 64).
+// registers: more warps to hide the grid walk's load latency), 1152 for the element-list kernel
+// (nine 128-thread CTAs, 56 registers: its phases are short latency chains, and it measured 3.5 %
+// faster than at 64 registers despite a few spilled bytes).
 template <int kAccel>
 constexpr int batch_threads_per_sm() {
-    return kAccel == kAccelFlat ? 768 : 1024;
+    return kAccel == kAccelFlat ? 1152 : 1024;
 }
 
 template <int kB, int kAccel>
