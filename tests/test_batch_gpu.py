@@ -215,6 +215,22 @@ def test_batch_pipelined_runs(gpu):
             b.clear_instances()
             for j in jobs:
                 b.add_instance(j[0], j[2], j[3], j[4], j[5], seed=j[6], instance=j[7], poses=j[1])
+        # a run that needs a larger arena than the one in flight (reallocation behind it)
+        b.clear_instances()
+        b.add_instance(0, th.sun_dir, th.sun_shape, th.sun_param, 400000, seed=4, instance=2)
+        b.run_async()  # small layout in flight
+        b.clear_instances()
+        for j in jobs * 3:
+            b.add_instance(j[0], j[2], j[3], j[4], j[5], seed=j[6], instance=j[7], poses=j[1])
+        b.run_async()  # three times the instances: the arena grows
+        b.wait()
+        np.testing.assert_array_equal(b.counts(0), counts_b)
+        b.wait()
+        for i in range(3 * len(jobs)):
+            np.testing.assert_array_equal(b.counts(i), ref_a[i % len(jobs)])
+        b.clear_instances()
+        for j in jobs:
+            b.add_instance(j[0], j[2], j[3], j[4], j[5], seed=j[6], instance=j[7], poses=j[1])
         # synchronous run after pipelined ones, and a run_async left in flight at close
         b.run()
         for i in range(len(jobs)):
