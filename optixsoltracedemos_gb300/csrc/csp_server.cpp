@@ -78,6 +78,8 @@ struct SRequest {
     int out_flags = 0;  // CSP_OUT_* of its flux map (the server's setting at submission)
 
     ReqState state = kPending;
+    InstanceDesc desc{};      // its step descriptor except the ray window and tile offset
+    bool desc_ready = false;  // built at its first step (its arena block and scene are fixed)
     std::string error;
     uint64_t next_ray = 0;
     int group = kAccelBvh;
@@ -549,27 +551,33 @@ int Server::step_launch(std::vector<SRequest*>& finishing, uint64_t& rays) {
         const SScene& s = *r->sc;
         const int g = r->group;
         const uint64_t slice = std::min<uint64_t>(quantum, r->rays - r->next_ray);
-        InstanceDesc d{};
-        d.args.nodes = r->own_records && g != kAccelGrid ? reinterpret_cast<const Node*>(d_arena + r->o_nodes) : s.d_nodes;
-        d.args.prims = r->own_records ? reinterpret_cast<const Prim*>(d_arena + r->o_prims) : s.d_prims;
-        d.args.optics = r->own_records ? reinterpret_cast<const Optics*>(d_arena + r->o_optics) : s.d_optics;
-        d.args.sun = reinterpret_cast<const SunFrame*>(d_arena + r->o_sun);
-        d.args.hits = nullptr;
-        d.args.ids = nullptr;
+        if (!r->desc_ready) {
+            InstanceDesc& d = r->desc;
+            d = InstanceDesc{};
+            d.args.nodes = r->own_records && g != kAccelGrid ? reinterpret_cast<const Node*>(d_arena + r->o_nodes)
+                                                             : s.d_nodes;
+            d.args.prims = r->own_records ? reinterpret_cast<const Prim*>(d_arena + r->o_prims) : s.d_prims;
+            d.args.optics = r->own_records ? reinterpret_cast<const Optics*>(d_arena + r->o_optics) : s.d_optics;
+            d.args.sun = reinterpret_cast<const SunFrame*>(d_arena + r->o_sun);
+            d.args.hits = nullptr;
+            d.args.ids = nullptr;
+            d.args.seed = r->seed;
+            d.args.instance = r->instance;
+            d.args.pad = 0;
+            d.args.grid = g == kAccelGrid ? reinterpret_cast<const GridDesc*>(d_arena + r->o_grid) : nullptr;
+            d.args.h3t12 = h3t12;
+            const csp_element& rcv = (r->poses.empty() ? s.elements : r->poses).back();
+            flux_target(rcv, nx, ny, d.flux);
+            d.flux.staged = (r->out_flags & CSP_OUT_STAGED) ? 1 : 0;
+            d.flux.counts = reinterpret_cast<uint32_t*>(d_arena + r->o_counts);
+            d.flux.stats = reinterpret_cast<unsigned long long*>(d_arena + r->o_stats);
+            d.n_prims = (int)s.elements.size();
+            r->desc_ready = true;
+        }
+        InstanceDesc d = r->desc;
         d.args.ray_begin = r->next_ray;
         d.args.count = slice;
-        d.args.seed = r->seed;
-        d.args.instance = r->instance;
-        d.args.pad = 0;
-        d.args.grid = g == kAccelGrid ? reinterpret_cast<const GridDesc*>(d_arena + r->o_grid) : nullptr;
-        d.args.h3t12 = h3t12;
-        const csp_element& rcv = (r->poses.empty() ? s.elements : r->poses).back();
-        flux_target(rcv, nx, ny, d.flux);
-        d.flux.staged = (r->out_flags & CSP_OUT_STAGED) ? 1 : 0;
-        d.flux.counts = reinterpret_cast<uint32_t*>(d_arena + r->o_counts);
-        d.flux.stats = reinterpret_cast<unsigned long long*>(d_arena + r->o_stats);
         d.tile_begin = tiles[g];
-        d.n_prims = (int)s.elements.size();
         tb[g].push_back(tiles[g]);
         const uint64_t block = (uint64_t)kServeTuning[g].block;
         tiles[g] += (slice + block - 1) / block;
