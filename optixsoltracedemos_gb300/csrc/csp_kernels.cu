@@ -50,7 +50,9 @@ __global__ void __launch_bounds__(kTraceBlock, 6) trace_kernel(const typename Pl
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TraceSmem<kAccel>& sm = *reinterpret_cast<TraceSmem<kAccel>*>(smem_raw);
     load_instance_smem<C>(A, sm.core);
-    for (uint32_t m = threadIdx.x; m < kH3Tab; m += kTraceBlock) sm.core.t6[m] = halton3(m);
+    // the shared-memory Halton table serves only launches without the device-wide 3^12 table
+    if (!A.h3t12)
+        for (uint32_t m = threadIdx.x; m < kH3Tab; m += kTraceBlock) sm.core.t6[m] = halton3(m);
     if (threadIdx.x == 0) {
         sm.core.qsize = 0;
         sm.core.gsize = 0;
