@@ -42,6 +42,22 @@ def test_staged_csv_equals_cleaned_csv(tmp_path, oracle32):
     assert os.path.getsize(staged) < os.path.getsize(plain)
 
 
+def test_clean_csv_group_rule(tmp_path):
+    """Hand-made file: ray numbers with stages {0}, {0,1}, {0,1,2}, {0,2}, {0,1,1,2}, {2} (no stage 0)
+    and {0,1,1}; the script's rule keeps a number with a stage-1 row or without a stage-2 row, so
+    numbers 4 and 6 go; kept rows are copied byte for byte."""
+    rows = {1: [0], 2: [0, 1], 3: [0, 1, 2], 4: [0, 2], 5: [0, 1, 1, 2], 6: [2], 7: [0, 1, 1]}
+    lines = ["number,stage,loc_x,loc_y,loc_z\n"]
+    for num, stages in rows.items():
+        for k, st in enumerate(stages):
+            lines.append(f"{num},{st},{k}.5,-{num}e-05,{num * 10 + k}\n")
+    src, dst = str(tmp_path / "in.csv"), str(tmp_path / "out.csv")
+    open(src, "w").write("".join(lines))
+    post.clean_receiver_direct_sun_hits(src, dst)
+    want = [lines[0]] + [l for l in lines[1:] if int(l.split(",")[0]) not in (4, 6)]
+    assert open(dst).read() == "".join(want)
+
+
 def test_staged_flag_validation(tmp_path):
     hits = np.zeros((1, 5, 4), np.float32)
     rc = native.load().csp_write_hits_csv_ex(hits.ctypes.data, 1, str(tmp_path / "x.csv").encode(), 2)
