@@ -80,21 +80,32 @@ struct Cfg {
 // coordinates of offsets that differ by a multiple of S = 2^a 3^b differ by less than 2^-a in u
 // (base 2) and 3^-b in v (base 3), so a warp's rays start within a small patch of the sun plane and
 // walk the same grid cells.  Whole blocks of S = 2^8 3^5 first, then of S = 2^7 3^4 over the rest,
-// then the identity order for the tail: a bijection on [0, count).
+// then the identity order for the tail: a bijection on [0, count).  kFine puts whole blocks of
+// S = 2^9 3^6 (11,943,936 rays) before them: launches without dense records gain from the smaller
+// patches, while in dense launches a warp's 32 rows would then span ~1 GB of the hit buffer, which
+// measured slower.
+constexpr uint64_t kCoherentS0 = 512u * 729u, kCoherentB0 = 32u * kCoherentS0;
 constexpr uint64_t kCoherentS1 = 256u * 243u, kCoherentB1 = 32u * kCoherentS1;
 constexpr uint64_t kCoherentS2 = 128u * 81u, kCoherentB2 = 32u * kCoherentS2;
 
+template <bool kFine>
 __device__ __forceinline__ uint64_t coherent_order(uint64_t kk, uint64_t count) {
-    const uint64_t full1 = (count / kCoherentB1) * kCoherentB1;
-    if (kk < full1) {
-        const uint64_t blk = kk / kCoherentB1, r = kk - blk * kCoherentB1;
-        return blk * kCoherentB1 + (r >> 5) + (r & 31u) * kCoherentS1;
+    const uint64_t full0 = kFine ? (count / kCoherentB0) * kCoherentB0 : 0;
+    if (kk < full0) {
+        const uint64_t blk = kk / kCoherentB0, r = kk - blk * kCoherentB0;
+        return blk * kCoherentB0 + (r >> 5) + (r & 31u) * kCoherentS0;
     }
-    const uint64_t k2 = kk - full1;
-    const uint64_t full2 = ((count - full1) / kCoherentB2) * kCoherentB2;
+    const uint64_t k1 = kk - full0, c1 = count - full0;
+    const uint64_t full1 = (c1 / kCoherentB1) * kCoherentB1;
+    if (k1 < full1) {
+        const uint64_t blk = k1 / kCoherentB1, r = k1 - blk * kCoherentB1;
+        return full0 + blk * kCoherentB1 + (r >> 5) + (r & 31u) * kCoherentS1;
+    }
+    const uint64_t k2 = k1 - full1;
+    const uint64_t full2 = ((c1 - full1) / kCoherentB2) * kCoherentB2;
     if (k2 < full2) {
         const uint64_t blk = k2 / kCoherentB2, r = k2 - blk * kCoherentB2;
-        return full1 + blk * kCoherentB2 + (r >> 5) + (r & 31u) * kCoherentS2;
+        return full0 + full1 + blk * kCoherentB2 + (r >> 5) + (r & 31u) * kCoherentS2;
     }
     return kk;
 }
@@ -1072,7 +1083,7 @@ __device__ __forceinline__ void trace_tile(const typename C::Args& A, const Sink
     }
     const uint64_t kk = tile * C::kB + threadIdx.x;
     uint64_t pos = kk;
-    if constexpr (C::kCoherent) pos = coherent_order(kk, A.count);
+    if constexpr (C::kCoherent) pos = coherent_order<!C::kDense>(kk, A.count);
     const uint64_t ray = A.ray_begin + pos;
     if constexpr (C::kDense && !C::kFlat) {
 #pragma unroll

@@ -240,6 +240,35 @@ def test_batch_pipelined_runs(gpu):
         b.close()
 
 
+def test_batch_fine_coherent_level(gpu):
+    """An instance of more than 32 * 2^9 * 3^6 = 11,943,936 rays (the first coherent-order level of
+    the launches without dense records) gives the plain run's flux map, count for count."""
+    from optixsoltracedemos_gb300 import native
+    sun = scenes.sun_vector(35.0, 20.0)
+    el = scenes.reaim(_field(600, sun), sun)
+    n = 11943936 + 1234567
+    b = native.Batch(0)
+    try:
+        sid = b.add_scene(el)
+        b.add_instance(sid, sun, scenes.SUN_PILLBOX, 4.65e-3, n, seed=6, instance=3)
+        b.run()
+        t = native.Tracer(0, n)
+        try:
+            t.set_elements(el)
+            t.set_sun_vector(sun)
+            t.set_sun_shape(scenes.SUN_PILLBOX, 4.65e-3)
+            t.set_seed(6, 3)
+            t.initialize()
+            t.run()
+            counts, _ = t.flux_map()
+        finally:
+            t.close()
+        assert counts.sum() > 10000
+        np.testing.assert_array_equal(b.counts(0), counts)
+    finally:
+        b.close()
+
+
 def test_batch_empty_instances(gpu):
     """Instances with no rays trace nothing and leave empty flux maps; the others are unaffected."""
     from optixsoltracedemos_gb300 import native
