@@ -83,29 +83,41 @@ struct Cfg {
 // then the identity order for the tail: a bijection on [0, count).  kFine puts whole blocks of
 // S = 2^9 3^6 (11,943,936 rays) before them: launches without dense records gain from the smaller
 // patches, while in dense launches a warp's 32 rows would then span ~1 GB of the hit buffer, which
-// measured slower.
+// measured slower.  With G > 1 the G warps of one tile (CTA) take neighbouring patches: warp k of
+// tile t in a block gets m = k S / G + t, and offsets that differ by S / G = 2^(a-log2 G) 3^b have
+// u coordinates 2^-a apart -- a strip of G adjacent patches whose grid cells the CTA's warps share
+// in L1.
 constexpr uint64_t kCoherentS0 = 512u * 729u, kCoherentB0 = 32u * kCoherentS0;
 constexpr uint64_t kCoherentS1 = 256u * 243u, kCoherentB1 = 32u * kCoherentS1;
 constexpr uint64_t kCoherentS2 = 128u * 81u, kCoherentB2 = 32u * kCoherentS2;
 
-template <bool kFine>
+// warp position m in a block of S warps for the warp at index r >> 5 of the block (G | S)
+template <int G>
+__device__ __forceinline__ uint64_t coherent_warp(uint64_t r, uint64_t S) {
+    const uint64_t w = r >> 5;
+    if constexpr (G == 1) return w;
+    else return (w % G) * (S / G) + w / G;
+}
+
+template <bool kFine, int G>
 __device__ __forceinline__ uint64_t coherent_order(uint64_t kk, uint64_t count) {
+    static_assert(G == 1 || G == 4 || G == 8 || G == 16, "tile warps must divide every S");
     const uint64_t full0 = kFine ? (count / kCoherentB0) * kCoherentB0 : 0;
     if (kk < full0) {
         const uint64_t blk = kk / kCoherentB0, r = kk - blk * kCoherentB0;
-        return blk * kCoherentB0 + (r >> 5) + (r & 31u) * kCoherentS0;
+        return blk * kCoherentB0 + coherent_warp<G>(r, kCoherentS0) + (r & 31u) * kCoherentS0;
     }
     const uint64_t k1 = kk - full0, c1 = count - full0;
     const uint64_t full1 = (c1 / kCoherentB1) * kCoherentB1;
     if (k1 < full1) {
         const uint64_t blk = k1 / kCoherentB1, r = k1 - blk * kCoherentB1;
-        return full0 + blk * kCoherentB1 + (r >> 5) + (r & 31u) * kCoherentS1;
+        return full0 + blk * kCoherentB1 + coherent_warp<G>(r, kCoherentS1) + (r & 31u) * kCoherentS1;
     }
     const uint64_t k2 = k1 - full1;
     const uint64_t full2 = ((c1 - full1) / kCoherentB2) * kCoherentB2;
     if (k2 < full2) {
         const uint64_t blk = k2 / kCoherentB2, r = k2 - blk * kCoherentB2;
-        return full0 + full1 + blk * kCoherentB2 + (r >> 5) + (r & 31u) * kCoherentS2;
+        return full0 + full1 + blk * kCoherentB2 + coherent_warp<G>(r, kCoherentS2) + (r & 31u) * kCoherentS2;
     }
     return kk;
 }
@@ -1083,7 +1095,7 @@ __device__ __forceinline__ void trace_tile(const typename C::Args& A, const Sink
     }
     const uint64_t kk = tile * C::kB + threadIdx.x;
     uint64_t pos = kk;
-    if constexpr (C::kCoherent) pos = coherent_order<!C::kDense>(kk, A.count);
+    if constexpr (C::kCoherent) pos = coherent_order<!C::kDense, C::kDense ? 1 : C::kB / 32>(kk, A.count);
     const uint64_t ray = A.ray_begin + pos;
     if constexpr (C::kDense && !C::kFlat) {
 #pragma unroll
