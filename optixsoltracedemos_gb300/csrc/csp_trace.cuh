@@ -83,10 +83,10 @@ struct Cfg {
 // then the identity order for the tail: a bijection on [0, count).  kFine puts whole blocks of
 // S = 2^9 3^6 (11,943,936 rays) before them: launches without dense records gain from the smaller
 // patches, while in dense launches a warp's 32 rows would then span ~1 GB of the hit buffer, which
-// measured slower.  With G > 1 the G warps of one tile (CTA) take neighbouring patches: warp k of
-// tile t in a block gets m = k S / G + t, and offsets that differ by S / G = 2^(a-log2 G) 3^b have
-// u coordinates 2^-a apart -- a strip of G adjacent patches whose grid cells the CTA's warps share
-// in L1.
+// measured slower.  With G > 1 groups of G consecutive warps (of one tile, i.e. CTA) take
+// neighbouring patches: warp k of group t in a block gets m = k S / G + t, and offsets that differ
+// by S / G = 2^(a-log2 G) 3^b have u coordinates 2^-a apart -- a strip of G adjacent patches whose
+// grid cells the group's warps share in L1.
 constexpr uint64_t kCoherentS0 = 512u * 729u, kCoherentB0 = 32u * kCoherentS0;
 constexpr uint64_t kCoherentS1 = 256u * 243u, kCoherentB1 = 32u * kCoherentS1;
 constexpr uint64_t kCoherentS2 = 128u * 81u, kCoherentB2 = 32u * kCoherentS2;
@@ -101,7 +101,7 @@ __device__ __forceinline__ uint64_t coherent_warp(uint64_t r, uint64_t S) {
 
 template <bool kFine, int G>
 __device__ __forceinline__ uint64_t coherent_order(uint64_t kk, uint64_t count) {
-    static_assert(G == 1 || G == 4 || G == 8 || G == 16, "tile warps must divide every S");
+    static_assert(G == 1 || G == 2 || G == 4 || G == 8 || G == 16, "warp groups must divide every S");
     const uint64_t full0 = kFine ? (count / kCoherentB0) * kCoherentB0 : 0;
     if (kk < full0) {
         const uint64_t blk = kk / kCoherentB0, r = kk - blk * kCoherentB0;
@@ -1095,7 +1095,9 @@ __device__ __forceinline__ void trace_tile(const typename C::Args& A, const Sink
     }
     const uint64_t kk = tile * C::kB + threadIdx.x;
     uint64_t pos = kk;
-    if constexpr (C::kCoherent) pos = coherent_order<!C::kDense, C::kDense ? 1 : C::kB / 32>(kk, A.count);
+    // dense launches group warps in pairs: larger groups scatter their record rows more than the
+    // shared cells save
+    if constexpr (C::kCoherent) pos = coherent_order<!C::kDense, C::kDense ? 2 : C::kB / 32>(kk, A.count);
     const uint64_t ray = A.ray_begin + pos;
     if constexpr (C::kDense && !C::kFlat) {
 #pragma unroll
