@@ -1,29 +1,38 @@
 #!/usr/bin/env python
-"""Benchmark: rays/s of the plain trace on one GB300 (single parabolic heliostat workload).
+"""Benchmark: rays/s of batched tracing on one GB300 (256 sun positions of the 10,000-heliostat field).
 
-Workload (default): 10 x 10 m paraboloid (focal length 100 m) at (0,100,0) aimed at a cylindrical
-receiver r = 2 m, h = 4 m centred (0,0,100); Gaussian sun 2.5 mrad; slope error 1.5 mrad;
-16,777,216 rays, float32, synthetic (the reference ships no benchmark scenes).
+Headline workload (default, `--workload batched`): the 10,000-heliostat radial-stagger field
+(10 x 10 m flat mirrors, cylindrical receiver r = 8 m, h = 20 m at 200 m; pillbox sun 4.65 mrad;
+slope error 1.5 mrad) at 256 sun positions (elevation U(10, 80) deg, azimuth U(-120, 120) deg,
+seed 2), every heliostat re-aimed per instance, ray counts log-uniform in [2^20, 2^25] (seed 3):
+2,343,992,611 rays, float32, synthetic (the reference ships no benchmark scenes).
 
-One step = one trace of all rays: generation, closest-hit search, shading, and the full rewrite of
-the dense 16M x 5 float4 hit buffer (1.34 GB, larger than L2, so no flush is needed between steps).
+One step = one csp_batch run of all 256 instances: per-instance BVH refit and sun planes, one
+persistent trace launch, receiver flux maps accumulated in the shading stage.
 
-  value      rays/s with the scene resident in HBM: K trace launches timed with CUDA events on the
-             launching stream.
-  e2e        rays/s through the public C ABI with host buffers: per step, upload of the element list
-             (csp_set_elements + csp_update: H2D, refit, sun plane) and csp_run_to_host (trace +
-             D2H of every hit record into page-locked memory), wall-clock timed.
-  roofline   HBM: algorithmic bytes = 80 B per ray (the dense hit records) / per-launch time.
-  cpu_baseline  the oracle port of the reference algorithm on all host cores, bounded sample.
+  value      rays/s with the instances' records resident in HBM: device time of K runs (refit, sun
+             planes and trace, CUDA events inside the run's graph); the instances' scenes
+             (~0.5 GB) exceed L2, so no flush is needed between steps.
+  e2e        rays/s through the C ABI from host memory: K pipelined runs (csp_batch_run_async /
+             csp_batch_wait) from the host pose arrays (element builds, staging, H2D upload) to the
+             flux maps in host memory, wall clock.
+  roofline   issue slots (nothing per ray leaves the SM: the batch kernel is bound by instruction
+             issue and latency, not HBM): warp instructions per ray from ncu x rays / device time
+             against SMs x 4 schedulers x the SM clock.
+  cpu_baseline  the oracle port of the reference algorithm on all host cores, on ray samples of
+             the batched workload's instances (brute-force closest hit over 10,001 elements).
+  plain_loop the same instances through the drop-in handle one scene at a time (new poses,
+             csp_update, csp_run, csp_flux_map): the north star's "plain per-scene launch loop".
 
-The default line also carries `batched` (256 sun positions of the 10,000-heliostat field, one
-csp_batch run, against the plain per-scene loop through the drop-in handle) and `served` (300
-requests over fields of 3 / 1,000 / 10,000 heliostats through csp_server, at saturation and with
-Poisson arrivals at 200/s: p50 / p99 latency, against the plain loop); `--workload batched|served`
-prints those lines in full, `--no-systems` leaves them out.
+The default line also carries the plain trace workloads and the served workload as sub-objects:
+`single_parabolic` (one parabolic heliostat, 16M rays, the dense-record HBM roofline),
+`large_field` (the field in one plain launch of 268M rays) and `served` (Poisson requests over
+fields of 3 / 1,000 / 10,000 heliostats through csp_server, p50 / p99 latency).  `--workload
+single_parabolic|three_heliostats|large_field|served` prints one of those as the whole line;
+`--no-systems` leaves the sub-objects out.
 
 --impl reference times the reference algorithm's CPU implementation (the oracle port: the
-reference's own programs cannot run this workload's Gaussian sun and slope error) on all host
+reference's own programs cannot run the slope error and re-aiming of this workload) on all host
 cores, on the same workload and metric.
 
 Multi-GPU: replicas only (each rank traces its own copy of the workload; no exchange), launched by
@@ -44,23 +53,30 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "rays/s on 1 GB300 (batched/served vs plain trace) at flux L2<=1%; p50/p99 latency"
-BYTES_PER_RAY = 80  # 5 float4 hit records per ray, fully rewritten by every trace
-# dram__bytes_read.sum + dram__bytes_write.sum of one full-size trace_kernel launch of this workload
-# (34,487,552 + 1,318,957,568 bytes), from the ncu capture summarised in
-# profiles/trace_kernel_single_parabolic.md
+BYTES_PER_RAY = 80  # 5 float4 hit records per ray, fully rewritten by every plain trace
+# dram__bytes_read.sum + dram__bytes_write.sum of one full-size trace_kernel launch of the single
+# parabolic workload (34,487,552 + 1,318,957,568 bytes), from an ncu capture of
+# `python bench.py --workload single_parabolic --steps 3 --warmup 2` (kernel trace_kernel, one launch)
 NCU_TRAFFIC_PER_LAUNCH = 1371278592
+# Batch kernel (field grid) on the batched workload: warp instructions and DRAM bytes per traced ray,
+# from `ncu --set full` of `python bench.py --workload batched --instances 8 --tuning 256,0,16
+# --steps 1 --warmup 3 --no-systems --no-cpu-baseline --plain-instances 1` (kernel batch_kernel,
+# one launch): smsp__inst_executed.sum and dram__bytes_read.sum + dram__bytes_write.sum divided by
+# that launch's rays.  None until captured for the current kernel.
+BATCH_WARP_INST_PER_RAY = None
+BATCH_DRAM_BYTES_PER_RAY = None
+ISSUE_PER_SM_PER_CYCLE = 4  # one warp instruction per cycle per scheduler, 4 schedulers per SM
 
 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=400)
-    p.add_argument("--warmup", type=int, default=10)
+    p.add_argument("--steps", type=int, default=None, help="timed steps (default: 10 batched, 400 plain)")
+    p.add_argument("--warmup", type=int, default=None, help="warm-up steps (default: 3 batched, 10 plain)")
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--rays", type=int, default=None, help="ray count (default: the workload's)")
-    p.add_argument("--workload", choices=["single_parabolic", "three_heliostats", "large_field", "batched", "served"],
-                   default="single_parabolic",
-                   help="single_parabolic is the benchmark line; the others are for reporting only")
+    p.add_argument("--workload", choices=["batched", "single_parabolic", "three_heliostats", "large_field", "served"],
+                   default="batched", help="batched is the benchmark line; the others are reported inside it")
     p.add_argument("--instances", type=int, default=256, help="batched workload: number of instances")
     p.add_argument("--heliostats", type=int, default=10000, help="batched / large_field: field size")
     p.add_argument("--e2e-steps", type=int, default=10)
@@ -68,13 +84,19 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-accuracy", action="store_true")
     p.add_argument("--no-systems", action="store_true",
-                   help="default line without the batched and served summaries")
+                   help="batched line without the plain and served sub-objects")
     p.add_argument("--tuning", type=str, default="", help="batched workload: block,ctas_per_sm,chunk (default: autotune)")
     p.add_argument("--requests", type=int, default=300, help="served workload: number of requests")
     p.add_argument("--rate", type=float, default=200.0, help="served workload: Poisson arrival rate (1/s)")
     p.add_argument("--plain-instances", type=int, default=0,
                    help="batched workload: instances timed in the plain loop (0 = all)")
-    return p.parse_args()
+    a = p.parse_args()
+    plain = a.workload in ("single_parabolic", "three_heliostats", "large_field")
+    if a.steps is None:
+        a.steps = 400 if plain and a.workload != "large_field" else 10
+    if a.warmup is None:
+        a.warmup = 10 if plain else 3
+    return a
 
 
 def dist_env():
@@ -85,12 +107,13 @@ def dist_env():
 
 
 def peaks():
+    """(HBM GB/s, source, SM max MHz) from the measured peaks, else the fallback figures."""
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             d = json.load(f)
-        return float(d["hbm_gbs"]), "measured"
+        return float(d["hbm_gbs"]), "measured", float(d.get("sm_max_mhz", 2070.0))
     except Exception:
-        return 6800.0, "fallback"
+        return 6800.0, "fallback", 2070.0
 
 
 class ClockSampler:
@@ -154,26 +177,32 @@ def max_over_ranks(seconds: float, pg, device: str) -> float:
     return float(t.item())
 
 
-def cpu_baseline(seconds: float, sc):
-    """Oracle port of the reference algorithm on all host cores over a bounded sample."""
+
+
+def _cpu_trace_for(seconds: float, jobs, sample: int):
+    """Oracle port of the reference algorithm on all host cores: `sample`-ray windows of the jobs
+    (elements, sun, shape, param, rays) round robin for about `seconds`.  Returns (rays, s, cores)."""
     from oracle import oracle
     oracle.build(with_ref=False)
     o = oracle.Oracle("f32")
-    rays = sc.num_rays
     cores = os.cpu_count() or 1
-    chunk = 1 << 20 if len(sc.elements) < 64 else 1 << 12
-    o.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, first_ray=0, count=chunk // 8, nthreads=cores,
-            with_ids=False)
-    done, first, t0 = 0, 0, time.perf_counter()
+    el, sun, shape, param, n = jobs[0]
+    o.trace(el, sun, shape, param, count=max(1, sample // 8), nthreads=cores, with_ids=False)
+    done, k, t0 = 0, 0, time.perf_counter()
     while time.perf_counter() - t0 < seconds:
-        o.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, first_ray=first, count=chunk, nthreads=cores,
-                with_ids=False)
-        done += chunk
-        first = (first + chunk) % rays
-    dt = time.perf_counter() - t0
+        el, sun, shape, param, n = jobs[k % len(jobs)]
+        first = ((k // len(jobs)) * sample) % max(1, n - sample + 1)
+        o.trace(el, sun, shape, param, first_ray=first, count=sample, nthreads=cores, with_ids=False)
+        done += sample
+        k += 1
+    return done, time.perf_counter() - t0, cores
+
+
+def cpu_baseline(seconds: float, jobs, sample: int, what: str):
+    done, dt, cores = _cpu_trace_for(seconds, jobs, sample)
     return {"value": done / dt, "unit": "rays/s", "cores": cores, "kind": "port",
-            "sample": f"{done} rays ({done // chunk} chunks of {chunk}) of the {sc.name} workload, "
-                      f"{dt:.1f} s, OpenMP over {cores} threads"}
+            "sample": f"{done} rays ({done // sample} windows of {sample}) of the {what} workload, {dt:.1f} s, "
+                      f"oracle port of the reference algorithm, OpenMP over {cores} threads"}
 
 
 def make_scene(workload, rays):
@@ -206,199 +235,6 @@ def config(sc):
     return base
 
 
-def run_reference(args):
-    rank, world, _ = dist_env()
-    if rank != 0:
-        return
-    from oracle import oracle
-    from optixsoltracedemos_gb300 import scenes
-    oracle.build(with_ref=False)
-    o = oracle.Oracle("f32")
-    cores = os.cpu_count() or 1
-    # per step: (elements, sun, shape, param, first ray, total rays of that scene or request)
-    if args.workload in ("batched", "served"):
-        from optixsoltracedemos_gb300 import scenes
-        if args.workload == "batched":
-            _, poses, suns, counts = batched_workload(args.instances, args.heliostats)
-            jobs = [(poses[i], suns[i], scenes.SUN_PILLBOX, 4.65e-3, int(counts[i])) for i in range(len(suns))]
-            cfg = {"workload": f"batched_{len(suns)}_instances_large_field_{args.heliostats}_heliostats",
-                   "instances": len(suns), "rays_total": int(sum(counts))}
-        else:
-            _, reqs = served_workload(args.requests, args.rate)
-            jobs = [(p, sun, scenes.SUN_PILLBOX, 4.65e-3, rays) for (_, p, sun, rays, _) in reqs]
-            cfg = {"workload": "served_requests_fields_3_1000_10000_flat_parabolic", "requests": len(reqs),
-                   "rays_total": int(sum(j[4] for j in jobs))}
-        sample = 1 << 14  # brute-force closest hit over up to 10,001 elements per ray
-        what = f"each step traces {sample} rays of the next instance/request"
-    else:
-        sc = make_scene(args.workload, args.rays)
-        jobs = [(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, sc.num_rays)]
-        cfg = config(sc)
-        sample = min(1 << 20, sc.num_rays) if args.workload != "large_field" else 1 << 14
-        what = f"each step traces {sample} of the {sc.num_rays} rays"
-
-    def step(k):
-        el, sun, shape, param, n = jobs[k % len(jobs)]
-        o.trace(el, sun, shape, param, first_ray=(k // len(jobs) * sample) % max(1, n), count=sample,
-                nthreads=cores, with_ids=False)
-
-    for w in range(args.warmup):
-        step(w)
-    t0 = time.perf_counter()
-    for k in range(args.steps):
-        step(k)
-    dt = time.perf_counter() - t0
-    v = args.steps * sample / dt
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "rays/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": cfg,
-            "cpu_baseline": {"value": v, "unit": "rays/s", "cores": cores, "kind": "port",
-                             "sample": f"{what} (oracle port of the reference algorithm, OpenMP over {cores} "
-                                       f"threads)"},
-            "e2e": {"value": v, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
-
-
-def run_ours(args):
-    import numpy as np
-    import torch
-
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    pg = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-        pg = dist
-
-    from optixsoltracedemos_gb300 import build as nbuild
-    if rank == 0:
-        nbuild.build()
-    if pg:
-        pg.barrier()
-    from optixsoltracedemos_gb300 import native, scenes
-    from optixsoltracedemos_gb300.flux import flux_map_from_hits, flux_l2
-
-    sc = make_scene(args.workload, args.rays)
-    N = sc.num_rays
-    tr = native.tracer_for(sc, device=local, record_ids=False)
-    stream = torch.cuda.Stream(device=local)
-    sp = stream.cuda_stream
-
-    for w in range(args.warmup):
-        tr.set_seed(w)
-        tr.trace_async(sp)
-    torch.cuda.synchronize()
-    if pg:
-        pg.barrier()
-
-    clk = ClockSampler(local)
-    clk.start()
-    time.sleep(0.3)
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for k in range(args.steps):
-        tr.set_seed(1000 + k, rank)  # each replica traces its own rays (Philox instance = rank)
-        starts[k].record(stream)
-        tr.trace_async(sp)
-        ends[k].record(stream)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    clocks = clk.stop()
-    total_s = e0.elapsed_time(e1) * 1e-3
-    launch_s = statistics.mean(s.elapsed_time(e) for s, e in zip(starts, ends)) * 1e-3
-    total_s = max_over_ranks(total_s, pg, f"cuda:{local}")
-    value = world * N * args.steps / total_s
-
-    # end to end through the C ABI with host buffers
-    host = torch.empty(N * 5 * 4, dtype=torch.float32, pin_memory=True)
-    elements = sc.elements.copy()
-    for _ in range(2):
-        tr.set_elements(elements)
-        tr.update()
-        tr.run_to_host_ptr(host.data_ptr())
-    if pg:
-        pg.barrier()
-    t0 = time.perf_counter()
-    for k in range(args.e2e_steps):
-        tr.set_seed(5000 + k, rank)
-        tr.set_elements(elements)
-        tr.update()
-        tr.run_to_host_ptr(host.data_ptr())
-    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
-    e2e_s = max_over_ranks(e2e_s, pg, f"cuda:{local}")
-
-    peak, peak_kind = peaks()
-    achieved = BYTES_PER_RAY * N / launch_s / 1e9
-    line = {
-        "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": config(sc),
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": NCU_TRAFFIC_PER_LAUNCH if (N == 1 << 24 and sc.name == "single_parabolic") else None,
-                     "peak_source": peak_kind,
-                     "algorithmic_bytes_per_launch": BYTES_PER_RAY * N, "launch_ms": launch_s * 1e3},
-        "e2e": {"value": world * N / e2e_s, "unit": "rays/s",
-                "h2d_bytes_per_step": int(elements.nbytes + 3 * 8),
-                "d2h_bytes_per_step": int(N * BYTES_PER_RAY)},
-        "gpu_launches": args.steps,
-        "clocks": clocks,
-    }
-    if rank == 0 and world == 1 and not args.no_accuracy:
-        try:
-            from oracle import oracle
-            oracle.build(with_ref=False)
-            tr.set_seed(0)
-            tr.run()
-            hits = host.numpy().reshape(N, 5, 4)
-            tr.run_to_host(hits.reshape(-1))
-            o64 = oracle.Oracle("f64")
-            oh, _ = o64.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, count=N, with_ids=False)
-            line["flux_l2_vs_fp64"] = flux_l2(flux_map_from_hits(hits, sc.elements[-1], N),
-                                              flux_map_from_hits(oh, sc.elements[-1], N))
-            del oh
-        except Exception as exc:  # accuracy is reported, not required for the timing line
-            line["flux_l2_vs_fp64"] = f"unavailable: {exc}"
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args.cpu_seconds, sc)
-    tr.close()
-    if world == 1 and not args.no_systems and args.workload == "single_parabolic" and args.rays is None:
-        # the batched and served workloads against the plain per-scene loop (flux maps identical)
-        sys_args = argparse.Namespace(**vars(args))
-        sys_args.steps, sys_args.warmup = 3, 2
-        b = measure_batched(sys_args, local, world)
-        line["batched"] = {
-            "workload": b["config"]["workload"], "rays": b["config"]["rays_total"],
-            "rays_per_s_device": b["value"], "rays_per_s_wall": b["batched_wall_rays_per_s"],
-            "rays_per_s_pipelined": b["batched_pipelined_rays_per_s"],
-            "plain_loop_rays_per_s": b["plain_loop"]["rays_per_s"], "speedup_vs_plain_loop": b["speedup_vs_plain_loop"],
-            "speedup_vs_plain_loop_single_run": b["speedup_vs_plain_loop_single_run"],
-            "flux_counts_mismatching_plain": b["plain_loop"]["flux_counts_mismatching_batched"]
-            + b["pipelined_flux_counts_mismatching"],
-            "tuning_grid": b["config"]["tuning_grid"]}
-        v = measure_served(sys_args, local, world)
-        line["served"] = {
-            "workload": v["config"]["workload"], "requests": v["config"]["requests"], "rays": v["config"]["rays_total"],
-            "saturation_rays_per_s": v["served_saturation"]["rays_per_s"],
-            "plain_loop_saturation_rays_per_s": v["plain_loop_saturation"]["rays_per_s"],
-            "speedup_vs_plain_loop": v["speedup_vs_plain_loop"],
-            "poisson_rate_per_s": v["config"]["arrival_rate_per_s"],
-            "poisson_p50_s": v["served_poisson"]["p50_s"], "poisson_p99_s": v["served_poisson"]["p99_s"],
-            "plain_loop_poisson_p50_s": v["plain_loop_poisson"]["p50_s"],
-            "plain_loop_poisson_p99_s": v["plain_loop_poisson"]["p99_s"],
-            "flux_counts_mismatching_plain": v["plain_loop_saturation"]["flux_counts_mismatching_served"]}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    if pg:
-        pg.barrier()
-        pg.destroy_process_group()
-
-
 def batched_workload(n_instances, n_heliostats):
     """The large field at per-instance sun positions with re-aimed heliostats and log-uniform ray
     counts: (base elements, poses per instance, suns, ray counts)."""
@@ -409,117 +245,15 @@ def batched_workload(n_instances, n_heliostats):
     return base, poses, suns, counts
 
 
-def run_batched(args):
-    rank, world, local = dist_env()
-    line = measure_batched(args, local, world)
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-
-
-def measure_batched(args, local, world):
-    """Batched workload: one csp_batch run (host element builds, upload, device refit, sun planes,
-    one persistent trace launch, flux maps back) against the plain per-scene loop through the
-    drop-in handle (per instance: new poses and sun, update, run, device flux map).  Reported three
-    ways: device time, wall time of one synchronous run, and the completion interval of pipelined
-    runs (run_async / wait: the host builds of a run overlap the device work of the previous one),
-    the headline and the `e2e` value."""
-    import numpy as np
-    import torch
-
-    torch.cuda.set_device(local)
-    from optixsoltracedemos_gb300 import build as nbuild
-    nbuild.build()
-    from optixsoltracedemos_gb300 import native, scenes
-
-    base, poses, suns, counts = batched_workload(args.instances, args.heliostats)
-    total = int(counts.sum())
-    b = native.Batch(local)
-    sid = b.add_scene(base)
-    for i in range(len(suns)):
-        b.add_instance(sid, suns[i], scenes.SUN_PILLBOX, 4.65e-3, int(counts[i]), seed=0, instance=i, poses=poses[i])
-    if args.tuning:
-        b.set_tuning(*[int(x) for x in args.tuning.split(",")])
-    t0 = time.perf_counter()
-    b.run()  # autotune (first run of this scene class) + graph capture
-    first_s = time.perf_counter() - t0
-    for _ in range(max(0, args.warmup - 1)):
-        b.run()
-    clk = ClockSampler(local)
-    clk.start()
-    time.sleep(0.2)
-    wall, dev = [], []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        b.run()
-        wall.append(time.perf_counter() - t0)
-        dev.append(b.timing()[1])
-    batch_counts = [b.counts(i).copy() for i in range(len(suns))]
-    # pipelined: the host builds of run k + 1 overlap the device work of run k; per-run time =
-    # interval between completions
-    b.run_async()
-    piped = []
-    t_prev = None
-    for _ in range(args.steps + 1):
-        b.run_async()
-        b.wait()
-        t = time.perf_counter()
-        if t_prev is not None:
-            piped.append(t - t_prev)
-        t_prev = t
-    b.wait()
-    clocks = clk.stop()
-    piped_mismatch = sum(int(not np.array_equal(b.counts(i), batch_counts[i])) for i in range(len(suns)))
-
-    # plain per-scene loop through the drop-in handle
-    tr = native.Tracer(local, int(counts.max()))
-    tr.set_elements(poses[0])
-    tr.set_sun_vector(suns[0])
-    tr.set_sun_shape(scenes.SUN_PILLBOX, 4.65e-3)
-    tr.initialize()
-    n_plain = len(suns) if args.plain_instances <= 0 else min(len(suns), args.plain_instances)
-    mismatches = 0
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for i in range(n_plain):
-        tr.set_elements(poses[i])
-        tr.set_sun_vector(suns[i])
-        tr.set_num_rays(int(counts[i]))
-        tr.set_seed(0, i)
-        tr.update()
-        tr.run()
-        c, _ = tr.flux_map()
-        mismatches += int(not np.array_equal(c, batch_counts[i]))
-    plain_s = time.perf_counter() - t0
-    plain_rays = int(counts[:n_plain].sum())
-    tr.close()
-    tg, tl = b.tuning(native.GROUP_GRID), b.tuning(native.GROUP_BVH)
-    line = {
-        "metric": METRIC, "value": total / statistics.median(dev), "unit": "rays/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.median(dev) * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"batched_{len(suns)}_instances_large_field_{args.heliostats}_heliostats",
-                   "instances": len(suns), "rays_total": total, "rays_min": int(counts.min()),
-                   "rays_max": int(counts.max()), "flux_grid": [100, 100], "sun": "pillbox 4.65 mrad",
-                   "slope_error_rad": 1.5e-3, "tuning_grid": tg, "tuning_bvh": tl,
-                   "l2_policy": "per-instance scenes and flux maps; no per-ray buffers"},
-        "batched_wall_rays_per_s": total / statistics.median(wall),
-        "batched_wall_ms": statistics.median(wall) * 1e3,
-        "batched_pipelined_rays_per_s": total / statistics.median(piped),
-        "batched_pipelined_ms": statistics.median(piped) * 1e3,
-        "pipelined_flux_counts_mismatching": piped_mismatch,
-        "first_run_s": first_s,
-        "plain_loop": {"rays_per_s": plain_rays / plain_s, "instances": n_plain, "seconds": plain_s,
-                       "flux_counts_mismatching_batched": mismatches},
-        "speedup_vs_plain_loop": (total / statistics.median(piped)) / (plain_rays / plain_s),
-        "speedup_vs_plain_loop_single_run": (total / statistics.median(wall)) / (plain_rays / plain_s),
-        "e2e": {"value": total / statistics.median(piped), "unit": "rays/s",
-                "h2d_bytes_per_step": int(sum(p.nbytes for p in poses)),
-                "d2h_bytes_per_step": int(len(suns) * 100 * 100 * 4)},
-        "gpu_launches": 1 + 1 + 1,
-        "clocks": clocks,
-    }
-    b.close()
-    return line
+def batched_config(n_inst, n_heliostats, counts, extra=None):
+    cfg = {"workload": f"batched_{n_inst}_instances_large_field_{n_heliostats}_heliostats",
+           "instances": n_inst, "rays_total": int(counts.sum()), "rays_min": int(counts.min()),
+           "rays_max": int(counts.max()), "flux_grid": [100, 100], "sun": "pillbox 4.65 mrad, elevation U(10,80) "
+           "azimuth U(-120,120), heliostats re-aimed per instance", "slope_error_rad": 1.5e-3,
+           "l2_policy": "per-instance scene records (~0.5 GB for 256 instances) exceed L2; no per-ray buffers",
+           "parallelism": "replicas"}
+    cfg.update(extra or {})
+    return cfg
 
 
 def served_workload(n_requests, rate):
@@ -550,11 +284,275 @@ def served_workload(n_requests, rate):
     return scene_list, reqs
 
 
-def run_served(args):
-    rank, world, local = dist_env()
-    line = measure_served(args, local, world)
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+def workload_jobs(args):
+    """CPU jobs (elements, sun, shape, param, rays), config and window size of the workload."""
+    from optixsoltracedemos_gb300 import scenes
+    if args.workload == "batched":
+        _, poses, suns, counts = batched_workload(args.instances, args.heliostats)
+        jobs = [(poses[i], suns[i], scenes.SUN_PILLBOX, 4.65e-3, int(counts[i])) for i in range(len(suns))]
+        return jobs, batched_config(len(suns), args.heliostats, counts), 1 << 14
+    if args.workload == "served":
+        _, reqs = served_workload(args.requests, args.rate)
+        jobs = [(p, sun, scenes.SUN_PILLBOX, 4.65e-3, rays) for (_, p, sun, rays, _) in reqs]
+        cfg = {"workload": "served_requests_fields_3_1000_10000_flat_parabolic", "requests": len(reqs),
+               "rays_total": int(sum(j[4] for j in jobs))}
+        return jobs, cfg, 1 << 14
+    sc = make_scene(args.workload, args.rays)
+    jobs = [(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, sc.num_rays)]
+    sample = min(1 << 20, sc.num_rays) if args.workload != "large_field" else 1 << 14
+    return jobs, config(sc), sample
+
+
+def run_reference(args):
+    """The reference algorithm's CPU implementation (oracle port) on all host cores, on the same
+    workload: each step traces one window of rays of the next instance / request / scene."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle
+    oracle.build(with_ref=False)
+    o = oracle.Oracle("f32")
+    cores = os.cpu_count() or 1
+    jobs, cfg, sample = workload_jobs(args)
+
+    def step(k):
+        el, sun, shape, param, n = jobs[k % len(jobs)]
+        first = ((k // len(jobs)) * sample) % max(1, n - sample + 1)
+        o.trace(el, sun, shape, param, first_ray=first, count=sample, nthreads=cores, with_ids=False)
+
+    for w in range(args.warmup):
+        step(w)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        step(k)
+    dt = time.perf_counter() - t0
+    v = args.steps * sample / dt
+    what = (f"each step traces {sample} rays of the next instance / request (brute-force closest hit over its "
+            f"elements)" if args.workload in ("batched", "served") else f"each step traces {sample} rays of the scene")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "rays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": cfg,
+            "cpu_baseline": {"value": v, "unit": "rays/s", "cores": cores, "kind": "port",
+                             "sample": f"{what} (oracle port of the reference algorithm, OpenMP over {cores} threads)"},
+            "e2e": {"value": v, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def measure_plain(args, sc, local, world, pg, steps, warmup, e2e_steps, accuracy, cpu_seconds):
+    """Plain trace of one scene: K launches with the scene resident (CUDA events on the launching
+    stream), the end-to-end rate through the C ABI with host buffers, the HBM roofline of the dense
+    record stream, and the flux-map L2 against the FP64 oracle."""
+    import torch
+    from optixsoltracedemos_gb300 import native
+    from optixsoltracedemos_gb300.flux import flux_map_from_hits, flux_l2
+
+    rank = int(os.environ.get("RANK", "0"))
+    N = sc.num_rays
+    tr = native.tracer_for(sc, device=local, record_ids=False)
+    stream = torch.cuda.Stream(device=local)
+    sp = stream.cuda_stream
+    for w in range(warmup):
+        tr.set_seed(w)
+        tr.trace_async(sp)
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    time.sleep(0.3)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for k in range(steps):
+        tr.set_seed(1000 + k, rank)  # each replica traces its own rays (Philox instance = rank)
+        starts[k].record(stream)
+        tr.trace_async(sp)
+        ends[k].record(stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    total_s = max_over_ranks(e0.elapsed_time(e1) * 1e-3, pg, f"cuda:{local}")
+    launch_s = statistics.mean(s.elapsed_time(e) for s, e in zip(starts, ends)) * 1e-3
+    peak, peak_kind, _ = peaks()
+    achieved = BYTES_PER_RAY * N / launch_s / 1e9
+    line = {
+        "metric": METRIC, "value": world * N * steps / total_s, "unit": "rays/s", "n_gpus": world, "steps": steps,
+        "warmup": warmup, "ms_per_step": total_s / steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config(sc),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": NCU_TRAFFIC_PER_LAUNCH if (N == 1 << 24 and sc.name == "single_parabolic") else None,
+                     "peak_source": peak_kind, "algorithmic_bytes_per_launch": BYTES_PER_RAY * N,
+                     "launch_ms": launch_s * 1e3},
+        "gpu_launches": steps, "clocks": clocks,
+    }
+    host = None
+    if e2e_steps > 0:
+        # end to end through the C ABI with host buffers: element list up, every record down
+        host = torch.empty(N * 5 * 4, dtype=torch.float32, pin_memory=True)
+        elements = sc.elements.copy()
+        for _ in range(2):
+            tr.set_elements(elements)
+            tr.update()
+            tr.run_to_host_ptr(host.data_ptr())
+        if pg:
+            pg.barrier()
+        t0 = time.perf_counter()
+        for k in range(e2e_steps):
+            tr.set_seed(5000 + k, rank)
+            tr.set_elements(elements)
+            tr.update()
+            tr.run_to_host_ptr(host.data_ptr())
+        e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, pg, f"cuda:{local}")
+        line["e2e"] = {"value": world * N / e2e_s, "unit": "rays/s", "h2d_bytes_per_step": int(elements.nbytes + 3 * 8),
+                       "d2h_bytes_per_step": int(N * BYTES_PER_RAY)}
+    if rank == 0 and world == 1 and accuracy and host is not None:
+        try:
+            from oracle import oracle
+            oracle.build(with_ref=False)
+            tr.set_seed(0)
+            hits = host.numpy().reshape(N, 5, 4)
+            tr.run_to_host(hits.reshape(-1))
+            o64 = oracle.Oracle("f64")
+            oh, _ = o64.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, count=N, with_ids=False)
+            line["flux_l2_vs_fp64"] = flux_l2(flux_map_from_hits(hits, sc.elements[-1], N),
+                                              flux_map_from_hits(oh, sc.elements[-1], N))
+            del oh
+        except Exception as exc:  # accuracy is reported, not required for the timing line
+            line["flux_l2_vs_fp64"] = f"unavailable: {exc}"
+    if rank == 0 and world == 1 and cpu_seconds > 0:
+        sample = min(1 << 20, N) if len(sc.elements) < 64 else 1 << 12
+        line["cpu_baseline"] = cpu_baseline(cpu_seconds, [(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, N)],
+                                            sample, sc.name)
+    tr.close()
+    return line
+
+
+def measure_batched(args, local, world, pg=None):
+    """Batched workload through csp_batch: K synchronous runs (device time of refit, sun planes and
+    trace per run, CUDA events inside the run's graph), K pipelined runs from host poses to host
+    flux maps (run_async / wait: the host builds of one run overlap the device work of the
+    previous one), and the plain per-scene loop through the drop-in handle (per instance: new poses
+    and sun, csp_update, csp_run, csp_flux_map) on the same instances, flux maps compared."""
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local)
+    from optixsoltracedemos_gb300 import native, scenes
+
+    base, poses, suns, counts = batched_workload(args.instances, args.heliostats)
+    total = int(counts.sum())
+    steps, warmup = args.steps, max(1, args.warmup)
+    b = native.Batch(local)
+    sid = b.add_scene(base)
+    rank = int(os.environ.get("RANK", "0"))
+    for i in range(len(suns)):
+        b.add_instance(sid, suns[i], scenes.SUN_PILLBOX, 4.65e-3, int(counts[i]), seed=rank, instance=i,
+                       poses=poses[i])
+    if args.tuning:
+        b.set_tuning(*[int(x) for x in args.tuning.split(",")])
+    t0 = time.perf_counter()
+    b.run()  # autotune (first run of this scene class) + graph capture
+    first_s = time.perf_counter() - t0
+    for _ in range(warmup - 1):
+        b.run()
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    time.sleep(0.2)
+    wall, dev = [], []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        b.run()
+        wall.append(time.perf_counter() - t0)
+        dev.append(b.timing()[1])
+    torch.cuda.synchronize()
+    batch_counts = [b.counts(i).copy() for i in range(len(suns))]
+    # pipelined from host memory: K runs, first submission to last completion
+    if pg:
+        pg.barrier()
+    t0 = time.perf_counter()
+    b.run_async()
+    for _ in range(steps - 1):
+        b.run_async()
+        b.wait()
+    b.wait()
+    piped_s = time.perf_counter() - t0
+    clocks = clk.stop()
+    h2d, d2h = b.transfer()
+    piped_mismatch = sum(int(not np.array_equal(b.counts(i), batch_counts[i])) for i in range(len(suns)))
+    dev_s = max_over_ranks(sum(dev), pg, f"cuda:{local}")
+    piped_s = max_over_ranks(piped_s, pg, f"cuda:{local}")
+
+    # plain per-scene loop through the drop-in handle
+    tr = native.Tracer(local, int(counts.max()))
+    tr.set_elements(poses[0])
+    tr.set_sun_vector(suns[0])
+    tr.set_sun_shape(scenes.SUN_PILLBOX, 4.65e-3)
+    tr.initialize()
+    n_plain = len(suns) if args.plain_instances <= 0 else min(len(suns), args.plain_instances)
+    mismatches = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(n_plain):
+        tr.set_elements(poses[i])
+        tr.set_sun_vector(suns[i])
+        tr.set_num_rays(int(counts[i]))
+        tr.set_seed(rank, i)
+        tr.update()
+        tr.run()
+        c, _ = tr.flux_map()
+        mismatches += int(not np.array_equal(c, batch_counts[i]))
+    plain_s = time.perf_counter() - t0
+    plain_rays = int(counts[:n_plain].sum())
+    tr.close()
+    tg, tl = b.tuning(native.GROUP_GRID), b.tuning(native.GROUP_BVH)
+    b.close()
+
+    value = world * total * steps / dev_s
+    _, _, sm_mhz = peaks()
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    issue_peak = sms * ISSUE_PER_SM_PER_CYCLE * sm_mhz * 1e6
+    per_gpu = value / world
+    roof = {"bound": "issue", "unit": "warp-inst/s", "peak": issue_peak,
+            "peak_source": f"{sms} SMs x {ISSUE_PER_SM_PER_CYCLE} schedulers x {sm_mhz:.0f} MHz",
+            "launch_ms": statistics.mean(dev) * 1e3, "rays_per_launch": total}
+    if BATCH_WARP_INST_PER_RAY is not None:
+        roof.update({"achieved": BATCH_WARP_INST_PER_RAY * per_gpu, "frac": BATCH_WARP_INST_PER_RAY * per_gpu / issue_peak,
+                     "warp_inst_per_ray": BATCH_WARP_INST_PER_RAY})
+    else:
+        roof.update({"achieved": None, "frac": None})
+    if BATCH_DRAM_BYTES_PER_RAY is not None:
+        hbm, _, _ = peaks()
+        roof.update({"traffic": BATCH_DRAM_BYTES_PER_RAY * total,
+                     "hbm_frac": BATCH_DRAM_BYTES_PER_RAY * per_gpu / 1e9 / hbm})
+    else:
+        roof["traffic"] = None
+    line = {
+        "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world,
+        "steps": steps, "warmup": warmup, "ms_per_step": dev_s / steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": batched_config(len(suns), args.heliostats, counts, {"tuning_grid": tg, "tuning_bvh": tl}),
+        "roofline": roof,
+        "e2e": {"value": world * total * steps / piped_s, "unit": "rays/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h),
+                "path": "csp_batch_run_async / csp_batch_wait from host pose arrays to host flux maps, pipelined"},
+        "gpu_launches": 3 * steps,
+        "clocks": clocks,
+        "batched_wall_rays_per_s": world * total / max_over_ranks(statistics.median(wall), pg, f"cuda:{local}"),
+        "pipelined_flux_counts_mismatching": piped_mismatch,
+        "first_run_s": first_s,
+        "plain_loop": {"rays_per_s": plain_rays / plain_s, "instances": n_plain, "seconds": plain_s,
+                       "flux_counts_mismatching_batched": mismatches,
+                       "path": "drop-in handle per instance: csp_set_elements, csp_update, csp_run, csp_flux_map"},
+        "speedup_vs_plain_loop": (total * steps / piped_s) / (plain_rays / plain_s),
+        "speedup_vs_plain_loop_device": (total * steps / sum(dev)) / (plain_rays / plain_s),
+    }
+    return line
 
 
 def measure_served(args, local, world):
@@ -566,8 +564,6 @@ def measure_served(args, local, world):
     import torch
 
     torch.cuda.set_device(local)
-    from optixsoltracedemos_gb300 import build as nbuild
-    nbuild.build()
     from optixsoltracedemos_gb300 import native, scenes
 
     scene_list, reqs = served_workload(args.requests, args.rate)
@@ -669,14 +665,79 @@ def measure_served(args, local, world):
     return line
 
 
+def _plain_summary(line):
+    keep = ("value", "ms_per_step", "roofline", "e2e", "flux_l2_vs_fp64", "cpu_baseline", "clocks")
+    out = {"workload": line["config"]["workload"], "rays": line["config"]["rays"], "unit": "rays/s"}
+    out.update({k: line[k] for k in keep if k in line})
+    out["rays_per_s"] = out.pop("value")
+    return out
+
+
+def _served_summary(v):
+    return {"workload": v["config"]["workload"], "requests": v["config"]["requests"], "rays": v["config"]["rays_total"],
+            "saturation_rays_per_s": v["served_saturation"]["rays_per_s"],
+            "plain_loop_saturation_rays_per_s": v["plain_loop_saturation"]["rays_per_s"],
+            "speedup_vs_plain_loop": v["speedup_vs_plain_loop"], "poisson_rate_per_s": v["config"]["arrival_rate_per_s"],
+            "poisson_p50_s": v["served_poisson"]["p50_s"], "poisson_p99_s": v["served_poisson"]["p99_s"],
+            "plain_loop_poisson_p50_s": v["plain_loop_poisson"]["p50_s"],
+            "plain_loop_poisson_p99_s": v["plain_loop_poisson"]["p99_s"],
+            "flux_counts_mismatching_plain": v["plain_loop_saturation"]["flux_counts_mismatching_served"]}
+
+
+def run_ours(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        pg = dist
+
+    from optixsoltracedemos_gb300 import build as nbuild
+    if rank == 0:
+        nbuild.build()
+    if pg:
+        pg.barrier()
+    from optixsoltracedemos_gb300 import native
+    native.load()
+
+    solo = rank == 0 and world == 1
+    if args.workload == "batched":
+        line = measure_batched(args, local, world, pg)
+        if solo and not args.no_cpu_baseline:
+            jobs, _, sample = workload_jobs(args)
+            line["cpu_baseline"] = cpu_baseline(args.cpu_seconds, jobs, sample, line["config"]["workload"])
+        if world == 1 and not args.no_systems:
+            sub = argparse.Namespace(**vars(args))
+            sc = make_scene("single_parabolic", None)
+            line["single_parabolic"] = _plain_summary(measure_plain(
+                sub, sc, local, world, pg, steps=200, warmup=10, e2e_steps=5, accuracy=not args.no_accuracy,
+                cpu_seconds=0.0 if args.no_cpu_baseline else 3.0))
+            sc = make_scene("large_field", None)
+            line["large_field"] = _plain_summary(measure_plain(
+                sub, sc, local, world, pg, steps=5, warmup=3, e2e_steps=0, accuracy=False, cpu_seconds=0.0))
+            line["served"] = _served_summary(measure_served(sub, local, world))
+    elif args.workload == "served":
+        line = measure_served(args, local, world)
+    else:
+        sc = make_scene(args.workload, args.rays)
+        e2e_steps = args.e2e_steps if sc.num_rays <= (1 << 26) else 0
+        line = measure_plain(args, sc, local, world, pg, args.steps, args.warmup, e2e_steps,
+                             not args.no_accuracy and sc.num_rays <= (1 << 24),
+                             0.0 if args.no_cpu_baseline else args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload == "batched":
-        run_batched(args)
-    elif args.workload == "served":
-        run_served(args)
     else:
         run_ours(args)
 

@@ -65,7 +65,15 @@ typedef enum csp_status {
 /* SurfaceType / ApertureType values of lib/soltrace_type.h:4-15 */
 enum { CSP_SURFACE_FLAT = 0, CSP_SURFACE_PARABOLIC = 1, CSP_SURFACE_CYLINDER = 3 };
 enum { CSP_APERTURE_RECTANGLE = 0, CSP_APERTURE_CIRCLE = 1 };
-enum { CSP_SUN_PILLBOX = 0, CSP_SUN_GAUSSIAN = 1 };
+/* Sun shape of a trace: CSP_SUN_PILLBOX or CSP_SUN_GAUSSIAN, optionally OR-ed with the
+ * CSP_SUN_ACCURATE flag (see csp_set_sun_shape). */
+enum {
+    CSP_SUN_PILLBOX = 0,
+    CSP_SUN_GAUSSIAN = 1,
+    CSP_SUN_ACCURATE = 2,
+    CSP_SUN_PILLBOX_ACCURATE = CSP_SUN_PILLBOX | CSP_SUN_ACCURATE,
+    CSP_SUN_GAUSSIAN_ACCURATE = CSP_SUN_GAUSSIAN | CSP_SUN_ACCURATE
+};
 
 /* One optical element, as the reference's Element holds it (lib/element.h:41-102): origin, aim
  * point, z rotation in degrees, rectangular aperture (for a cylinder: width = 2 * radius, height =
@@ -102,8 +110,17 @@ CSP_API int csp_set_elements(csp_handle h, const csp_element* elements, uint32_t
 CSP_API int csp_get_num_elements(csp_handle h, uint32_t* count);
 CSP_API int csp_get_elements(csp_handle h, csp_element* out, uint32_t capacity);
 CSP_API int csp_set_sun_vector(csp_handle h, double x, double y, double z);
-/* shape CSP_SUN_PILLBOX: param = half angle (rad), the reference's max_sun_angle;
- * shape CSP_SUN_GAUSSIAN: param = sigma (rad) per tangent-plane axis (extension). */
+/* shape CSP_SUN_PILLBOX: param = half angle (rad), the reference's max_sun_angle, sampled with the
+ *   reference's float formula z = cos(angle) + (1 - cos(angle)) r (cuda/sun.cu:82-86);
+ * shape CSP_SUN_GAUSSIAN: param = sigma (rad) per tangent-plane axis (extension).
+ * Flag CSP_SUN_ACCURATE (extension): the same scene, sun and random draws traced with two float
+ * formulas of the reference replaced by cancellation-free ones -- the pillbox cone carries
+ * 1 - z = (1 - cos(angle)) (1 - r) with 1 - cos(angle) = 2 sin^2(angle / 2) (the reference's float z
+ * quantizes 1 - z in steps of 2^-24, ~2e-4 rad of direction error at 4.65 mrad), and the cylinder
+ * receiver's side roots come from the ray's closest approach to its axis (the reference's
+ * B^2 - 4AC cancels for rays that start hundreds of metres away, ~1 mm on the hit point).  Records
+ * then differ from the reference's float trace by the rounding removed; flux maps agree with the
+ * FP64 oracle to well under 1 %.  Without the flag the trace is the reference's, bit for bit. */
 CSP_API int csp_set_sun_shape(csp_handle h, int shape, double param_rad);
 /* Philox key of the random draws (seed) and the instance word of their counter. */
 CSP_API int csp_set_seed(csp_handle h, uint64_t seed, uint32_t instance);
@@ -153,7 +170,8 @@ CSP_API int csp_trace_into(csp_handle h, void* hits, void* ids, uint64_t first_r
  * intermediate data live in a fixed 4 KB device array inside the library (held on every device that
  * uses it until the library is unloaded); every call overwrites it fully, and calls whose work
  * overlaps on the GPU (different streams or host threads) race on it.  The first call on a device
- * looks up that array's address; make it before any stream capture.  More than 8 elements is
+ * looks up that array's address; make it before any stream capture, and do not reset the device
+ * after it (the address is kept for the life of the process).  More than 8 elements is
  * rejected with CSP_ERR_INVALID_ARGUMENT.  No host synchronisation. */
 CSP_API int csp_trace_noalloc(int device, const csp_element* elements, uint32_t count, const double* sun_dir,
                               int sun_shape, double sun_param, uint64_t seed, uint32_t instance, uint64_t first_ray,
@@ -262,6 +280,9 @@ CSP_API int csp_batch_get_stats(csp_batch b, uint32_t index, uint64_t* stats);
 CSP_API int csp_batch_get_sun_plane(csp_batch b, uint32_t index, float* out);
 /* setup_s: host element builds and upload; trace_s: device time of refit + sun planes + trace. */
 CSP_API int csp_batch_get_timing(csp_batch b, double* setup_s, double* trace_s);
+/* Bytes the last completed run copied host to device (the staging image: element records, grids,
+ * launch descriptors) and device to host (flux maps, counters, sun frames). */
+CSP_API int csp_batch_get_transfer(csp_batch b, uint64_t* h2d_bytes, uint64_t* d2h_bytes);
 
 /* ---- Serving: a request loop with continuous batching ----
  * A server owns one worker thread, one CUDA stream and a device-memory arena of memory_budget

@@ -47,6 +47,9 @@ public:
     void set_seed(uint64_t seed, uint32_t instance = 0);
     // Gaussian sun of per-axis sigma (rad) instead of the pillbox of set_sun_angle
     void set_sun_shape_gaussian(double sigma_rad);
+    // trace in the cancellation-free float formulas (CSP_SUN_ACCURATE: cone sampler, cylinder
+    // roots) instead of the reference's; false (the default) traces the reference's arithmetic
+    void set_accurate_arithmetic(bool enable);
     void set_record_element_ids(bool enable);
     const std::vector<std::shared_ptr<Element>>& get_elements() const { return m_element_list; }
     uint64_t get_num_rays() const { return m_num_sunpoints; }
@@ -64,6 +67,7 @@ private:
     Vector3d m_sun_vector{0.0, 0.0, 1.0};
     double m_sun_angle = 0.0;
     int m_sun_shape = CSP_SUN_PILLBOX;
+    bool m_accurate = false;
     double m_sun_sigma = 0.0;
     std::vector<std::shared_ptr<Element>> m_element_list;
     Timer m_timer_setup, m_timer_trace;

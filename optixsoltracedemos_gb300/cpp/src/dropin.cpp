@@ -119,8 +119,10 @@ void SolTraceSystem::push_scene() {
     for (const auto& e : m_element_list) el.push_back(e->to_csp_element());
     check(csp_set_elements(m_handle, el.data(), (uint32_t)el.size()), "csp_set_elements");
     check(csp_set_sun_vector(m_handle, m_sun_vector[0], m_sun_vector[1], m_sun_vector[2]), "csp_set_sun_vector");
-    if (m_sun_shape == CSP_SUN_GAUSSIAN) check(csp_set_sun_shape(m_handle, CSP_SUN_GAUSSIAN, m_sun_sigma), "sun shape");
-    else check(csp_set_sun_shape(m_handle, CSP_SUN_PILLBOX, m_sun_angle), "sun shape");
+    const int flags = m_accurate ? CSP_SUN_ACCURATE : 0;
+    if (m_sun_shape == CSP_SUN_GAUSSIAN)
+        check(csp_set_sun_shape(m_handle, CSP_SUN_GAUSSIAN | flags, m_sun_sigma), "sun shape");
+    else check(csp_set_sun_shape(m_handle, CSP_SUN_PILLBOX | flags, m_sun_angle), "sun shape");
 }
 
 void SolTraceSystem::initialize() {
@@ -229,6 +231,8 @@ void SolTraceSystem::set_sun_shape_gaussian(double sigma_rad) {
     m_sun_shape = CSP_SUN_GAUSSIAN;
     m_sun_sigma = sigma_rad;
 }
+
+void SolTraceSystem::set_accurate_arithmetic(bool enable) { m_accurate = enable; }
 
 void SolTraceSystem::set_record_element_ids(bool enable) {
     if (!m_handle) throw std::runtime_error("SolTraceSystem used after clean_up()");

@@ -153,7 +153,7 @@ int Batch::add_instance(const BInst& bi, uint32_t* index) {
             if (bi.poses[k].surface != s.elements[k].surface || bi.poses[k].aperture != s.elements[k].aperture)
                 return set_error(CSP_ERR_BAD_SCENE, "instance pose " + std::to_string(k) + " changes the surface type");
     }
-    if (bi.shape != CSP_SUN_PILLBOX && bi.shape != CSP_SUN_GAUSSIAN)
+    if (!valid_sun_shape(bi.shape))
         return set_error(CSP_ERR_INVALID_ARGUMENT, "unknown sun shape");
     if (!(bi.param >= 0.0) || bi.param > 0.5) return set_error(CSP_ERR_INVALID_ARGUMENT, "sun shape parameter out of range");
     if (bi.rays >= (1ull << 40)) return set_error(CSP_ERR_INVALID_ARGUMENT, "too many rays for one instance");
@@ -337,7 +337,7 @@ void Batch::fill_instance(size_t i) {
     sj.sx = sv[0];
     sj.sy = sv[1];
     sj.sz = sv[2];
-    sj.tan_pad = tanf((float)(b.shape == CSP_SUN_GAUSSIAN ? 5.0 * b.param : b.param));
+    sj.tan_pad = tanf((float)sun_pad_angle(b.shape, b.param));
     sj.shape = b.shape;
     sj.param = (float)b.param;
     sj.out = reinterpret_cast<SunFrame*>(d_arena + p.sun);
@@ -636,6 +636,8 @@ int Batch::run_async() {
     S.nx = nx;
     S.ny = ny;
     S.time_setup = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    S.up_bytes = up_bytes;
+    S.res_bytes = res_bytes;
     if ((rc = cuda_status(cudaGraphLaunch(S.graph, stream), "cudaGraphLaunch"))) return rc;
     if ((rc = cuda_status(cudaEventRecord(S.done, stream), "cudaEventRecord"))) return rc;
     flight.push_back(si);
@@ -653,6 +655,8 @@ int Batch::wait() {
     if ((rc = cuda_status(cudaEventElapsedTime(&ms, S.ev0, S.ev1), "batch timing"))) return rc;
     time_trace = ms * 1e-3;
     time_setup = S.time_setup;
+    last_up = S.up_bytes;
+    last_res = S.res_bytes;
     cur = si;
     return CSP_OK;
 }
@@ -844,6 +848,14 @@ int csp_batch_get_timing(csp_batch bh, double* setup_s, double* trace_s) {
     const Batch* b = reinterpret_cast<Batch*>(bh);
     if (setup_s) *setup_s = b->time_setup;
     if (trace_s) *trace_s = b->time_trace;
+    return CSP_OK;
+}
+
+int csp_batch_get_transfer(csp_batch bh, uint64_t* h2d_bytes, uint64_t* d2h_bytes) {
+    CSP_BGUARD(bh);
+    const Batch* b = reinterpret_cast<Batch*>(bh);
+    if (h2d_bytes) *h2d_bytes = b->last_up;
+    if (d2h_bytes) *d2h_bytes = b->last_res;
     return CSP_OK;
 }
 

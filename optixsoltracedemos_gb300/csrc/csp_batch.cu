@@ -8,6 +8,7 @@
 // optixLaunch of lib/soltrace_system.cpp:145-170 with the flux binning of
 // scripts/post_processing/flux_map_calculator.py:135-179 moved into the closest-hit stage.
 #include <algorithm>
+#include <atomic>
 
 #include "csp_kernels.cuh"
 #include "csp_trace.cuh"
@@ -170,10 +171,18 @@ constexpr size_t batch_smem() {
     return sizeof(BatchSmem<kB, kAccel>);
 }
 
+// Occupancy limit on the current device; the shared-memory attribute is set (and the limit
+// computed) once per device.
 template <int kB, int kAccel>
 int occupancy_t() {
-    static int cached = -1;
-    if (cached >= 0) return cached;
+    constexpr int kMaxDevices = 64;
+    static std::atomic<int> cached[kMaxDevices];  // 0 = not yet known (a kernel that fits has >= 1)
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (dev >= 0 && dev < kMaxDevices) {
+        const int c = cached[dev].load(std::memory_order_acquire);
+        if (c > 0) return c;
+    }
     if (cudaFuncSetAttribute(batch_kernel<kB, kAccel>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)batch_smem<kB, kAccel>()) != cudaSuccess)
         return 0;
@@ -181,7 +190,7 @@ int occupancy_t() {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<kB, kAccel>, kB, batch_smem<kB, kAccel>()) !=
         cudaSuccess)
         return 0;
-    cached = per_sm;
+    if (dev >= 0 && dev < kMaxDevices && per_sm > 0) cached[dev].store(per_sm, std::memory_order_release);
     return per_sm;
 }
 

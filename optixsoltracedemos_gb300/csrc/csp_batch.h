@@ -66,6 +66,7 @@ struct RunSlot {
     size_t res_off = 0;
     uint32_t nx = 0, ny = 0;
     double time_setup = 0.0;
+    size_t up_bytes = 0, res_bytes = 0;  // host-to-device and device-to-host bytes of the run
 };
 
 struct Batch {
@@ -95,6 +96,7 @@ struct Batch {
     int max_nodes = 0;
 
     double time_setup = 0.0, time_trace = 0.0;  // of the last completed run
+    size_t last_up = 0, last_res = 0;            // its transfer sizes
 
     ~Batch();
     void release();

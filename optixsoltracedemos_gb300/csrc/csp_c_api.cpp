@@ -136,9 +136,7 @@ int System::upload_grid(bool arrays) {
 }
 
 float System::pad_angle() const {
-    // the reference pads the sun plane by the pillbox half angle (lib/geometry_manager.cpp:129);
-    // the Gaussian sun pads by 5 sigma
-    return (float)(sun_shape == CSP_SUN_GAUSSIAN ? 5.0 * sun_param : sun_param);
+    return (float)sun_pad_angle(sun_shape, sun_param);
 }
 
 int System::prepare_sun() {
@@ -362,6 +360,7 @@ int csp_create(csp_handle* out, int device, uint64_t num_rays) {
     cudaError_t e = cudaGetDeviceCount(&count);
     if (e != cudaSuccess) return csp::cuda_status(e, "cudaGetDeviceCount");
     if (device < 0 || device >= count) return fail(CSP_ERR_INVALID_ARGUMENT, "no such CUDA device");
+    if (!csp::valid_ray_window(0, num_rays)) return fail(CSP_ERR_INVALID_ARGUMENT, "num_rays must stay below 2^56");
     System* s = new (std::nothrow) System();
     if (!s) return fail(CSP_ERR_OUT_OF_MEMORY, "host allocation failed");
     s->device = device;
@@ -378,6 +377,7 @@ int csp_destroy(csp_handle h) {
 
 int csp_set_num_rays(csp_handle h, uint64_t num_rays) {
     CSP_GUARD(h);
+    if (!csp::valid_ray_window(0, num_rays)) return fail(CSP_ERR_INVALID_ARGUMENT, "num_rays must stay below 2^56");
     reinterpret_cast<System*>(h)->num_rays = num_rays;
     return CSP_OK;
 }
@@ -423,7 +423,7 @@ int csp_set_sun_vector(csp_handle h, double x, double y, double z) {
 
 int csp_set_sun_shape(csp_handle h, int shape, double param) {
     CSP_GUARD(h);
-    if (shape != CSP_SUN_PILLBOX && shape != CSP_SUN_GAUSSIAN) return fail(CSP_ERR_INVALID_ARGUMENT, "unknown sun shape");
+    if (!csp::valid_sun_shape(shape)) return fail(CSP_ERR_INVALID_ARGUMENT, "unknown sun shape");
     if (!(param >= 0.0) || param > 0.5) return fail(CSP_ERR_INVALID_ARGUMENT, "sun shape parameter out of range");
     System* s = reinterpret_cast<System*>(h);
     s->sun_shape = shape;
@@ -512,6 +512,8 @@ int csp_trace_into(csp_handle h, void* hits, void* ids, uint64_t first, uint64_t
     System* s = reinterpret_cast<System*>(h);
     if (!s->initialized) return fail(CSP_ERR_STATE, "trace before initialize()");
     if (!hits && count) return fail(CSP_ERR_INVALID_ARGUMENT, "null hit buffer");
+    if (!csp::valid_ray_window(first, count))
+        return fail(CSP_ERR_INVALID_ARGUMENT, "ray window [first_ray, first_ray + count) must stay below 2^56");
     csp::TraceArgs a = s->args(0, 0);
     a.hits = reinterpret_cast<float4*>(hits);
     a.ids = reinterpret_cast<uint32_t*>(ids);

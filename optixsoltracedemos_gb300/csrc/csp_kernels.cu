@@ -15,6 +15,7 @@
 //                        (scripts/post_processing/flux_map_calculator.py:135-179)
 // The device functions of the path live in csp_trace.cuh.
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 
 #include "csp_kernels.cuh"
@@ -70,11 +71,13 @@ cudaError_t launch_trace_t(const TraceArgs& args, cudaStream_t stream) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    static bool attr_set = false;  // per process; the attribute belongs to the function
-    if (e == cudaSuccess && !attr_set) {
+    // the attribute is set once per device (bit `dev` of the mask; devices past 63 set it every time)
+    static std::atomic<unsigned long long> attr_set{0};
+    const unsigned long long bit = (dev >= 0 && dev < 64) ? 1ull << dev : 0ull;
+    if (e == cudaSuccess && !(bit && (attr_set.load(std::memory_order_acquire) & bit))) {
         e = cudaFuncSetAttribute(trace_kernel<kAccel>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)sizeof(TraceSmem<kAccel>));
-        attr_set = (e == cudaSuccess);
+        if (e == cudaSuccess) attr_set.fetch_or(bit, std::memory_order_acq_rel);
     }
     if (e == cudaSuccess)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel<kAccel>, kTraceBlock,

@@ -15,10 +15,13 @@
 // it completely before the kernels read it, so nothing carries over from one call to the next; two
 // calls whose work overlaps on the GPU (different streams, or different host threads) race on it.
 // The first call on a device looks up the array's device address (cudaGetSymbolAddress) with that
-// device current; make that first call before any stream capture.
+// device current; make that first call before any stream capture.  The address is kept for the
+// life of the process, so resetting a device (cudaDeviceReset, or anything else that destroys its
+// primary context) after that first call is not supported: later calls would use a stale address.
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <string>
 
 #include "csp_c_api.h"
 #include "csp_kernels.cuh"
@@ -72,80 +75,23 @@ int scratch_address(int device, unsigned char** out) {
     return CSP_OK;
 }
 
-inline float3 f3d(double x, double y, double z) { return make_float3((float)x, (float)y, (float)z); }
-
-// Element records of a scene of at most kNoAllocMaxElements elements, packed in the scratch layout,
-// with the same arithmetic as the scene builder used by csp_initialize (entity types of
-// lib/geometry_manager.cpp:50-90, geometry of lib/element.cpp:114-164 and the GeometryDataST
-// constructors); the nodes are the element list itself, one leaf per element in element order.
+// Element records of a scene of at most kNoAllocMaxElements elements, packed in the scratch layout
+// by the scene builder's own per-element packing (pack_element, the one csp_initialize uses); the
+// nodes are the element list itself, one leaf per element in element order.
 int pack_records(const csp_element* el, uint32_t n, unsigned char* block) {
     Node* nodes = reinterpret_cast<Node*>(block + kOffNodes);
     Prim* prims = reinterpret_cast<Prim*>(block + kOffPrims);
     Optics* optics = reinterpret_cast<Optics*>(block + kOffOptics);
     Aabb* aabbs = reinterpret_cast<Aabb*>(block + kOffAabbs);
     for (uint32_t i = 0; i < n; ++i) {
-        const csp_element& e = el[i];
-        const bool last = (i + 1 == n);
-        if (e.aperture != CSP_APERTURE_RECTANGLE || !(e.width > 0) || !(e.height > 0))
-            return set_error(CSP_ERR_BAD_SCENE, "csp_trace_noalloc: elements need a rectangular aperture of positive size");
-        uint32_t type;
-        if (e.surface == CSP_SURFACE_FLAT) type = last ? kFlatReceiver : kFlatMirror;
-        else if (e.surface == CSP_SURFACE_PARABOLIC) type = kParabolicMirror;
-        else if (e.surface == CSP_SURFACE_CYLINDER && last) type = kCylReceiver;
-        else return set_error(CSP_ERR_BAD_SCENE, "csp_trace_noalloc: unsupported surface, or a cylinder that is not last");
-        double G[9], euler[3], lo[3], hi[3];
-        element_frame(e, euler, G, lo, hi);
-        const double w = e.width, h = e.height;
-        Aabb& box = aabbs[i];
-        box.lo = make_float4((float)lo[0], (float)lo[1], (float)lo[2], 0.f);
-        box.hi = make_float4((float)hi[0], (float)hi[1], (float)hi[2], 0.f);
-        Prim& p = prims[i];
-        if (e.surface == CSP_SURFACE_FLAT) {
-            const float3 center = f3d(e.origin[0], e.origin[1], e.origin[2]);
-            const float3 x = f3d(G[0], G[1], G[2]), y = f3d(G[3], G[4], G[5]);
-            const float fw = (float)w, fh = (float)h;
-            const float3 nrm = normalize(cross(x, y));
-            const float pw = dot(nrm, center);
-            p.a = make_float4(nrm.x, nrm.y, nrm.z, pw);
-            p.b = make_float4(center.x, center.y, center.z, fw / 2);
-            p.c = make_float4(x.x, x.y, x.z, fh / 2);
-            p.d = make_float4(y.x, y.y, y.z, 0.f);
-        } else if (e.surface == CSP_SURFACE_PARABOLIC) {
-            const double sw = (double)(float)(-w), sh = (double)(float)h;
-            const double v1[3] = {G[0] * sw, G[1] * sw, G[2] * sw}, v2[3] = {G[3] * sh, G[4] * sh, G[5] * sh};
-            float3 fv1 = f3d(v1[0], v1[1], v1[2]), fv2 = f3d(v2[0], v2[1], v2[2]);
-            const float3 anchor = f3d(e.origin[0] - v1[0] * 0.5 - v2[0] * 0.5, e.origin[1] - v1[1] * 0.5 - v2[1] * 0.5,
-                                      e.origin[2] - v1[2] * 0.5 - v2[2] * 0.5);
-            const float i1 = 1.0f / dot(fv1, fv1), i2 = 1.0f / dot(fv2, fv2);
-            fv1 = make_float3(fv1.x * i1, fv1.y * i1, fv1.z * i1);
-            fv2 = make_float3(fv2.x * i2, fv2.y * i2, fv2.z * i2);
-            const float L1 = 1.0f / length(fv1), L2 = 1.0f / length(fv2);
-            const float3 e1 = scale(L1, fv1), e2 = scale(L2, fv2);
-            const float3 nn = normalize(cross(e2, e1));
-            const float3 rc = add(add(anchor, scale(L1 / 2.0f, e1)), scale(L2 / 2.0f, e2));
-            p.a = make_float4(e1.x, e1.y, e1.z, L1 / 2.0f);
-            p.b = make_float4(e2.x, e2.y, e2.z, L2 / 2.0f);
-            p.c = make_float4(nn.x, nn.y, nn.z, (float)e.curv_x);
-            p.d = make_float4(rc.x, rc.y, rc.z, (float)e.curv_y);
-        } else {
-            const float radius = (float)w / 2.0f, half = (float)h / 2.0f;
-            const float3 center = f3d(e.origin[0], e.origin[1], e.origin[2]);
-            const float3 bx = f3d(G[0], G[1], G[2]), bz = f3d(G[6], G[7], G[8]);
-            const float3 ly = cross(bz, bx);
-            p.a = make_float4(center.x, center.y, center.z, radius);
-            p.b = make_float4(bx.x, bx.y, bx.z, half);
-            p.c = make_float4(ly.x, ly.y, ly.z, radius * radius);
-            p.d = make_float4(bz.x, bz.y, bz.z, 0.f);
-        }
-        Optics& o = optics[i];
-        o.reflectivity = (float)e.reflectivity;
-        o.slope = (float)e.slope_error;
-        o.spec = (float)e.specularity_error;
-        o.pad = 0.f;
+        uint32_t type = 0;
+        const char* why = "";
+        if (pack_element(el[i], i + 1 == n, type, aabbs[i], prims[i], optics[i], nullptr, why))
+            return set_error(CSP_ERR_BAD_SCENE, std::string("csp_trace_noalloc: element ") + std::to_string(i) + ": " + why);
         const uint32_t hitw = kLeafFlag | (type << kTypeShift) | i;
         const int32_t miss = (i + 1 < n) ? (int32_t)(i + 1) : -1;
-        nodes[i].lo = make_float4(box.lo.x, box.lo.y, box.lo.z, u2f(hitw));
-        nodes[i].hi = make_float4(box.hi.x, box.hi.y, box.hi.z, u2f((uint32_t)miss));
+        nodes[i].lo = make_float4(aabbs[i].lo.x, aabbs[i].lo.y, aabbs[i].lo.z, u2f(hitw));
+        nodes[i].hi = make_float4(aabbs[i].hi.x, aabbs[i].hi.y, aabbs[i].hi.z, u2f((uint32_t)miss));
     }
     return CSP_OK;
 }
@@ -163,7 +109,9 @@ extern "C" int csp_trace_noalloc(int device, const csp_element* elements, uint32
                          "csp_trace_noalloc: 1 to 8 elements (its fixed scratch array holds no more); "
                          "use csp_create/csp_initialize for larger scenes");
     if (!hits && num_rays) return set_error(CSP_ERR_INVALID_ARGUMENT, "csp_trace_noalloc: null hit buffer");
-    if (sun_shape != CSP_SUN_PILLBOX && sun_shape != CSP_SUN_GAUSSIAN)
+    if (!valid_ray_window(first_ray, num_rays))
+        return set_error(CSP_ERR_INVALID_ARGUMENT, "csp_trace_noalloc: ray window must stay below 2^56");
+    if (!valid_sun_shape(sun_shape))
         return set_error(CSP_ERR_INVALID_ARGUMENT, "csp_trace_noalloc: unknown sun shape");
     if (!(sun_param >= 0.0) || sun_param > 0.5)
         return set_error(CSP_ERR_INVALID_ARGUMENT, "csp_trace_noalloc: sun shape parameter out of range");
@@ -185,7 +133,7 @@ extern "C" int csp_trace_noalloc(int device, const csp_element* elements, uint32
     if (!rc) {
         float s[3];
         sun_vector_f(sun_dir, s);
-        const float pad = (float)(sun_shape == CSP_SUN_GAUSSIAN ? 5.0 * sun_param : sun_param);
+        const float pad = (float)sun_pad_angle(sun_shape, sun_param);
         SunFrame* sun = reinterpret_cast<SunFrame*>(scratch + kOffSun);
         rc = cuda_status(launch_prepare_sun(reinterpret_cast<const Aabb*>(scratch + kOffAabbs), (int)count, s[0], s[1],
                                             s[2], tanf(pad), sun_shape, (float)sun_param, sun, st),

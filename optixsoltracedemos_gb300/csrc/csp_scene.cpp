@@ -165,6 +165,100 @@ void sun_vector_f(const double d[3], float out[3]) {
     out[2] = (float)n[2];
 }
 
+int pack_element(const csp_element& e, bool last, uint32_t& type, Aabb& box, Prim& p, Optics& o, Aabb* prune,
+                 const char*& why) {
+    if (e.aperture != CSP_APERTURE_RECTANGLE) {
+        why = "only rectangular apertures are supported";
+        return CSP_ERR_BAD_SCENE;
+    }
+    if (!(e.width > 0) || !(e.height > 0)) {
+        why = "aperture dimensions must be positive";
+        return CSP_ERR_BAD_SCENE;
+    }
+    // entity type: lib/geometry_manager.cpp:50-59 (mirrors), :78-90 (last element = receiver)
+    if (e.surface == CSP_SURFACE_FLAT) type = last ? kFlatReceiver : kFlatMirror;
+    else if (e.surface == CSP_SURFACE_PARABOLIC) type = kParabolicMirror;  // a parabolic last element stays a mirror
+    else if (e.surface == CSP_SURFACE_CYLINDER) {
+        if (!last) {
+            why = "a cylinder is only supported as the receiver (last element)";
+            return CSP_ERR_BAD_SCENE;
+        }
+        type = kCylReceiver;
+    } else {
+        why = "unknown surface type";
+        return CSP_ERR_BAD_SCENE;
+    }
+
+    double G[9], euler[3], lo[3], hi[3];
+    element_frame(e, euler, G, lo, hi);
+    const double w = e.width, h = e.height;
+    box.lo = make_float4((float)lo[0], (float)lo[1], (float)lo[2], 0.f);
+    box.hi = make_float4((float)hi[0], (float)hi[1], (float)hi[2], 0.f);
+
+    // device geometry: lib/element.cpp:114-164 and the GeometryDataST constructors
+    const D3 xb{G[0], G[1], G[2]}, yb{G[3], G[4], G[5]}, zb{G[6], G[7], G[8]};
+    double plo[3] = {lo[0], lo[1], lo[2]}, phi[3] = {hi[0], hi[1], hi[2]};
+    if (e.surface == CSP_SURFACE_FLAT) {
+        const float3 center = tof3(D3{e.origin[0], e.origin[1], e.origin[2]});
+        const float3 x = tof3(xb), y = tof3(yb);
+        const float fw = (float)w, fh = (float)h;
+        const float3 nrm = normalize(cross(x, y));
+        const float pw = dot(nrm, center);
+        p.a = make_float4(nrm.x, nrm.y, nrm.z, pw);
+        p.b = make_float4(center.x, center.y, center.z, fw / 2);
+        p.c = make_float4(x.x, x.y, x.z, fh / 2);
+        p.d = make_float4(y.x, y.y, y.z, 0.f);
+    } else if (e.surface == CSP_SURFACE_PARABOLIC) {
+        const double sw = (double)(float)(-w), sh = (double)(float)h;
+        const D3 v1{xb.x * sw, xb.y * sw, xb.z * sw}, v2{yb.x * sh, yb.y * sh, yb.z * sh};
+        const D3 an{e.origin[0] - v1.x * 0.5 - v2.x * 0.5, e.origin[1] - v1.y * 0.5 - v2.y * 0.5,
+                    e.origin[2] - v1.z * 0.5 - v2.z * 0.5};
+        float3 fv1 = tof3(v1), fv2 = tof3(v2);
+        const float3 anchor = tof3(an);
+        const float i1 = 1.0f / dot(fv1, fv1), i2 = 1.0f / dot(fv2, fv2);
+        fv1 = make_float3(fv1.x * i1, fv1.y * i1, fv1.z * i1);
+        fv2 = make_float3(fv2.x * i2, fv2.y * i2, fv2.z * i2);
+        // per-call values of cuda/intersection.cu:335-352
+        const float L1 = 1.0f / length(fv1), L2 = 1.0f / length(fv2);
+        const float3 e1 = scale(L1, fv1), e2 = scale(L2, fv2);
+        const float3 nn = normalize(cross(e2, e1));
+        const float3 rc = add(add(anchor, scale(L1 / 2.0f, e1)), scale(L2 / 2.0f, e2));
+        const float cx = (float)e.curv_x, cy = (float)e.curv_y;
+        p.a = make_float4(e1.x, e1.y, e1.z, L1 / 2.0f);
+        p.b = make_float4(e2.x, e2.y, e2.z, L2 / 2.0f);
+        p.c = make_float4(nn.x, nn.y, nn.z, cx);
+        p.d = make_float4(rc.x, rc.y, rc.z, cy);
+        // surface bounds: z = cx/2 x^2 + cy/2 y^2 over |x| <= L1/2, |y| <= L2/2
+        const double h1 = L1 / 2.0, h2 = L2 / 2.0;
+        const double zx = 0.5 * cx * h1 * h1, zy = 0.5 * cy * h2 * h2;
+        const double zmin = std::min(0.0, zx) + std::min(0.0, zy), zmax = std::max(0.0, zx) + std::max(0.0, zy);
+        for (int k = 0; k < 8; ++k) {
+            const double lx = (k & 1) ? h1 : -h1, ly = (k & 2) ? h2 : -h2, lz = (k & 4) ? zmax : zmin;
+            const double P[3] = {rc.x + lx * e1.x + ly * e2.x + lz * nn.x, rc.y + lx * e1.y + ly * e2.y + lz * nn.y,
+                                 rc.z + lx * e1.z + ly * e2.z + lz * nn.z};
+            for (int a = 0; a < 3; ++a) {
+                plo[a] = std::min(plo[a], P[a]);
+                phi[a] = std::max(phi[a], P[a]);
+            }
+        }
+    } else {
+        const float radius = (float)w / 2.0f, half = (float)h / 2.0f;
+        const float3 center = tof3(D3{e.origin[0], e.origin[1], e.origin[2]});
+        const float3 bx = tof3(xb), bz = tof3(zb);
+        const float3 ly = cross(bz, bx);
+        p.a = make_float4(center.x, center.y, center.z, radius);
+        p.b = make_float4(bx.x, bx.y, bx.z, half);
+        p.c = make_float4(ly.x, ly.y, ly.z, radius * radius);
+        p.d = make_float4(bz.x, bz.y, bz.z, 0.f);
+    }
+    if (prune) *prune = outward(plo, phi);
+    o.reflectivity = (float)e.reflectivity;
+    o.slope = (float)e.slope_error;
+    o.spec = (float)e.specularity_error;
+    o.pad = 0.f;
+    return CSP_OK;
+}
+
 int build_elements(const csp_element* el, uint32_t n, HostScene& s, std::string& err) {
     if (n == 0) {
         err = "scene has no elements";
@@ -180,102 +274,15 @@ int build_elements(const csp_element* el, uint32_t n, HostScene& s, std::string&
     s.prune.assign(n, Aabb{});
     s.types.assign(n, 0);
     for (uint32_t i = 0; i < n; ++i) {
-        const csp_element& e = el[i];
-        const bool last = (i + 1 == n);
-        if (e.aperture != CSP_APERTURE_RECTANGLE) {
-            err = "element " + std::to_string(i) + ": only rectangular apertures are supported";
-            return CSP_ERR_BAD_SCENE;
+        const char* why = "";
+        const int rc = pack_element(el[i], i + 1 == n, s.types[i], s.aabbs[i], s.prims[i], s.optics[i], &s.prune[i], why);
+        if (rc) {
+            err = "element " + std::to_string(i) + ": " + why;
+            if (el[i].surface != CSP_SURFACE_FLAT && el[i].surface != CSP_SURFACE_PARABOLIC &&
+                el[i].surface != CSP_SURFACE_CYLINDER)
+                err += " " + std::to_string(el[i].surface);
+            return rc;
         }
-        if (!(e.width > 0) || !(e.height > 0)) {
-            err = "element " + std::to_string(i) + ": aperture dimensions must be positive";
-            return CSP_ERR_BAD_SCENE;
-        }
-        // entity type: lib/geometry_manager.cpp:50-59 (mirrors), :78-90 (last element = receiver)
-        uint32_t type;
-        if (e.surface == CSP_SURFACE_FLAT) type = last ? kFlatReceiver : kFlatMirror;
-        else if (e.surface == CSP_SURFACE_PARABOLIC) type = kParabolicMirror;  // a parabolic last element stays a mirror
-        else if (e.surface == CSP_SURFACE_CYLINDER) {
-            if (!last) {
-                err = "element " + std::to_string(i) + ": a cylinder is only supported as the receiver (last element)";
-                return CSP_ERR_BAD_SCENE;
-            }
-            type = kCylReceiver;
-        } else {
-            err = "element " + std::to_string(i) + ": unknown surface type " + std::to_string(e.surface);
-            return CSP_ERR_BAD_SCENE;
-        }
-        s.types[i] = type;
-
-        double G[9], euler[3], lo[3], hi[3];
-        element_frame(e, euler, G, lo, hi);
-        const double w = e.width, h = e.height;
-        Aabb& box = s.aabbs[i];
-        box.lo = make_float4((float)lo[0], (float)lo[1], (float)lo[2], 0.f);
-        box.hi = make_float4((float)hi[0], (float)hi[1], (float)hi[2], 0.f);
-
-        // device geometry: lib/element.cpp:114-164 and the GeometryDataST constructors
-        const D3 xb{G[0], G[1], G[2]}, yb{G[3], G[4], G[5]}, zb{G[6], G[7], G[8]};
-        Prim& p = s.prims[i];
-        double plo[3] = {lo[0], lo[1], lo[2]}, phi[3] = {hi[0], hi[1], hi[2]};
-        if (e.surface == CSP_SURFACE_FLAT) {
-            const float3 center = tof3(D3{e.origin[0], e.origin[1], e.origin[2]});
-            const float3 x = tof3(xb), y = tof3(yb);
-            const float fw = (float)w, fh = (float)h;
-            const float3 nrm = normalize(cross(x, y));
-            const float pw = dot(nrm, center);
-            p.a = make_float4(nrm.x, nrm.y, nrm.z, pw);
-            p.b = make_float4(center.x, center.y, center.z, fw / 2);
-            p.c = make_float4(x.x, x.y, x.z, fh / 2);
-            p.d = make_float4(y.x, y.y, y.z, 0.f);
-        } else if (e.surface == CSP_SURFACE_PARABOLIC) {
-            const double sw = (double)(float)(-w), sh = (double)(float)h;
-            const D3 v1{xb.x * sw, xb.y * sw, xb.z * sw}, v2{yb.x * sh, yb.y * sh, yb.z * sh};
-            const D3 an{e.origin[0] - v1.x * 0.5 - v2.x * 0.5, e.origin[1] - v1.y * 0.5 - v2.y * 0.5,
-                        e.origin[2] - v1.z * 0.5 - v2.z * 0.5};
-            float3 fv1 = tof3(v1), fv2 = tof3(v2);
-            const float3 anchor = tof3(an);
-            const float i1 = 1.0f / dot(fv1, fv1), i2 = 1.0f / dot(fv2, fv2);
-            fv1 = make_float3(fv1.x * i1, fv1.y * i1, fv1.z * i1);
-            fv2 = make_float3(fv2.x * i2, fv2.y * i2, fv2.z * i2);
-            // per-call values of cuda/intersection.cu:335-352
-            const float L1 = 1.0f / length(fv1), L2 = 1.0f / length(fv2);
-            const float3 e1 = scale(L1, fv1), e2 = scale(L2, fv2);
-            const float3 nn = normalize(cross(e2, e1));
-            const float3 rc = add(add(anchor, scale(L1 / 2.0f, e1)), scale(L2 / 2.0f, e2));
-            const float cx = (float)e.curv_x, cy = (float)e.curv_y;
-            p.a = make_float4(e1.x, e1.y, e1.z, L1 / 2.0f);
-            p.b = make_float4(e2.x, e2.y, e2.z, L2 / 2.0f);
-            p.c = make_float4(nn.x, nn.y, nn.z, cx);
-            p.d = make_float4(rc.x, rc.y, rc.z, cy);
-            // surface bounds: z = cx/2 x^2 + cy/2 y^2 over |x| <= L1/2, |y| <= L2/2
-            const double h1 = L1 / 2.0, h2 = L2 / 2.0;
-            const double zx = 0.5 * cx * h1 * h1, zy = 0.5 * cy * h2 * h2;
-            const double zmin = std::min(0.0, zx) + std::min(0.0, zy), zmax = std::max(0.0, zx) + std::max(0.0, zy);
-            for (int k = 0; k < 8; ++k) {
-                const double lx = (k & 1) ? h1 : -h1, ly = (k & 2) ? h2 : -h2, lz = (k & 4) ? zmax : zmin;
-                const double P[3] = {rc.x + lx * e1.x + ly * e2.x + lz * nn.x, rc.y + lx * e1.y + ly * e2.y + lz * nn.y,
-                                     rc.z + lx * e1.z + ly * e2.z + lz * nn.z};
-                for (int a = 0; a < 3; ++a) {
-                    plo[a] = std::min(plo[a], P[a]);
-                    phi[a] = std::max(phi[a], P[a]);
-                }
-            }
-        } else {
-            const float radius = (float)w / 2.0f, half = (float)h / 2.0f;
-            const float3 center = tof3(D3{e.origin[0], e.origin[1], e.origin[2]});
-            const float3 bx = tof3(xb), bz = tof3(zb);
-            const float3 ly = cross(bz, bx);
-            p.a = make_float4(center.x, center.y, center.z, radius);
-            p.b = make_float4(bx.x, bx.y, bx.z, half);
-            p.c = make_float4(ly.x, ly.y, ly.z, radius * radius);
-            p.d = make_float4(bz.x, bz.y, bz.z, 0.f);
-        }
-        s.prune[i] = outward(plo, phi);
-        Optics& o = s.optics[i];
-        o.reflectivity = (float)e.reflectivity;
-        o.slope = (float)e.slope_error;
-        o.spec = (float)e.specularity_error;
-        o.pad = 0.f;
     }
     return CSP_OK;
 }
@@ -579,7 +586,7 @@ void build_grid(const HostScene& s, HostGrid& g) {
 }
 
 GridDesc grid_desc(const HostGrid& g, const uint32_t* cell_start, const Aabb* items, const Aabb* global) {
-    GridDesc d;
+    GridDesc d{};
     d.x0 = g.x0;
     d.y0 = g.y0;
     d.x1 = g.x1;

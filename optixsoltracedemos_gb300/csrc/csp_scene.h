@@ -27,6 +27,12 @@ struct HostScene {
 // cuda/GeometryDataST.h constructors), in the same double/float operation order.
 int build_elements(const csp_element* el, uint32_t n, HostScene& s, std::string& err);
 
+// The records of one element, as build_elements makes them: entity type, exact AABB, Prim, Optics
+// and (when `prune` is not null) the pruning box.  Allocates nothing.  Returns CSP_OK, or
+// CSP_ERR_BAD_SCENE with `why` pointing to a static message.
+int pack_element(const csp_element& e, bool last, uint32_t& type, Aabb& box, Prim& p, Optics& o, Aabb* prune,
+                 const char*& why);
+
 // Build the stackless BVH over the pruning boxes (binned SAH, one element per leaf; scenes of up
 // to kFlatListMax elements get a plain list of leaves instead).
 constexpr uint32_t kFlatListMax = 8;  // = kFlatMax of the trace kernel
@@ -52,6 +58,7 @@ struct HostGrid {
     std::vector<Aabb> items;
     std::vector<Aabb> global;
 };
+
 
 // Build the grid of a scene with more than kFlatListMax elements whose mirrors lie in a thin layer
 // (at most a quarter of the field's horizontal extent); otherwise leave g.valid false (the BVH is

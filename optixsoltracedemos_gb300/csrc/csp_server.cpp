@@ -81,6 +81,7 @@ struct SRequest {
     InstanceDesc desc{};      // its step descriptor except the ray window and tile offset
     bool desc_ready = false;  // built at its first step (its arena block and scene are fixed)
     std::string error;
+    int error_status = CSP_ERR_CUDA;  // status csp_server_wait returns for a failed request
     uint64_t next_ray = 0;
     int group = kAccelBvh;
     size_t off = 0, bytes = 0;  // arena block
@@ -176,6 +177,7 @@ struct Server {
     std::condition_variable cv_work, cv_done;
     std::thread worker;
     bool stopping = false;
+    int waiting = 0;  // threads inside csp_server_wait (stop() frees nothing while one is there)
     bool hold = false;  // admission paused (requests queue; active ones finish)
     std::string fatal;
 
@@ -206,6 +208,19 @@ void Server::stop() {
     }
     cv_work.notify_all();
     if (worker.joinable()) worker.join();
+    {
+        // requests still queued (admission held, or the worker stopped on an error) will never
+        // run: fail them, wake their waiters and let every waiter leave before anything is freed
+        std::unique_lock<std::mutex> lk(mu);
+        for (SRequest* r : pending) {
+            r->state = kFailed;
+            r->error = "server destroyed before the request was admitted";
+            r->error_status = CSP_ERR_STATE;
+        }
+        pending.clear();
+        cv_done.notify_all();
+        cv_done.wait(lk, [&] { return waiting == 0; });
+    }
     if (device >= 0) cudaSetDevice(device);
     if (stream) cudaStreamSynchronize(stream);
     for (auto& s : scenes) {
@@ -334,7 +349,7 @@ int Server::submit(const SRequest& in, uint64_t* id) {
     }
     std::lock_guard<std::mutex> lk(mu);
     if (!fatal.empty()) return set_error(CSP_ERR_CUDA, "server stopped: " + fatal);
-    if (in.shape != CSP_SUN_PILLBOX && in.shape != CSP_SUN_GAUSSIAN)
+    if (!valid_sun_shape(in.shape))
         return set_error(CSP_ERR_INVALID_ARGUMENT, "unknown sun shape");
     if (!(in.param >= 0.0) || in.param > 0.5) return set_error(CSP_ERR_INVALID_ARGUMENT, "sun shape parameter out of range");
     if (in.rays == 0 || in.rays >= (1ull << 40)) return set_error(CSP_ERR_INVALID_ARGUMENT, "bad ray count");
@@ -503,7 +518,7 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
         sj.sx = sv[0];
         sj.sy = sv[1];
         sj.sz = sv[2];
-        sj.tan_pad = tanf((float)(r.shape == CSP_SUN_GAUSSIAN ? 5.0 * r.param : r.param));
+        sj.tan_pad = tanf((float)sun_pad_angle(r.shape, r.param));
         sj.shape = r.shape;
         sj.param = (float)r.param;
         sj.out = reinterpret_cast<SunFrame*>(d_arena + r.o_sun);
@@ -791,17 +806,32 @@ int csp_server_wait(csp_server sh, uint64_t request, double timeout_s, uint32_t*
     CSP_SGUARD(sh);
     Server* s = reinterpret_cast<Server*>(sh);
     std::unique_lock<std::mutex> lk(s->mu);
-    auto it = s->requests.find(request);
-    if (it == s->requests.end()) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "no such request");
-    csp::SRequest* r = it->second.get();
-    auto done = [&] { return r->state == csp::kDone || r->state == csp::kFailed; };
+    // the request is looked up again after every wake-up: another thread waiting on the same id
+    // may have taken its results (and freed it) in the meantime
+    auto find = [&]() -> csp::SRequest* {
+        auto f = s->requests.find(request);
+        return f == s->requests.end() ? nullptr : f->second.get();
+    };
+    if (!find()) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "no such request");
+    auto done = [&] {
+        const csp::SRequest* q = find();
+        return !q || q->state == csp::kDone || q->state == csp::kFailed;
+    };
+    ++s->waiting;
+    bool in_time = true;
     if (timeout_s < 0) s->cv_done.wait(lk, done);
-    else if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), done))
-        return csp::set_error(CSP_ERR_TIMEOUT, "request not finished within the timeout");
+    else in_time = s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), done);
+    if (--s->waiting == 0 && s->stopping) s->cv_done.notify_all();
+    if (!in_time) return csp::set_error(CSP_ERR_TIMEOUT, "request not finished within the timeout");
+    auto it = s->requests.find(request);
+    if (it == s->requests.end())
+        return csp::set_error(CSP_ERR_STATE, "the request's results went to another thread waiting on it");
+    csp::SRequest* r = it->second.get();
     if (r->state == csp::kFailed) {
         const std::string msg = r->error;
+        const int status = r->error_status;
         s->requests.erase(it);
-        return csp::set_error(CSP_ERR_CUDA, "request failed: " + msg);
+        return csp::set_error(status, "request failed: " + msg);
     }
     if (counts) std::memcpy(counts, r->counts.data(), r->counts.size() * sizeof(uint32_t));
     if (stats) std::memcpy(stats, r->stats, sizeof r->stats);

@@ -16,6 +16,19 @@ namespace csp {
 int set_error(int status, const std::string& msg);
 int cuda_status(cudaError_t e, const char* what);
 
+// Sun shapes the ABI accepts: pillbox or Gaussian, with or without CSP_SUN_ACCURATE.
+inline bool valid_sun_shape(int shape) { return shape >= 0 && shape <= (CSP_SUN_GAUSSIAN | CSP_SUN_ACCURATE); }
+
+// Angle the sun plane is padded by: the pillbox half angle (lib/geometry_manager.cpp:129), or 5
+// sigma for the Gaussian sun.
+inline double sun_pad_angle(int shape, double param) { return (shape & CSP_SUN_GAUSSIAN) ? 5.0 * param : param; }
+
+// A ray window [first, first + count) whose indices all stay below kRayIndexLimit (checked without
+// overflow).
+inline bool valid_ray_window(uint64_t first, uint64_t count) {
+    return first <= kRayIndexLimit && count <= kRayIndexLimit - first;
+}
+
 struct System {
     int device = -1;
     uint64_t num_rays = 0;

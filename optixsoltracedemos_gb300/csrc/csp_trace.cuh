@@ -200,9 +200,18 @@ __device__ void sun_frame_block(const Aabb* __restrict__ aabbs, int n, float3 s,
     f.w = make_float4(w.x, w.y, w.z, 0.f);
     f.u = make_float4(cu.x, cu.y, cu.z, 0.f);
     f.v = make_float4(cv.x, cv.y, cv.z, 0.f);
-    if (shape == 1) {
+    f.omc = 0.0f;
+    if (shape & 1) {
         f.cos_theta = 1.0f;
         f.sigma = param;
+    } else if (shape & 2) {
+        // accurate cone sampler: 1 - cos(half_angle) = 2 sin^2(half_angle / 2), free of the
+        // cancellation of 1 - cosf(half_angle)
+        float sn, cs;
+        det_sincos(param * 0.5f, sn, cs);
+        f.omc = (sn + sn) * sn;
+        f.cos_theta = 1.0f - f.omc;
+        f.sigma = 0.0f;
     } else {
         float sn, cs;
         det_sincos(param, sn, cs);  // cosf(half_angle), cuda/sun.cu:82
@@ -210,7 +219,6 @@ __device__ void sun_frame_block(const Aabb* __restrict__ aabbs, int n, float3 s,
         f.sigma = 0.0f;
     }
     f.tan_pad = tan_pad;
-    f.pad = 0.f;
     f.shape = shape;
     f.n_prims = n;
     f.pad1 = f.pad2 = 0;
@@ -358,8 +366,12 @@ __device__ __forceinline__ float3 parab_normal(const Prim& p, float3 o, float3 d
     return normalize(add(add(scale(nl.x, e1), scale(nl.y, e2)), scale(nl.z, n)));
 }
 
-// Cylinder_Y with caps, cuda/intersection.cu:177-296.
-__device__ __forceinline__ bool hit_cyl(const Prim& p, float3 o, float3 draw, float tmin, float& tout) {
+// Cylinder_Y with caps, cuda/intersection.cu:177-296.  `accurate` (extension, the CSP_SUN_ACCURATE
+// trace flag): the side roots from the ray's closest approach to the axis, tm = -(Ox Dx + Oz Dz) / A,
+// and the half chord sqrt((r^2 - |Q|^2) / A) with Q = O + tm D in the (x, z) plane, instead of
+// B^2 - 4AC, which cancels to ~1e-4 relative when the ray starts hundreds of metres from the
+// receiver (about 1 mm on the hit point in float).
+__device__ __forceinline__ bool hit_cyl(const Prim& p, float3 o, float3 draw, float tmin, bool accurate, float& tout) {
     const float3 d = normalize(draw);
     const float3 lo = sub(o, xyz(p.a));
     const float3 lx = xyz(p.b), ly = xyz(p.c), lz = xyz(p.d);
@@ -367,15 +379,34 @@ __device__ __forceinline__ bool hit_cyl(const Prim& p, float3 o, float3 draw, fl
     const float Dx = dot(d, lx), Dy = dot(d, ly), Dz = dot(d, lz);
     const float half = p.b.w, r2 = p.c.w;
     const float A = Dx * Dx + Dz * Dz;
-    const float B = 2.0f * (Ox * Dx + Oz * Dz);
-    const float C = Ox * Ox + Oz * Oz - r2;
-    const float det = B * B - 4.0f * A * C;
     const float inval = kTmax + 1.0f;
     float tc = inval;
-    if (det >= 0.0f) {
-        const float sq = sqrtf(det);
-        const float t1 = (-B - sq) / (2.0f * A);
-        const float t2 = (-B + sq) / (2.0f * A);
+    float t1 = 0.0f, t2 = 0.0f;
+    bool side = false;
+    if (accurate) {
+        if (A > 0.0f) {
+            const float tm = -(Ox * Dx + Oz * Dz) / A;
+            const float qx = Ox + tm * Dx, qz = Oz + tm * Dz;
+            const float h2 = r2 - (qx * qx + qz * qz);
+            if (h2 >= 0.0f) {
+                const float hh = sqrtf(h2 / A);
+                t1 = tm - hh;
+                t2 = tm + hh;
+                side = true;
+            }
+        }
+    } else {
+        const float B = 2.0f * (Ox * Dx + Oz * Dz);
+        const float C = Ox * Ox + Oz * Oz - r2;
+        const float det = B * B - 4.0f * A * C;
+        if (det >= 0.0f) {
+            const float sq = sqrtf(det);
+            t1 = (-B - sq) / (2.0f * A);
+            t2 = (-B + sq) / (2.0f * A);
+            side = true;
+        }
+    }
+    if (side) {
         if (t1 > tmin && t1 < kTmax && fabsf(Oy + t1 * Dy) <= half) tc = t1;
         else if (t2 > tmin && t2 < kTmax && fabsf(Oy + t2 * Dy) <= half) tc = t2;
     }
@@ -394,9 +425,11 @@ __device__ __forceinline__ bool hit_cyl(const Prim& p, float3 o, float3 draw, fl
     return true;
 }
 
-__device__ __forceinline__ bool hit_prim(uint32_t type, const Prim& p, float3 o, float3 d, float tmin, float& t) {
+// `acc`: the accurate arithmetic trace flag (bit 1 of the sun shape).
+__device__ __forceinline__ bool hit_prim(uint32_t type, const Prim& p, float3 o, float3 d, float tmin, bool acc,
+                                         float& t) {
     if (type == kParabolicMirror) return hit_parab(p, o, d, tmin, t);
-    if (type == kCylReceiver) return hit_cyl(p, o, d, tmin, t);
+    if (type == kCylReceiver) return hit_cyl(p, o, d, tmin, acc, t);
     return hit_flat(p, o, d, tmin, t);
 }
 
@@ -414,7 +447,7 @@ __device__ __forceinline__ Prim load_prim(const Prim* prims, uint32_t i) {
 // lower element index.  Internal nodes are pruned against the closest hit so far with slack
 // (their boxes bound every surface below them with a margin); leaves test the exact AABB.
 __device__ __forceinline__ int traverse(const Node* __restrict__ nodes, const Prim* __restrict__ prims, float3 o,
-                                        float3 d, float tmin, float& best_t, uint32_t& best_type) {
+                                        float3 d, float tmin, bool acc, float& best_t, uint32_t& best_type) {
     const float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
     int best = -1;
     best_t = __int_as_float(0x7f800000);
@@ -435,7 +468,7 @@ __device__ __forceinline__ int traverse(const Node* __restrict__ nodes, const Pr
                 const uint32_t prim = hitw & kPrimMask;
                 const uint32_t type = (hitw >> kTypeShift) & 7u;
                 float t;
-                if (hit_prim(type, load_prim(prims, prim), o, d, tmin, t) &&
+                if (hit_prim(type, load_prim(prims, prim), o, d, tmin, acc, t) &&
                     (t < best_t || (t == best_t && (int)prim < best))) {
                     best = (int)prim;
                     best_t = t;
@@ -456,8 +489,8 @@ __device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefe
 // Exact-AABB culling and intersection program of one grid candidate (a BVH leaf's work): the
 // element's exact AABB lo, hi with lo.w = element | type << 28.
 __device__ __forceinline__ void test_box(float4 lo, float4 hi, const Prim* __restrict__ prims, float3 o, float3 d,
-                                         float3 inv, float tmin, int& best, float& best_t, uint32_t& best_type,
-                                         float& prune) {
+                                         float3 inv, float tmin, bool acc, int& best, float& best_t,
+                                         uint32_t& best_type, float& prune) {
     const float t0x = (lo.x - o.x) * inv.x, t1x = (hi.x - o.x) * inv.x;
     const float t0y = (lo.y - o.y) * inv.y, t1y = (hi.y - o.y) * inv.y;
     const float t0z = (lo.z - o.z) * inv.z, t1z = (hi.z - o.z) * inv.z;
@@ -468,20 +501,13 @@ __device__ __forceinline__ void test_box(float4 lo, float4 hi, const Prim* __res
     const uint32_t prim = w & kPrimMask;
     const uint32_t type = (w >> kTypeShift) & 7u;
     float t;
-    if (hit_prim(type, load_prim(prims, prim), o, d, tmin, t) && (t < best_t || (t == best_t && (int)prim < best))) {
+    if (hit_prim(type, load_prim(prims, prim), o, d, tmin, acc, t) &&
+        (t < best_t || (t == best_t && (int)prim < best))) {
         best = (int)prim;
         best_t = t;
         best_type = type;
         prune = fminf(kTmax, best_t + best_t * 1e-3f + 1e-3f);
     }
-}
-
-// The same for the candidate stored at `it`.
-__device__ __forceinline__ void test_item(const Aabb* __restrict__ it, const Prim* __restrict__ prims, float3 o,
-                                          float3 d, float3 inv, float tmin, int& best, float& best_t,
-                                          uint32_t& best_type, float& prune) {
-    const float4* q = reinterpret_cast<const float4*>(it);
-    test_box(__ldg(q), __ldg(q + 1), prims, o, d, inv, tmin, best, best_t, best_type, prune);
 }
 
 // Restrict [ta, tb] to the parameters where coordinate o + t d lies in [lo, hi] (an empty range
@@ -500,13 +526,13 @@ __device__ __forceinline__ void clip_axis(float o, float d, float inv, float lo,
 }
 
 // Closest hit through the field grid: the global elements, then the cells of the xy path inside
-// the layer in ray order (2D DDA), each cell's candidates through test_item, until a cell is
+// the layer in ray order (2D DDA), each cell's candidates through test_box, until a cell is
 // entered beyond the pruning distance.  The result equals traverse()'s: every element whose
 // surface holds a hit point at t is registered in the cell the walk assigns to that point (the
 // registered boxes exceed the surfaces by a margin far above the walk's rounding), that cell is
 // entered at or before t, and the walk only stops beyond best_t + best_t 1e-3 + 1e-3.
 __device__ __forceinline__ int traverse_grid(const GridDesc& G, const Prim* __restrict__ prims, float3 o, float3 d,
-                                             float tmin, float& best_t, uint32_t& best_type) {
+                                             float tmin, bool acc, float& best_t, uint32_t& best_type) {
     const float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
     int best = -1;
     best_t = __int_as_float(0x7f800000);
@@ -532,7 +558,10 @@ __device__ __forceinline__ int traverse_grid(const GridDesc& G, const Prim* __re
     if (next) prefetch_l1(G.cell_start + (iy * G.nx + ix));
     int step = 0;
     for (;;) {
-        for (; j < e; ++j) test_item(list + j, prims, o, d, inv, tmin, best, best_t, best_type, prune);
+        for (; j < e; ++j) {
+            const float4* q = reinterpret_cast<const float4*>(list + j);
+            test_box(__ldg(q), __ldg(q + 1), prims, o, d, inv, tmin, acc, best, best_t, best_type, prune);
+        }
         if (!next || ctc > tb || ctc > prune || step > G.nx + G.ny) break;
         const int c = iy * G.nx + ix;
         list = G.items;
@@ -615,14 +644,14 @@ __device__ __forceinline__ uint32_t candidates(const FlatScene& fs, float3 o, fl
 
 // Closest hit among the candidate elements, in ascending index (equal t keeps the lower index).
 __device__ __forceinline__ int closest_in(const FlatScene& fs, uint32_t mask, float3 o, float3 d, float tmin,
-                                          float& best_t, uint32_t& best_type) {
+                                          bool acc, float& best_t, uint32_t& best_type) {
     int best = -1;
     best_t = __int_as_float(0x7f800000);
     while (mask) {
         const int k = __ffs(mask) - 1;
         mask &= mask - 1u;
         float t;
-        if (hit_prim(fs.type[k], fs.prim[k], o, d, tmin, t) && t < best_t) {
+        if (hit_prim(fs.type[k], fs.prim[k], o, d, tmin, acc, t) && t < best_t) {
             best = k;
             best_t = t;
             best_type = fs.type[k];
@@ -710,10 +739,23 @@ __device__ __forceinline__ float3 sun_direction(const typename C::Args& A, const
     const u32x4 r0 = draw<C>(A, ray, 0, 0);
     const float3 w = xyz(S.w), cu = xyz(S.u), cv = xyz(S.v);
     float3 dir;
-    if (S.shape == 1) {
+    if (S.shape & 1) {
         float g1, g2;
         box_muller(u01(r0.x), u01(r0.y), g1, g2);
         dir = normalize(add(add(w, scale(S.sigma * g1, cu)), scale(S.sigma * g2, cv)));
+    } else if (S.shape & 2) {
+        // the reference's uniform z in [cos(half_angle), 1] (cuda/sun.cu:82-86) carried as
+        // 1 - z = (1 - cos(half_angle)) (1 - rand2), so that the cone radius
+        // sqrt(1 - z^2) = sqrt((1 - z)(2 - (1 - z))) keeps full relative precision (the float z of
+        // the reference formula quantizes 1 - z in steps of 2^-24)
+        const float rand1 = u01(r0.x), rand2 = u01(r0.y);
+        const float phi = kTwoPi * rand1;
+        const float omz = S.omc * (1.0f - rand2);
+        const float z = 1.0f - omz;
+        const float r = sqrtf(omz * (2.0f - omz));
+        float sp, cp;
+        det_sincos(phi, sp, cp);
+        dir = normalize(add(scale(r, add(scale(cp, cu), scale(sp, cv))), scale(z, w)));
     } else {
         const float rand1 = u01(r0.x), rand2 = u01(r0.y);
         const float phi = kTwoPi * rand1;
@@ -739,7 +781,7 @@ __device__ __forceinline__ Segment generate(const typename C::Args& A, const Sun
 // it, and every point of the box lies at depth <= H (its deepest corner).  So o projects within
 // H tan a of the box's projection; in Halton units that is the corners' range of
 // ((c - v0).e1 / |e1|^2, (c - v0).e2 / |e2|^2) widened by H tan a / |e1|, H tan a / |e2|.
-// tan a: pillbox tan(half angle); Gaussian sigma |(g1, g2)| with |(g1, g2)| <= sqrt(-2 ln 2^-24)
+// tan a: pillbox tan(half angle) (the accurate sampler: from 1 - cos directly); Gaussian sigma |(g1, g2)| with |(g1, g2)| <= sqrt(-2 ln 2^-24)
 // = 5.77 (the smallest uniform is 2^-24).  Margins: 1 % on tan a, 1e-4 of the scene's extent plus
 // 1 mm on the distance, 1e-5 in Halton units, far above the float rounding of the ray's origin,
 // direction and box test, so a ray outside every rectangle fails the exact box test of every
@@ -748,8 +790,11 @@ __device__ __forceinline__ float4 reach_rect(const SunFrame& S, float4 lo, float
     const float3 v0 = xyz(S.v0), e1 = xyz(S.e1), e2 = xyz(S.e2), w = xyz(S.w);
     const float l1 = dot(e1, e1), l2 = dot(e2, e2);
     float tan_a;
-    if (S.shape == 1) {
+    if (S.shape & 1) {
         tan_a = 5.8f * S.sigma;
+    } else if (S.shape & 2) {
+        const float c = S.cos_theta;
+        tan_a = c > 0.2f ? sqrtf(S.omc * (2.0f - S.omc)) / c : __int_as_float(0x7f800000);
     } else {
         const float c = S.cos_theta;
         tan_a = c > 0.2f ? sqrtf(fmaxf(0.0f, 1.0f - c * c)) / c : __int_as_float(0x7f800000);
@@ -779,9 +824,10 @@ __device__ __forceinline__ float4 reach_rect(const SunFrame& S, float4 lo, float
 }
 
 // Queue entries of BVH/grid launches carry the depth of their pending mirror hit in the top bits of
-// the ray index (ray indices stay below 2^56).
+// the ray index (ray indices stay below 2^56, kRayIndexLimit, which every host entry point checks).
 constexpr int kDepthShift = 56;
 constexpr uint64_t kRayMask = (1ull << kDepthShift) - 1u;
+static_assert((1ull << kDepthShift) == kRayIndexLimit, "the host ray-window check must match the packing");
 
 // Shared memory of one CTA: the ray queue, the Halton table, the sun frame and the kFlat scene;
 // with kGen also the generation queue (sun rays waiting for their direction) and the reach
@@ -807,8 +853,9 @@ struct CoreSmem {
 template <class C>
 __device__ __forceinline__ int find_closest(const typename C::Args& A, const typename C::Core& sm, float3 o, float3 d,
                                             float tmin, float& t, uint32_t& type) {
-    if constexpr (C::kAccel == kAccelGrid) return traverse_grid(sm.grid, A.prims, o, d, tmin, t, type);
-    else return traverse(A.nodes, A.prims, o, d, tmin, t, type);
+    const bool acc = (sm.sun.shape & 2) != 0;
+    if constexpr (C::kAccel == kAccelGrid) return traverse_grid(sm.grid, A.prims, o, d, tmin, acc, t, type);
+    else return traverse(A.nodes, A.prims, o, d, tmin, acc, t, type);
 }
 
 // Phase A record staging of the kDense sink, ray-major per warp.
@@ -932,7 +979,7 @@ __device__ void finish_path(const typename C::Args& A, const Sink& k, const type
         g = next;
         if (C::kFlat) {
             const uint32_t m = candidates(sm.flat, g.o, g.d, g.tmin);
-            h.best = closest_in(sm.flat, m, g.o, g.d, g.tmin, h.t, h.type);
+            h.best = closest_in(sm.flat, m, g.o, g.d, g.tmin, (sm.sun.shape & 2) != 0, h.t, h.type);
         } else {
             h.best = find_closest<C>(A, sm, g.o, g.d, g.tmin, h.t, h.type);
         }
@@ -967,7 +1014,7 @@ __device__ __forceinline__ void bounce_batch(const typename C::Args& A, const Si
                 // first segment from the sun: intersection programs of the candidate elements
                 const Segment g{o, d, kTminSun, 0};
                 Hit h;
-                h.best = closest_in(sm.flat, w, o, d, kTminSun, h.t, h.type);
+                h.best = closest_in(sm.flat, w, o, d, kTminSun, (sm.sun.shape & 2) != 0, h.t, h.type);
                 finish_path<C>(A, k, sm, ray, g, h, false);
             }
         }

@@ -25,6 +25,10 @@ constexpr uint32_t kLeafFlag = 0x80000000u;
 constexpr uint32_t kTypeShift = 28;
 constexpr uint32_t kPrimMask = 0x0FFFFFFFu;
 constexpr uint32_t kNoElement = 0xFFFFFFFFu;
+// Every ray index of a trace lies below 2^56: the BVH and grid kernels queue a ray with the bounce
+// depth of its pending hit in the top 8 bits of its 64-bit index.  The host entry points reject
+// ray windows that reach past it before any launch.
+constexpr uint64_t kRayIndexLimit = 1ull << 56;
 
 // Prim field layout by entity type (all values float, computed on the host with the same float
 // operations the reference's intersection programs perform per call, so hoisting them is exact):
@@ -66,7 +70,8 @@ struct alignas(16) SunFrame {
     float4 v1, v2, v3;
     float4 w;      // cone axis = -sun
     float4 u, v;   // cone frame
-    float cos_theta, sigma, tan_pad, pad;
+    float cos_theta, sigma, tan_pad;
+    float omc;     // 1 - cos_theta as 2 sin^2(half angle / 2) (shape 2, the accurate cone sampler)
     int shape, n_prims, pad1, pad2;
 };
 

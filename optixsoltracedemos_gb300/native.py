@@ -93,6 +93,7 @@ SIGNATURES = {
     "csp_batch_get_stats": (ctypes.c_int, [_H, ctypes.c_uint32, _P]),
     "csp_batch_get_sun_plane": (ctypes.c_int, [_H, ctypes.c_uint32, _P]),
     "csp_batch_get_timing": (ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    "csp_batch_get_transfer": (ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
     "csp_server_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_uint64,
                                          ctypes.c_uint32, ctypes.c_uint64]),
     "csp_server_destroy": (ctypes.c_int, [_H]),
@@ -378,6 +379,12 @@ class Batch:
     def timing(self):
         a, b = ctypes.c_double(), ctypes.c_double()
         _check(self.lib.csp_batch_get_timing(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def transfer(self):
+        """(host-to-device bytes, device-to-host bytes) of the last completed run."""
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(self.lib.csp_batch_get_transfer(self.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
     def close(self):

@@ -52,6 +52,9 @@ SURFACE_PARABOLIC = 1
 SURFACE_CYLINDER = 3
 SUN_PILLBOX = 0
 SUN_GAUSSIAN = 1
+SUN_ACCURATE = 2  # flag: the trace in cancellation-free float formulas (cone sampler, cylinder roots)
+SUN_PILLBOX_ACCURATE = SUN_PILLBOX | SUN_ACCURATE
+SUN_GAUSSIAN_ACCURATE = SUN_GAUSSIAN | SUN_ACCURATE
 
 
 @dataclass

@@ -116,7 +116,8 @@ typedef struct {
     real d;               /* sun plane distance */
     v3 w, u, v;           /* cone frame */
     real cos_theta;       /* cos(max_sun_angle) */
-    int shape;            /* 0 pillbox, 1 gaussian */
+    real omc;             /* 1 - cos(max_sun_angle) = 2 sin^2(max_sun_angle / 2) (accurate pillbox) */
+    int shape;            /* bit 0: gaussian (else pillbox); bit 1: accurate arithmetic (extension) */
     real sigma;           /* gaussian sun sigma */
 } sun_t;
 
@@ -248,7 +249,7 @@ static void build_sun(const prim_t* prims, uint32_t n, const double sun_dir[3], 
     S->s = tov(sd);
     S->shape = shape;
     /* The reference pads the plane by the pillbox half angle; the Gaussian extension pads by 5 sigma. */
-    const double pad_angle = (shape == 1) ? 5.0 * param : param;
+    const double pad_angle = (shape & 1) ? 5.0 * param : param;
     const real angle = tor(pad_angle);
     real d = 0;
     for (uint32_t i = 0; i < n; ++i)
@@ -288,8 +289,21 @@ static void build_sun(const prim_t* prims, uint32_t n, const double sun_dir[3], 
     S->w = normalize(dir);
     S->u = normalize(cross(rabs_(S->w.x) > (real)0.99f ? mk(0, 1, 0) : mk(1, 0, 0), S->w));
     S->v = cross(S->w, S->u);
-    if (shape == 1) { S->cos_theta = 1; S->sigma = tor(param); }
-    else {
+    S->omc = 0;
+    if (shape & 1) { S->cos_theta = 1; S->sigma = tor(param); }
+    else if (shape & 2) {
+        /* accurate cone sampler (extension): 1 - cos(angle) as 2 sin^2(angle / 2), no cancellation */
+        if (IS_F32) {
+            float sn, cs;
+            orc_sincosf((float)param * 0.5f, &sn, &cs);
+            S->omc = (sn + sn) * sn;
+        } else {
+            const double sn = sin(param * 0.5);
+            S->omc = (real)(2.0 * sn * sn);
+        }
+        S->cos_theta = (real)1 - S->omc;
+        S->sigma = 0;
+    } else {
         /* cosf(half_angle) of cuda/sun.cu:82, with the project's deterministic cos */
         if (IS_F32) { float sn, cs; orc_sincosf((float)param, &sn, &cs); S->cos_theta = cs; }
         else S->cos_theta = (real)cos(param);
@@ -357,19 +371,35 @@ static int is_flat(const prim_t* p, v3 o, v3 d, real tmin, real tmax, real* tout
     return 0;
 }
 
-/* cuda/intersection.cu:177-296 */
-static int is_cyl(const prim_t* p, v3 o, v3 draw, real tmin, real tmax, real* tout) {
+/* cuda/intersection.cu:177-296.  accurate (extension): the side roots from the ray's closest
+ * approach to the axis, tm = -(Ox Dx + Oz Dz) / A, and the half chord sqrt((r^2 - |Q|^2) / A) with
+ * Q = O + tm D in the (x, z) plane, instead of B^2 - 4AC, which cancels to ~1e-4 relative when the
+ * ray starts hundreds of metres from the receiver (about 1 mm on the hit point in float). */
+static int is_cyl(const prim_t* p, v3 o, v3 draw, real tmin, real tmax, int accurate, real* tout) {
     v3 d = normalize(draw);
     v3 lo = sub(o, p->c_center);
     v3 lx = p->c_bx, lz = p->c_bz, ly = cross(lz, lx);
     v3 O = mk(dot(lo, lx), dot(lo, ly), dot(lo, lz));
     v3 D = mk(dot(d, lx), dot(d, ly), dot(d, lz));
     real A = D.x * D.x + D.z * D.z;
+    real tc = tmax + (real)1;
+    if (accurate) {
+        if (A > 0) {
+            real tm = -(O.x * D.x + O.z * D.z) / A;
+            real qx = O.x + tm * D.x, qz = O.z + tm * D.z;
+            real h2 = p->c_radius * p->c_radius - (qx * qx + qz * qz);
+            if (h2 >= 0) {
+                real hh = rsqrt_(h2 / A);
+                real t1 = tm - hh, t2 = tm + hh;
+                if (t1 > tmin && t1 < tmax && rabs_(O.y + t1 * D.y) <= p->c_half) tc = t1;
+                else if (t2 > tmin && t2 < tmax && rabs_(O.y + t2 * D.y) <= p->c_half) tc = t2;
+            }
+        }
+    }
     real B = (real)2 * (O.x * D.x + O.z * D.z);
     real C = O.x * O.x + O.z * O.z - p->c_radius * p->c_radius;
     real det = B * B - (real)4 * A * C;
-    real tc = tmax + (real)1;
-    if (det >= 0) {
+    if (!accurate && det >= 0) {
         real sq = rsqrt_(det);
         real t1 = (-B - sq) / ((real)2 * A);
         real t2 = (-B + sq) / ((real)2 * A);
@@ -455,10 +485,22 @@ static void trace_ray(const prim_t* prims, uint32_t n, const sun_t* S, uint64_t 
     v3 pos = add(add(S->v0, scl(hu, e1)), scl(hv, e2));
     orc_u32x4 r0 = orc_draw(ray, 0, 0, instance, seed);
     v3 dir;
-    if (S->shape == 1) {
+    if (S->shape & 1) {
         real g1, g2;
         box_muller_r(orc_u01(r0.v[0]), orc_u01(r0.v[1]), &g1, &g2);
         dir = normalize(add(add(S->w, scl(S->sigma * g1, S->u)), scl(S->sigma * g2, S->v)));
+    } else if (S->shape & 2) {
+        /* the same uniform z in [cos(angle), 1] as cuda/sun.cu:82-86, carried as 1 - z =
+         * (1 - cos(angle)) (1 - rand2) so the cone radius sqrt(1 - z^2) = sqrt((1 - z)(2 - (1 - z)))
+         * keeps full relative precision (the reference's float z quantizes 1 - z in steps of 2^-24) */
+        real rand1 = (real)orc_u01(r0.v[0]), rand2 = (real)orc_u01(r0.v[1]);
+        real phi = (IS_F32 ? (real)(2.0f * 3.14159265358979323846f) : (real)(2.0 * M_PI)) * rand1;
+        real omz = S->omc * ((real)1 - rand2);
+        real z = (real)1 - omz;
+        real r = rsqrt_(omz * ((real)2 - omz));
+        real sp, cp;
+        sincos_r(phi, &sp, &cp);
+        dir = normalize(add(scl(r, add(scl(cp, S->u), scl(sp, S->v))), scl(z, S->w)));
     } else {
         real rand1 = (real)orc_u01(r0.v[0]), rand2 = (real)orc_u01(r0.v[1]);
         real phi = (IS_F32 ? (real)(2.0f * 3.14159265358979323846f) : (real)(2.0 * M_PI)) * rand1;
@@ -489,7 +531,7 @@ static void trace_ray(const prim_t* prims, uint32_t n, const sun_t* S, uint64_t 
                 case ENT_FLAT_MIRROR:
                 case ENT_FLAT_RECEIVER: ok = is_flat(p, o, d, tmin, tmax, &t); nn = p->f_n; break;
                 case ENT_PARABOLIC_MIRROR: ok = is_parab(p, o, d, tmin, tmax, &t, &nn); break;
-                default: ok = is_cyl(p, o, d, tmin, tmax, &t); nn = mk(0, 0, 0); break;
+                default: ok = is_cyl(p, o, d, tmin, tmax, (S->shape & 2) != 0, &t); nn = mk(0, 0, 0); break;
             }
             /* closest hit; equal t keeps the lower element index */
             if (ok && t < best_t) { best_t = t; best = (int)k; best_n = nn; }
@@ -580,7 +622,7 @@ EXPORT int orc_trace(const orc_element* el, uint32_t n, const double sun_dir[3],
 
 /* Scene introspection for tests: per element 32 doubles, the sun frame in 32 doubles.
  * prim layout: [type, lo3, hi3, geometry 16 (type dependent), rho, slope, spec, pad...]
- * sun layout:  [s3, v0 3, v1 3, v2 3, v3 3, d, w3, u3, v3, cos_theta, sigma, shape] */
+ * sun layout:  [s3, v0 3, v1 3, v2 3, v3 3, d, w3, u3, v3, cos_theta, sigma, shape, 1 - cos_theta (shape 2)] */
 EXPORT int orc_scene_info(const orc_element* el, uint32_t n, const double sun_dir[3], int sun_shape,
                           double sun_param, double* prim_out, double* sun_out) {
     prim_t* prims;
@@ -610,7 +652,7 @@ EXPORT int orc_scene_info(const orc_element* el, uint32_t n, const double sun_di
     }
     const real sv[31] = {S.s.x, S.s.y, S.s.z, S.v0.x, S.v0.y, S.v0.z, S.v1.x, S.v1.y, S.v1.z, S.v2.x, S.v2.y,
                          S.v2.z, S.v3_.x, S.v3_.y, S.v3_.z, S.d, S.w.x, S.w.y, S.w.z, S.u.x, S.u.y, S.u.z,
-                         S.v.x, S.v.y, S.v.z, S.cos_theta, S.sigma, (real)S.shape, 0, 0, 0};
+                         S.v.x, S.v.y, S.v.z, S.cos_theta, S.sigma, (real)S.shape, S.omc, 0, 0};
     for (int k = 0; k < 31; ++k) sun_out[k] = sv[k];
     free(prims);
     return 0;

@@ -40,13 +40,24 @@ assert ELEMENT_DTYPE.itemsize == 120
 MAX_DEPTH = 5
 
 
+def reference_dir() -> str | None:
+    """The reference checkout named by CSP_REFERENCE_DIR, or None when unset or absent."""
+    d = os.environ.get("CSP_REFERENCE_DIR", "")
+    return d if d and os.path.isdir(os.path.join(d, "cuda")) else None
+
+
 def build(with_ref: bool | None = None) -> None:
-    """Compile the oracle libraries (and _ref when the reference sources exist)."""
-    ref_dir = os.environ.get("CSP_REFERENCE_DIR", "/root/reference")
+    """Compile the oracle libraries, and _ref (the reference's own programs on the host) when
+    with_ref is True, or None and CSP_REFERENCE_DIR names the reference checkout."""
+    ref_dir = reference_dir()
     if with_ref is None:
-        with_ref = os.path.isdir(os.path.join(ref_dir, "cuda"))
-    target = "ref" if with_ref else "all"
-    subprocess.run(["make", "-s", "-C", HERE, target, f"REF_DIR={ref_dir}"], check=True)
+        with_ref = ref_dir is not None
+    if with_ref and ref_dir is None:
+        raise RuntimeError("building the reference host build needs CSP_REFERENCE_DIR=<reference checkout>")
+    cmd = ["make", "-s", "-C", HERE, "ref" if with_ref else "all"]
+    if with_ref:
+        cmd.append(f"REF_DIR={ref_dir}")
+    subprocess.run(cmd, check=True)
 
 
 def _p(a):

@@ -5,8 +5,8 @@ cuda/materials.cu, lib/element.cpp, lib/Aperture.cpp), built on the host by `mak
 under the project's OptiX/cuRAND stand-ins, on small seeded cases, and stores their hit records,
 element ids, device geometry and sun plane as compressed .npz files next to this script.
 
-Usage (needs the reference sources, i.e. only where they are mounted):
-    python tests/golden/make_golden.py
+Usage (needs the reference sources):
+    CSP_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py
 """
 import os
 import sys

@@ -7,7 +7,8 @@ import pytest
 from optixsoltracedemos_gb300 import native, scenes
 from tests.golden import cases
 
-REF_TOY = "/root/reference/data/stinput/toy_problem_parabolic.stinput"
+# the reference's own .stinput fixture, read where CSP_REFERENCE_DIR names the reference checkout
+REF_TOY = os.path.join(os.environ.get("CSP_REFERENCE_DIR", ""), "data", "stinput", "toy_problem_parabolic.stinput")
 
 
 def _write_stinput(path, elements, sun, sigma_mrad, optics=True):
@@ -97,7 +98,8 @@ def test_stinput_errors(native_lib, tmp_path):
         native.parse_stinput(p)
 
 
-@pytest.mark.skipif(not os.path.exists(REF_TOY), reason="reference data file not mounted")
+@pytest.mark.skipif(not os.environ.get("CSP_REFERENCE_DIR") or not os.path.exists(REF_TOY),
+                    reason="CSP_REFERENCE_DIR does not name the reference checkout")
 def test_reference_toy_stinput(native_lib):
     el, sun, ang = native.parse_stinput(REF_TOY)
     exp = cases.toy_problem_parabolic()[0]

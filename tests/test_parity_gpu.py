@@ -42,7 +42,17 @@ def _configs():
         "field_300": scenes.large_field(n_heliostats=300, sun=scenes.sun_vector(40.0, 30.0)),
         "field_2000_parabolic": scenes.large_field(n_heliostats=2000, parabolic=True, sun=scenes.sun_vector(60.0, -45.0)),
         "corridor_multibounce": scenes.corridor(slope_error=1e-3),
+        # the accurate arithmetic flag: cancellation-free cone sampler and cylinder roots
+        "single_parabolic_accurate": scenes.single_parabolic(sun_shape=scenes.SUN_GAUSSIAN_ACCURATE),
+        "three_heliostats_accurate": _with_shape(scenes.three_heliostats(), scenes.SUN_PILLBOX_ACCURATE),
+        "field_300_accurate": _with_shape(scenes.large_field(n_heliostats=300, sun=scenes.sun_vector(40.0, 30.0)),
+                                          scenes.SUN_PILLBOX_ACCURATE),
     }
+
+
+def _with_shape(sc, shape):
+    sc.sun_shape = shape
+    return sc
 
 
 @pytest.mark.parametrize("name", list(_configs()))
@@ -238,6 +248,126 @@ def test_full_size_single_parabolic_sampled_and_properties(gpu, oracle32):
     assert not np.any((after > 0) & (st != 0))
     # sun points lie in the sun-plane parallelogram (Halton u, v in [0, 1))
     assert recv.sum() > 0.05 * N
+
+
+# Coherent-order regions of a dense field launch of N rays: whole blocks of B1 = 32 * 2^8 3^5 rays,
+# then blocks of B2 = 32 * 2^7 3^4 over the rest, then the identity order.
+_B1, _B2 = 32 * 256 * 243, 32 * 128 * 81
+
+
+@pytest.mark.parametrize("el,az,parabolic,shape", [(45.0, 0.0, False, 0), (15.0, 0.0, False, 0), (45.0, 0.0, True, 0),
+                                                    (45.0, 0.0, False, 2)],
+                         ids=["flat_45deg", "flat_15deg", "parabolic_45deg", "flat_45deg_accurate"])
+def test_large_field_full_launch_windows_bit_exact(gpu, oracle32, el, az, parabolic, shape):
+    """The 10,000-heliostat field (radial stagger, cylinder receiver at 200 m, pillbox 4.65 mrad,
+    slope error 1.5 mrad) traced at its full size of 268,435,456 rays in one launch through the
+    field grid, against the oracle's brute-force closest hit over all 10,001 elements on windows of
+    50,000 rays: around 2^24 (where the Halton base-2 path changes), across the boundary between the
+    B1 and B2 coherent-order regions, and at the end of the launch (identity-order tail)."""
+    sc = scenes.large_field(sun=scenes.sun_vector(el, az), parabolic=parabolic)
+    sc.sun_shape = shape
+    N = sc.num_rays
+    assert N == 1 << 28
+    full1 = (N // _B1) * _B1
+    t = native.tracer_for(sc, seed=17, instance=3, num_rays=N)
+    try:
+        assert t.accel() == native.ACCEL_GRID
+        t.run()
+        w = 50000
+        for first in ((1 << 24) - w // 2, full1 - w // 2, N - w):
+            hits, ids = t.copy_hits(first, w)
+            oh, oi = oracle32.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, first_ray=first, count=w,
+                                    seed=17, instance=3)
+            np.testing.assert_array_equal(ids, oi, err_msg=f"window at {first}")
+            np.testing.assert_array_equal(hits, oh.astype(np.float32), err_msg=f"window at {first}")
+            assert (oh[:, 1:, 0] == 2).sum() > 1000
+    finally:
+        t.close()
+
+
+def test_large_field_flux_l2_vs_fp64_oracle(gpu, oracle64):
+    """Flux-map L2 of the full-size field trace (268,435,456 rays in one launch) against the FP64
+    oracle with matched seeds, by the same method as the smaller workloads (100 x 100 bins on the
+    cylinder), over a 524,288-ray window of the launch (the FP64 brute force over 10,001 elements
+    bounds the window; ~16 receiver hits per bin).  With the accurate arithmetic flag the float
+    trace is within 1 % (tolerance 0.01).  The reference's float formulas -- the cone sampler's
+    z = cos(a) + (1 - cos(a)) r (~2e-4 rad of direction error, 8 cm at the receiver) and the
+    cylinder's B^2 - 4AC (~1 mm on hit points from mirrors hundreds of metres away) -- move rays
+    across bin edges and stay statistics-limited at this window (asserted below 10 %; the figure
+    falls as 1/sqrt(hits per bin) over the whole launch)."""
+    base = scenes.large_field()
+    N = base.num_rays
+    first, w = 1 << 26, 1 << 19
+    oh, _ = oracle64.trace(base.elements, base.sun_dir, base.sun_shape, base.sun_param, first_ray=first, count=w,
+                           with_ids=False)
+    ref_map = flux_map_from_hits(oh, base.elements[-1], w)
+    del oh
+    l2 = {}
+    for shape in (scenes.SUN_PILLBOX_ACCURATE, scenes.SUN_PILLBOX):
+        sc = scenes.large_field()
+        sc.sun_shape = shape
+        t = native.tracer_for(sc, seed=0, num_rays=N, record_ids=False)
+        try:
+            t.run()
+            hits, _ = t.copy_hits(first, w, with_ids=False)
+        finally:
+            t.close()
+        l2[shape] = flux_l2(flux_map_from_hits(hits, sc.elements[-1], w), ref_map)
+    print("large_field 512k-ray window flux L2 vs FP64: accurate arithmetic", l2[scenes.SUN_PILLBOX_ACCURATE],
+          "reference arithmetic", l2[scenes.SUN_PILLBOX])
+    assert l2[scenes.SUN_PILLBOX_ACCURATE] <= 0.01
+    assert l2[scenes.SUN_PILLBOX] <= 0.10
+
+
+def test_accurate_arithmetic_three_heliostats(gpu, oracle32, oracle64):
+    """CSP_SUN_PILLBOX_ACCURATE on the three-heliostat workload at 1,048,576 rays: bit-identical to
+    the oracle's restatement of the same arithmetic, and flux-map L2 against the FP64 oracle within
+    1 % (tolerance 0.01).  The reference's float cone formula (CSP_SUN_PILLBOX, the default) stays
+    above that bound at this ray count (6.9 %): its float z quantizes 1 - z in steps of 2^-24
+    against 1 - cos(4.65 mrad) = 1.08e-5."""
+    base = scenes.three_heliostats()
+    n = base.num_rays
+    assert n == 1 << 20
+    oh64, _ = oracle64.trace(base.elements, base.sun_dir, base.sun_shape, base.sun_param, count=n, with_ids=False)
+    ref_map = flux_map_from_hits(oh64, base.elements[-1], n)
+    l2 = {}
+    for shape in (scenes.SUN_PILLBOX_ACCURATE, scenes.SUN_PILLBOX):
+        sc = scenes.three_heliostats()
+        sc.sun_shape = shape
+        hits, ids = gpu_trace(sc, n)
+        first, w = 500000, 60000
+        oh, oi = oracle32.trace(sc.elements, sc.sun_dir, shape, sc.sun_param, first_ray=first, count=w)
+        np.testing.assert_array_equal(ids[first:first + w], oi)
+        np.testing.assert_array_equal(hits[first:first + w], oh.astype(np.float32))
+        l2[shape] = flux_l2(flux_map_from_hits(hits, sc.elements[-1], n), ref_map)
+    print("three_heliostats 1M flux L2 vs FP64: accurate sampler", l2[scenes.SUN_PILLBOX_ACCURATE],
+          "reference sampler", l2[scenes.SUN_PILLBOX])
+    assert l2[scenes.SUN_PILLBOX_ACCURATE] <= 0.01
+    assert 0.03 <= l2[scenes.SUN_PILLBOX] <= 0.12
+
+
+def test_ray_windows_past_2_56_rejected(gpu):
+    """The BVH and grid kernels queue rays with their bounce depth in the top 8 bits of the 64-bit
+    ray index, so every entry point rejects a window reaching past 2^56 before any launch
+    (CSP_ERR_INVALID_ARGUMENT): csp_trace_into on an initialized 300-heliostat field, csp_set_num_rays
+    and csp_trace_noalloc.  Nothing is traced."""
+    sc = scenes.large_field(n_heliostats=300)
+    t = native.tracer_for(sc, num_rays=1024)
+    try:
+        for first, count in (((1 << 56) - 10, 1024), ((1 << 64) - 5, 16), (1 << 56, 1)):
+            with pytest.raises(native.CspError) as e:
+                t.trace_into(0x1000, None, first, count)
+            assert e.value.status == -1 and "2^56" in str(e.value)
+        with pytest.raises(native.CspError) as e:
+            t.set_num_rays((1 << 56) + 1)
+        assert e.value.status == -1
+    finally:
+        t.close()
+    small = scenes.three_heliostats()
+    with pytest.raises(native.CspError) as e:
+        native.trace_noalloc(small.elements, small.sun_dir, small.sun_shape, small.sun_param, 0x1000,
+                             first_ray=(1 << 56) - 3, num_rays=8)
+    assert e.value.status == -1
 
 
 def test_flux_map_l2_vs_fp64_oracle(gpu, oracle64):

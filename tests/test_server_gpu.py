@@ -181,3 +181,34 @@ def test_server_ray_indices_beyond_32_bits(gpu):
         assert st_srv[0] == rays and st_srv[3] > 0.02 * rays
     finally:
         b.close()
+
+
+def test_server_destroy_fails_held_requests(gpu):
+    """A request still queued when the server is destroyed (admission held) never runs: a thread
+    blocked waiting on it wakes with CSP_ERR_STATE before the server frees anything, and a second
+    thread waiting on the same id gets an error instead of a result that was already handed out."""
+    import threading
+    from optixsoltracedemos_gb300 import native
+    th = scenes.three_heliostats()
+    srv = native.Server(0, memory_budget=64 << 20, max_active=4)
+    sid = srv.add_scene(th.elements)
+    srv.hold(True)
+    rid = srv.submit(sid, th.sun_dir, th.sun_shape, th.sun_param, 1 << 20, seed=1)
+    errors = []
+
+    def waiter():
+        try:
+            srv.wait(rid)
+        except native.CspError as e:
+            errors.append(e.status)
+
+    threads = [threading.Thread(target=waiter) for _ in range(2)]
+    for t in threads:
+        t.start()
+    import time
+    time.sleep(0.3)
+    srv.close()
+    for t in threads:
+        t.join(timeout=60)
+        assert not t.is_alive()
+    assert sorted(errors) == [-6, -6]

@@ -59,3 +59,27 @@ def test_noalloc_ray_window_and_limits(gpu):
     with pytest.raises(native.CspError) as e:
         native.trace_noalloc(big.elements, big.sun_dir, big.sun_shape, big.sun_param, out.data_ptr(), num_rays=16)
     assert e.value.status == -1 and "8 elements" in str(e.value)
+
+
+def test_noalloc_allocates_no_device_memory(gpu):
+    """The property the entry point exists for: after a first call (which loads the kernels and
+    looks up the scratch array's address), further calls leave the device's free memory unchanged --
+    no cudaMalloc, no Halton table, no staging buffer."""
+    torch = pytest.importorskip("torch")
+    sc = scenes.single_parabolic()
+    n = 1 << 16
+    hits = torch.empty(n * 5 * 4, dtype=torch.float32, device="cuda")
+    ids = torch.empty(n * 5, dtype=torch.int32, device="cuda")
+
+    def call(seed):
+        native.trace_noalloc(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, hits.data_ptr(), ids.data_ptr(),
+                             num_rays=n, seed=seed, device=0, stream=torch.cuda.current_stream().cuda_stream)
+
+    call(0)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for seed in (1, 2, 3):
+        call(seed)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
