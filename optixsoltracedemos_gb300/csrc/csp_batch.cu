@@ -86,10 +86,11 @@ struct BatchSmem {
     unsigned long long want;
 };
 
-// Drain the queue of the current instance and add its record counters to the instance's totals.
+// Drain the queues of the current instance and add its record counters to the instance's totals.
 template <class C>
-__device__ __forceinline__ void finish_instance(BatchSmem<C::kB, C::kAccel>& sm, const Sink& k) {
-    drain<C>(sm.A, k, sm.core, true);  // ends with a barrier
+__device__ __forceinline__ void finish_instance(BatchSmem<C::kB, C::kAccel>& sm, const Sink& k, int& qs, int& gs) {
+    drain<C>(sm.A, k, sm.core, true, qs, gs);
+    __syncthreads();
     if (threadIdx.x > 0 && threadIdx.x < 4) {
         const unsigned long long v = sm.stat[threadIdx.x];
         if (v) atomicAdd(sm.F.stats + threadIdx.x, v);
@@ -122,6 +123,7 @@ __global__ void __launch_bounds__(kB, batch_threads_per_sm<kAccel>() / kB) batch
     const Sink k{&sm.F, sm.stat};
     bool have = false;
     uint64_t t0 = 0, t1 = 0;  // tile range of the current instance
+    int qs = 0, gs = 0;       // queue sizes (see drain)
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -145,7 +147,7 @@ __global__ void __launch_bounds__(kB, batch_threads_per_sm<kAccel>() / kB) batch
                     if (__ldg(L.tile_begin + mid) <= g) lo = mid;
                     else hi = mid - 1;
                 }
-                if (have) finish_instance<C>(sm, k);
+                if (have) finish_instance<C>(sm, k, qs, gs);
                 const uint32_t* src = reinterpret_cast<const uint32_t*>(L.inst + lo);
                 constexpr int kWordsA = sizeof(TraceArgs) / 4, kWordsF = sizeof(FluxTarget) / 4;
                 for (int w = threadIdx.x; w < kWordsA + kWordsF; w += kB) {
@@ -160,10 +162,10 @@ __global__ void __launch_bounds__(kB, batch_threads_per_sm<kAccel>() / kB) batch
                 t0 = __ldg(L.tile_begin + lo);
                 t1 = __ldg(L.tile_begin + lo + 1);
             }
-            trace_tile<C>(sm.A, k, sm.core, nullptr, g - t0);
+            trace_tile<C>(sm.A, k, sm.core, nullptr, g - t0, qs, gs);
         }
     }
-    if (have) finish_instance<C>(sm, k);
+    if (have) finish_instance<C>(sm, k, qs, gs);
 }
 
 template <int kB, int kAccel>

@@ -61,8 +61,10 @@ __global__ void __launch_bounds__(kTraceBlock, 6) trace_kernel(const typename Pl
     __syncthreads();
     const Sink none{nullptr, nullptr};
     const uint64_t tiles = (A.count + kTraceBlock - 1) / kTraceBlock;
-    for (uint64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) trace_tile<C>(A, none, sm.core, &sm.stage, tile);
-    drain<C>(A, none, sm.core, true);
+    int qs = 0, gs = 0;
+    for (uint64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x)
+        trace_tile<C>(A, none, sm.core, &sm.stage, tile, qs, gs);
+    drain<C>(A, none, sm.core, true, qs, gs);
 }
 
 template <int kAccel>

@@ -845,6 +845,8 @@ struct CoreSmem {
     FlatScene flat;
     SunFrame sun;
     GridDesc grid;
+    // next free queue positions (shared atomics hand them out); every thread also carries the
+    // sizes in registers, updated at the barriers that close each append
     int qsize;
     int gsize;
 };
@@ -987,9 +989,12 @@ __device__ void finish_path(const typename C::Args& A, const Sink& k, const type
 }
 
 // One batch of up to kB rays from the top of the bounce queue (qs entries): kFlat launches finish
-// their paths, BVH/grid launches advance them by one bounce.  Ends with a barrier.
+// their paths, BVH/grid launches advance them by one bounce.  Returns the queue size after it, the
+// same in every thread (the barrier that ends the batch counts the rays queued again), so that no
+// thread reads the shared counter after the batch: a warp that has gone on to the next tile may
+// already be appending to it.
 template <class C>
-__device__ __forceinline__ void bounce_batch(const typename C::Args& A, const Sink& k, typename C::Core& sm, int qs) {
+__device__ __forceinline__ int bounce_batch(const typename C::Args& A, const Sink& k, typename C::Core& sm, int qs) {
     {
         const int n = min(qs, C::kB);
         const int base = qs - n;
@@ -1043,16 +1048,19 @@ __device__ __forceinline__ void bounce_batch(const typename C::Args& A, const Si
             }
             push(sm, again, r | ((uint64_t)next.depth << kDepthShift), next.o, next.d, h2.t,
                  (uint32_t)h2.best | (h2.type << kTypeShift));
+            return base + __syncthreads_count(again);
         }
         __syncthreads();
+        return base;
     }
 }
 
 // One batch of up to kB rays from the top of the generation queue (gs entries, kFlat launches):
-// sun direction and box tests; the rays that meet a box go to the bounce queue with their
-// candidate mask.  The bounce queue holds fewer than kB entries on entry.  Ends with a barrier.
+// sun direction and box tests; the rays that meet a box go to the bounce queue (qs entries, fewer
+// than kB on entry) with their candidate mask.  Updates gs and qs, the same in every thread (the
+// closing barrier counts the rays queued).
 template <class C>
-__device__ __forceinline__ void gen_batch(const typename C::Args& A, typename C::Core& sm, int gs) {
+__device__ __forceinline__ void gen_batch(const typename C::Args& A, typename C::Core& sm, int& gs, int& qs) {
     const int n = min(gs, C::kB);
     const int base = gs - n;
     const bool have = (int)threadIdx.x < n;
@@ -1071,29 +1079,24 @@ __device__ __forceinline__ void gen_batch(const typename C::Args& A, typename C:
         m = candidates(sm.flat, o, d, kTminSun);
     }
     push(sm, m != 0u, ray, o, d, 0.0f, m);
-    __syncthreads();
+    qs += __syncthreads_count(m != 0u);
+    gs = base;
 }
 
 // Phase B: run full batches of queued rays (all = also the remainders).  kFlat launches keep the
-// bounce queue below kB before each generation batch, so neither queue exceeds 2 kB.
+// bounce queue below kB before each generation batch, so neither queue exceeds 2 kB.  qs and gs
+// are the sizes of the bounce and generation queues, carried in registers by every thread of the
+// CTA (equal in all of them); the caller has passed a barrier since the last append.
 template <class C>
-__device__ void drain(const typename C::Args& A, const Sink& k, typename C::Core& sm, bool all) {
-    __syncthreads();
-    int qs = sm.qsize;
+__device__ void drain(const typename C::Args& A, const Sink& k, typename C::Core& sm, bool all, int& qs, int& gs) {
     if constexpr (C::kFlat) {
-        int gs = sm.gsize;
         for (;;) {
-            if (qs >= C::kB || (all && qs > 0 && gs == 0)) bounce_batch<C>(A, k, sm, qs);
-            else if (gs >= C::kB || (all && gs > 0)) gen_batch<C>(A, sm, gs);
+            if (qs >= C::kB || (all && qs > 0 && gs == 0)) qs = bounce_batch<C>(A, k, sm, qs);
+            else if (gs >= C::kB || (all && gs > 0)) gen_batch<C>(A, sm, gs, qs);
             else break;
-            qs = sm.qsize;
-            gs = sm.gsize;
         }
     } else {
-        while (qs >= C::kB || (all && qs > 0)) {
-            bounce_batch<C>(A, k, sm, qs);
-            qs = sm.qsize;
-        }
+        while (qs >= C::kB || (all && qs > 0)) qs = bounce_batch<C>(A, k, sm, qs);
     }
 }
 
@@ -1123,10 +1126,10 @@ __device__ __forceinline__ void load_instance_smem(const typename C::Args& A, ty
 }
 
 // Phase A of one tile (rays A.ray_begin + tile * kB ...) followed by phase B on full batches.
-// `stage` is the kDense staging area (unused otherwise).
+// `stage` is the kDense staging area (unused otherwise); qs, gs: the queue sizes (see drain).
 template <class C>
 __device__ __forceinline__ void trace_tile(const typename C::Args& A, const Sink& k, typename C::Core& sm,
-                                           typename C::Stage* stage, uint64_t tile) {
+                                           typename C::Stage* stage, uint64_t tile, int& qs, int& gs) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float4* wh = nullptr;
     uint32_t* wi = nullptr;
@@ -1253,7 +1256,12 @@ __device__ __forceinline__ void trace_tile(const typename C::Args& A, const Sink
             }
         }
     }
-    drain<C>(A, k, sm, false);
+    // the barrier before phase B counts this tile's appends (the bounce queue of BVH/grid launches,
+    // the generation queue of element-list launches)
+    const int added = __syncthreads_count(want);
+    if constexpr (C::kFlat) gs += added;
+    else qs += added;
+    drain<C>(A, k, sm, false, qs, gs);
 }
 
 }  // namespace
