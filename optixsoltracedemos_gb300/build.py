@@ -22,6 +22,7 @@ LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = [
     "csp_kernels.cu",
+    "csp_sungrid.cu",
     "csp_scene.cpp",
     "csp_c_api.cpp",
     "csp_io.cpp",

@@ -6,17 +6,18 @@
 //           parallel threads, written into one pinned staging image of the device arena
 //   device  one CUDA graph: upload the image, zero the flux maps and counters, refit every
 //           instance's BVH (refit_kernel), compute every instance's sun plane
-//           (prepare_sun_batch_kernel), trace the small-scene instances and the BVH instances
-//           (one persistent batch_kernel launch each), copy flux maps, counters and sun frames back
+//           (prepare_sun_batch_kernel) and sun-ray candidate grid (csp_sungrid.cu), trace the
+//           small-scene, BVH and grid instances (one persistent batch_kernel launch per group),
+//           copy flux maps, counters and sun frames back
 // The graph is captured once per batch layout (instances, element counts, ray counts, tuning) and
 // re-launched while the layout is unchanged.  Runs are pipelined over two slots (pinned staging and
 // result buffers, graph, events): run_async builds the next run on the host while the previous one
 // executes, wait completes the oldest run in flight.
 //
 // Arena layout (one cudaMalloc, offsets 16-byte aligned):
-//   upload  [per instance: prims | optics | aabbs | prune] [descs flat | descs bvh]
-//           [tile_begin flat | tile_begin bvh] [refit jobs] [sun jobs]
-//   nodes   per-instance refitted BVH nodes
+//   upload  [per instance: prims | optics | aabbs | prune (| own field grid)] [descs per group]
+//           [tile_begin per group] [refit jobs] [sun jobs] [sun grid jobs]
+//   nodes   per-instance refitted BVH nodes and sun grid (written on the device)
 //   zeroed  [work counters (2)] [stats, 4 x u64 per instance] [counts, nx*ny x u32 per instance]
 //   suns    per-instance SunFrame
 // The download region is [stats .. suns end), one copy.
@@ -174,6 +175,8 @@ int Batch::layout(int si) {
     place.assign(n, Place{});
     for (int g = 0; g < kBatchGroups; ++g) n_group[g] = 0;
     max_nodes = 0;
+    n_sg = 0;
+    max_sg_n = 0;
     size_t off = 0;
     for (size_t i = 0; i < n; ++i) {
         const BScene& s = scenes[inst[i].scene];
@@ -199,6 +202,10 @@ int Batch::layout(int si) {
             off += align16(std::max<size_t>(1, hg.global.size()) * sizeof(Aabb));
         }
         max_nodes = std::max(max_nodes, (int)s.base.nodes.size());
+        if (p.group != kAccelFlat) {
+            p.sg_slot = n_sg++;
+            max_sg_n = std::max(max_sg_n, (int)ne);
+        }
     }
     for (int g = 0; g < kBatchGroups; ++g) {
         desc_off[g] = off;
@@ -212,10 +219,16 @@ int Batch::layout(int si) {
     off += align16(n * sizeof(RefitJob));
     sunjob_off = off;
     off += align16(n * sizeof(SunJob));
+    sgjob_off = off;
+    off += align16((size_t)n_sg * sizeof(SunGridJob));
     up_bytes = off;
     for (size_t i = 0; i < n; ++i) {
         place[i].nodes = off;
         off += align16(scenes[inst[i].scene].base.nodes.size() * sizeof(Node));
+        if (place[i].sg_slot >= 0) {
+            place[i].sgrid = off;
+            off += align16(sungrid_bytes(count_of(i)));
+        }
     }
     zero_off = off;
     counter_off = off;
@@ -342,6 +355,13 @@ void Batch::fill_instance(size_t i) {
     sj.param = (float)b.param;
     sj.out = reinterpret_cast<SunFrame*>(d_arena + p.sun);
     std::memcpy(h_stage + sunjob_off + i * sizeof(SunJob), &sj, sizeof sj);
+    if (p.sg_slot >= 0) {
+        SunGridJob gj;
+        sungrid_place(d_arena + p.sgrid, ne, gj);
+        gj.sun = sj.out;
+        gj.aabbs = rj.aabbs;
+        std::memcpy(h_stage + sgjob_off + (size_t)p.sg_slot * sizeof(SunGridJob), &gj, sizeof gj);
+    }
 }
 
 // Instance descriptors and tile tables of both groups for the given tile sizes; `sample` > 0
@@ -374,6 +394,12 @@ void Batch::fill_descs(const int* block, double sample, std::vector<InstanceDesc
         d.args.pad = 0;
         d.args.grid = nullptr;
         d.args.h3t12 = h3t12;
+        d.args.sgrid = nullptr;
+        if (p.sg_slot >= 0) {
+            SunGridJob gj;
+            sungrid_place(d_arena + p.sgrid, count_of(i), gj);
+            d.args.sgrid = gj.desc;
+        }
         if (g == kAccelGrid) {
             const bool own = !b.poses.empty();
             const BScene& bs = scenes[b.scene];
@@ -428,9 +454,12 @@ int Batch::enqueue_scene_setup(cudaStream_t st) {
                                        max_nodes, st),
                           "refit_kernel")))
         return rc;
-    return cuda_status(launch_prepare_sun_batch(reinterpret_cast<const SunJob*>(d_arena + sunjob_off),
-                                                (int)inst.size(), st),
-                       "prepare_sun_batch_kernel");
+    if ((rc = cuda_status(launch_prepare_sun_batch(reinterpret_cast<const SunJob*>(d_arena + sunjob_off),
+                                                   (int)inst.size(), st),
+                          "prepare_sun_batch_kernel")))
+        return rc;
+    return cuda_status(launch_sungrid_build(reinterpret_cast<const SunGridJob*>(d_arena + sgjob_off), n_sg, max_sg_n, st),
+                       "sun grid build");
 }
 
 // Time the candidate launch parameters of group g on a sample of its instances and keep the

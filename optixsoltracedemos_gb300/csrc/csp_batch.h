@@ -45,6 +45,8 @@ struct BInst {
 struct Place {
     size_t prims = 0, optics = 0, aabbs = 0, prune = 0, nodes = 0, sun = 0, counts = 0, stats = 0;
     size_t cells = 0, items = 0, global = 0;  // own grid arrays (instances with poses in the grid group)
+    size_t sgrid = 0;  // sun-ray candidate grid (BVH and grid groups), built on the device
+    int sg_slot = -1;  // index of its build job
     int group = 0;  // kAccelFlat, kAccelBvh or kAccelGrid: the kernel that traces the instance
     int slot = 0;   // index within the group
 };
@@ -91,7 +93,9 @@ struct Batch {
     std::vector<Place> place;
     size_t up_bytes = 0, zero_off = 0, zero_bytes = 0, res_off = 0, res_bytes = 0;
     size_t desc_off[kBatchGroups] = {}, tb_off[kBatchGroups] = {}, refit_off = 0, sunjob_off = 0, counter_off = 0;
+    size_t sgjob_off = 0;
     int n_group[kBatchGroups] = {};
+    int n_sg = 0, max_sg_n = 0;  // sun grid build jobs and their largest element count
     std::vector<InstBuild> builds;  // per instance, during a run (instances with poses)
     int max_nodes = 0;
 

@@ -73,6 +73,11 @@ void System::release() {
     d_cells = nullptr;
     d_items = d_global = nullptr;
     cap_cells = cap_items = cap_global = 0;
+    cudaFree(d_sgrid);
+    cudaFree(d_sgjob);
+    d_sgrid = nullptr;
+    d_sgjob = nullptr;
+    cap_sgrid = 0;
     cudaFree(d_flux);
     cudaFree(d_fstats);
     d_flux = nullptr;
@@ -151,6 +156,31 @@ int System::prepare_sun() {
                        "prepare_sun_kernel");
 }
 
+// Sun-ray candidate grid of the current poses and sun frame, built on the device behind the sun
+// plane (scenes of more than kFlatListMax elements; the element list needs none).
+int System::build_sungrid() {
+    const uint32_t n = (uint32_t)scene.prims.size();
+    if (n <= kFlatListMax) return CSP_OK;
+    int rc;
+    const size_t bytes = sungrid_bytes(n);
+    if (bytes > cap_sgrid) {
+        cudaFree(d_sgrid);
+        d_sgrid = nullptr;
+        cap_sgrid = 0;
+        if ((rc = cuda_status(cudaMalloc((void**)&d_sgrid, bytes), "cudaMalloc sun grid"))) return rc;
+        cap_sgrid = bytes;
+    }
+    if (!d_sgjob && (rc = cuda_status(cudaMalloc((void**)&d_sgjob, sizeof(SunGridJob)), "cudaMalloc sun grid job")))
+        return rc;
+    sungrid_place(d_sgrid, n, sgjob_host);
+    sgjob_host.sun = d_sun;
+    sgjob_host.aabbs = d_aabbs;
+    if ((rc = cuda_status(cudaMemcpyAsync(d_sgjob, &sgjob_host, sizeof(SunGridJob), cudaMemcpyHostToDevice, stream),
+                          "upload sun grid job")))
+        return rc;
+    return cuda_status(launch_sungrid_build(d_sgjob, 1, (int)n, stream), "sun grid build");
+}
+
 int System::ensure_hit_buffers() {
     if (num_rays > cap_rays || (record_ids && !ids_allocated)) {
         cudaFree(d_hits);
@@ -187,6 +217,7 @@ int System::initialize() {
     if ((rc = upload_scene())) return rc;
     if ((rc = upload_grid(true))) return rc;
     if ((rc = prepare_sun())) return rc;
+    if ((rc = build_sungrid())) return rc;
     if ((rc = ensure_hit_buffers())) return rc;
     if ((rc = cuda_status(cudaStreamSynchronize(stream), "initialize"))) return rc;
     initialized = true;
@@ -210,6 +241,7 @@ int System::update() {
     if ((rc = upload_scene())) return rc;
     if ((rc = upload_grid(true))) return rc;
     if ((rc = prepare_sun())) return rc;
+    if ((rc = build_sungrid())) return rc;
     if ((rc = ensure_hit_buffers())) return rc;
     return cuda_status(cudaStreamSynchronize(stream), "update");
 }
@@ -229,6 +261,7 @@ TraceArgs System::args(uint64_t begin, uint64_t count) const {
     a.pad = 0;
     a.grid = grid.valid ? d_grid : nullptr;
     a.h3t12 = h3t12;
+    a.sgrid = scene.prims.size() > kFlatListMax && d_sgrid ? sgjob_host.desc : nullptr;
     return a;
 }
 

@@ -44,9 +44,18 @@ struct TraceSmem {
     typename PlainCfg<kAccel>::Core core;
 };
 
+// Resident 128-thread CTAs per SM the register budget is cut for: six for the element-list kernel
+// (short latency chains), eight for the BVH and grid kernels (64 registers: more warps to cover
+// the dependent loads of the candidate and cell lists).
+template <int kAccel>
+constexpr int trace_min_blocks() {
+    return kAccel == kAccelFlat ? 6 : 8;
+}
+
 // Persistent kernel over the tiles of one launch (static round robin); dense records out.
 template <int kAccel>
-__global__ void __launch_bounds__(kTraceBlock, 6) trace_kernel(const typename PlainCfg<kAccel>::Args A) {
+__global__ void __launch_bounds__(kTraceBlock, trace_min_blocks<kAccel>()) trace_kernel(
+    const typename PlainCfg<kAccel>::Args A) {
     using C = PlainCfg<kAccel>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TraceSmem<kAccel>& sm = *reinterpret_cast<TraceSmem<kAccel>*>(smem_raw);
@@ -151,6 +160,7 @@ cudaError_t launch_prepare_sun(const Aabb* aabbs, int n, float sx, float sy, flo
 cudaError_t launch_trace(const TraceArgs& args, int n_prims, cudaStream_t stream) {
     if (args.count == 0) return cudaSuccess;
     if (n_prims <= kFlatMax) return launch_trace_t<kAccelFlat>(args, stream);
+    if (!args.sgrid) return cudaErrorInvalidValue;  // scenes above the element list need their sun grid
     if (args.grid) return launch_trace_t<kAccelGrid>(args, stream);
     return launch_trace_t<kAccelBvh>(args, stream);
 }

@@ -26,6 +26,7 @@ struct TraceArgs {
     int pad;
     const GridDesc* grid;  // field grid of the scene, nullptr: BVH (or element list) traversal
     const float* h3t12;    // Halton base-3 partial sums after 12 digits (halton3_table), or nullptr
+    const SunGrid* sgrid;  // candidate grid of the sun rays (scenes of more than 8 elements)
 };
 
 // Arguments of the single-scene element-list kernel: TraceArgs plus the Philox key schedule of
@@ -44,8 +45,43 @@ const float* halton3_table();
 cudaError_t launch_prepare_sun(const Aabb* aabbs, int n, float sx, float sy, float sz, float tan_pad, int shape,
                                float param, SunFrame* out, cudaStream_t stream);
 
+// Sun-ray candidate grid of one scene state (SunGrid): device arrays of its build and where its
+// descriptor goes.  All of it is written by launch_sungrid_build (nothing needs zeroing).
+struct SunGridJob {
+    SunGrid* desc;            // the descriptor the trace reads (TraceArgs::sgrid)
+    const SunFrame* sun;      // sun frame of the state (prepare_sun output)
+    const Aabb* aabbs;        // [n] exact boxes, lo.w = element | type << kTypeShift
+    int n;
+    int cap_cells;            // cell_start holds cap_cells + 1 entries, cursor cap_cells
+    uint32_t cap_items;
+    int pad;
+    uint32_t* cell_start;
+    uint32_t* cursor;
+    float4* rect;             // [n]
+    float4* item_rect;        // [cap_items]
+    uint32_t* item_id;        // [cap_items]
+    uint32_t* global_id;      // [n]
+};
+
+// Capacities of the sun grid of an n-element scene and the device bytes of its arrays (each array
+// 256-byte aligned, in the order of sungrid_place), descriptor included.
+struct SunGridCaps {
+    int cap_cells;
+    uint32_t cap_items;
+};
+SunGridCaps sungrid_caps(uint32_t n);
+size_t sungrid_bytes(uint32_t n);
+// Carve the arrays of an n-element scene's sun grid out of `base` (sungrid_bytes(n) bytes, 256-byte
+// aligned); fills every SunGridJob field except sun and aabbs.
+void sungrid_place(unsigned char* base, uint32_t n, SunGridJob& job);
+
+// Build the sun grids of n_jobs scene states (jobs: device array) on `stream`: reach rectangles and
+// grid size, counts, prefix sums, fill.  max_n = the largest element count among the jobs.
+cudaError_t launch_sungrid_build(const SunGridJob* jobs, int n_jobs, int max_n, cudaStream_t stream);
+
 // Trace rays [ray_begin, ray_begin + count): generation, closest-hit search, shading, the dense
-// hit-record write.  Scenes of up to 8 elements (n_prims) take the shared-memory element list path.
+// hit-record write.  Scenes of up to 8 elements (n_prims) take the shared-memory element list path;
+// larger ones need args.sgrid.
 cudaError_t launch_trace(const TraceArgs& args, int n_prims, cudaStream_t stream);
 
 // Bin the stage-2 records of a dense hit buffer into F.counts and count records into F.stats[1..3]

@@ -153,6 +153,7 @@ extern "C" int csp_trace_noalloc(int device, const csp_element* elements, uint32
             a.pad = 0;
             a.grid = nullptr;
             a.h3t12 = nullptr;
+            a.sgrid = nullptr;
             rc = cuda_status(launch_trace(a, (int)count, st), "csp_trace_noalloc: trace_kernel");
         }
     }

@@ -276,6 +276,8 @@ int build_elements(const csp_element* el, uint32_t n, HostScene& s, std::string&
     for (uint32_t i = 0; i < n; ++i) {
         const char* why = "";
         const int rc = pack_element(el[i], i + 1 == n, s.types[i], s.aabbs[i], s.prims[i], s.optics[i], &s.prune[i], why);
+        // the exact box carries its element and entity type (the sun grid's candidate tests)
+        s.aabbs[i].lo.w = u2f((s.types[i] << kTypeShift) | i);
         if (rc) {
             err = "element " + std::to_string(i) + ": " + why;
             if (el[i].surface != CSP_SURFACE_FLAT && el[i].surface != CSP_SURFACE_PARABOLIC &&

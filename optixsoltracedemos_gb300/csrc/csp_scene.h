@@ -13,7 +13,7 @@ namespace csp {
 struct HostScene {
     std::vector<Prim> prims;      // per element, element order
     std::vector<Optics> optics;   // per element
-    std::vector<Aabb> aabbs;      // exact element AABBs (float), element order
+    std::vector<Aabb> aabbs;      // exact element AABBs (float), element order; lo.w = element | type << 28 (bits)
     std::vector<Aabb> prune;      // boxes bounding each element's surface (sag, rounding margin)
     std::vector<uint32_t> types;  // EntityType per element
     std::vector<Node> nodes;      // traversal order

@@ -9,15 +9,15 @@
 //      counters and sun frame to pinned host memory behind the launch;
 //   2. while the GPU runs: admit pending requests while slots and device memory allow -- host
 //      element builds (the reference's geometry arithmetic, as the single-scene path), upload,
-//      refit of the scene's BVH topology in place into the request's nodes, sun plane; all queued on
-//      the stream behind step k, so the request joins step k+1;
+//      refit of the scene's BVH topology in place into the request's nodes, sun plane, sun-ray
+//      candidate grid; all queued on the stream behind step k, so the request joins step k+1;
 //   3. wait for the step, complete the finished requests (latency = completion - submission), free
 //      their device memory.
 // A request's result does not depend on what it was batched with or how its rays were sliced: its
 // rays are traced with the same (seed, instance, ray index) and its flux map is an integer sum.
 //
 // Device memory: one arena of the configured budget, first-fit blocks per request (element
-// records when the request has its own poses, refitted nodes, sun frame, flux map).  A request is
+// records when the request has its own poses, refitted nodes, sun frame, sun grid, flux map).  A request is
 // admitted when its block fits; requests larger than the whole budget fail.
 #include <algorithm>
 #include <chrono>
@@ -86,7 +86,7 @@ struct SRequest {
     int group = kAccelBvh;
     size_t off = 0, bytes = 0;  // arena block
     size_t o_prims = 0, o_optics = 0, o_aabbs = 0, o_prune = 0, o_nodes = 0, o_sun = 0, o_grid = 0, o_counts = 0,
-           o_stats = 0, o_cells = 0, o_items = 0, o_global = 0;
+           o_stats = 0, o_cells = 0, o_items = 0, o_global = 0, o_sgrid = 0;
     bool own_records = false;
     int result_slot = -1;
     Clock::time_point t_submit, t_admit, t_done;
@@ -153,7 +153,7 @@ struct Server {
     std::deque<SRequest*> pending;
     std::vector<SRequest*> active;
     uint64_t next_id = 1;
-    // refit and sun-plane job tables of one admission round (at most max_active requests); the
+    // refit, sun-plane and sun-grid job tables of one admission round (at most max_active requests); the
     // kernels that read them finish at the step synchronisation before the next round
     unsigned char* d_jobs = nullptr;
     size_t jobs_cap = 0;
@@ -269,7 +269,8 @@ int Server::start(int dev, size_t budget_bytes, int max_act, uint64_t step_targe
     if ((rc = cuda_status(cudaHostAlloc((void**)&h_step, step_bytes, cudaHostAllocDefault), "cudaHostAlloc"))) return rc;
     if ((rc = cuda_status(cudaMalloc((void**)&d_counter, kBatchGroups * sizeof(unsigned long long)), "cudaMalloc")))
         return rc;
-    jobs_cap = align256((size_t)max_active * sizeof(RefitJob)) + align256((size_t)max_active * sizeof(SunJob));
+    jobs_cap = align256((size_t)max_active * sizeof(RefitJob)) + align256((size_t)max_active * sizeof(SunJob)) +
+               align256((size_t)max_active * sizeof(SunGridJob));
     if ((rc = cuda_status(cudaMalloc((void**)&d_jobs, jobs_cap), "cudaMalloc job tables"))) return rc;
     res_slot_bytes = align256((size_t)nx * ny * sizeof(uint32_t) + 4 * sizeof(unsigned long long) + sizeof(SunFrame));
     if ((rc = cuda_status(cudaHostAlloc((void**)&h_res, res_slot_bytes * max_active, cudaHostAllocDefault),
@@ -316,6 +317,7 @@ size_t Server::request_bytes(const SRequest& r) const {
     const size_t n = s.elements.size();
     size_t b = align256(sizeof(SunFrame)) + align256(sizeof(GridDesc)) + align256((size_t)nx * ny * sizeof(uint32_t)) +
                align256(4 * sizeof(unsigned long long));
+    if (r.group != kAccelFlat) b += align256(sungrid_bytes((uint32_t)n));
     if (!r.poses.empty()) {
         b += align256(n * sizeof(Prim)) + align256(n * sizeof(Optics)) + 2 * align256(n * sizeof(Aabb));
         if (r.group != kAccelGrid) b += align256(s.base.nodes.size() * sizeof(Node));
@@ -406,6 +408,10 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
         o += align256((size_t)nx * ny * sizeof(uint32_t));
         r.o_stats = o;
         o += align256(4 * sizeof(unsigned long long));
+        if (r.group != kAccelFlat) {
+            r.o_sgrid = o;
+            o += align256(sungrid_bytes((uint32_t)n));
+        }
         r.own_records = !r.poses.empty();
         if (r.own_records) {
             r.o_prims = o;
@@ -440,6 +446,8 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
     stage += align256(admitted.size() * sizeof(RefitJob));
     const size_t sun_at = stage;
     stage += align256(admitted.size() * sizeof(SunJob));
+    const size_t sg_at = stage;
+    stage += align256(admitted.size() * sizeof(SunGridJob));
     if (stage > adm_cap) {
         // the previous round's uploads from h_adm finished at the step synchronisation before this call
         if (h_adm) cudaFreeHost(h_adm);
@@ -451,7 +459,8 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
     }
     RefitJob* refits = reinterpret_cast<RefitJob*>(h_adm + refit_at);
     SunJob* suns = reinterpret_cast<SunJob*>(h_adm + sun_at);
-    int n_refit = 0, n_sun = 0, max_nodes = 0;
+    SunGridJob* sgs = reinterpret_cast<SunGridJob*>(h_adm + sg_at);
+    int n_refit = 0, n_sun = 0, max_nodes = 0, n_sg = 0, max_sg_n = 0;
     for (size_t i = 0; i < admitted.size(); ++i) {
         SRequest& r = *admitted[i];
         const SScene& s = *r.sc;
@@ -522,6 +531,13 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
         sj.shape = r.shape;
         sj.param = (float)r.param;
         sj.out = reinterpret_cast<SunFrame*>(d_arena + r.o_sun);
+        if (r.group != kAccelFlat) {
+            SunGridJob& gj = sgs[n_sg++];
+            sungrid_place(d_arena + r.o_sgrid, n, gj);
+            gj.sun = sj.out;
+            gj.aabbs = d_aabbs;
+            max_sg_n = std::max(max_sg_n, (int)n);
+        }
         int rc2 = cuda_status(cudaMemsetAsync(d_arena + r.o_counts, 0, (size_t)nx * ny * sizeof(uint32_t), stream), "memset");
         if (!rc2) rc2 = cuda_status(cudaMemsetAsync(d_arena + r.o_stats, 0, 4 * sizeof(unsigned long long), stream), "memset");
         if (rc2) return rc2;
@@ -540,6 +556,10 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
         rc = cuda_status(
             launch_prepare_sun_batch(reinterpret_cast<const SunJob*>(d_jobs + (sun_at - refit_at)), n_sun, stream),
             "prepare_sun_batch_kernel");
+    if (!rc && n_sg)
+        rc = cuda_status(launch_sungrid_build(reinterpret_cast<const SunGridJob*>(d_jobs + (sg_at - refit_at)), n_sg,
+                                              max_sg_n, stream),
+                         "sun grid build");
     return rc;
 }
 
@@ -581,6 +601,12 @@ int Server::step_launch(std::vector<SRequest*>& finishing, uint64_t& rays) {
             d.args.pad = 0;
             d.args.grid = g == kAccelGrid ? reinterpret_cast<const GridDesc*>(d_arena + r->o_grid) : nullptr;
             d.args.h3t12 = h3t12;
+            d.args.sgrid = nullptr;
+            if (g != kAccelFlat) {
+                SunGridJob gj;
+                sungrid_place(d_arena + r->o_sgrid, (uint32_t)s.elements.size(), gj);
+                d.args.sgrid = gj.desc;
+            }
             const csp_element& rcv = (r->poses.empty() ? s.elements : r->poses).back();
             flux_target(rcv, nx, ny, d.flux);
             d.flux.staged = (r->out_flags & CSP_OUT_STAGED) ? 1 : 0;

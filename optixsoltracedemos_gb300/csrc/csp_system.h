@@ -59,6 +59,12 @@ struct System {
     Aabb* d_items = nullptr;
     Aabb* d_global = nullptr;
     size_t cap_cells = 0, cap_items = 0, cap_global = 0;
+    // sun-ray candidate grid (scenes of more than kFlatListMax elements): its arrays, and the build
+    // job (host copy = source of the async upload)
+    unsigned char* d_sgrid = nullptr;
+    size_t cap_sgrid = 0;
+    SunGridJob* d_sgjob = nullptr;
+    SunGridJob sgjob_host{};
     uint32_t* d_flux = nullptr;              // csp_flux_map counts
     unsigned long long* d_fstats = nullptr;  // [4]
     size_t cap_flux = 0;
@@ -79,6 +85,7 @@ struct System {
     int upload_scene();
     int upload_grid(bool arrays);
     int prepare_sun();
+    int build_sungrid();
     float pad_angle() const;
     int ensure_hit_buffers();
     int initialize();

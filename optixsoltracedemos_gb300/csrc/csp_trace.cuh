@@ -46,10 +46,8 @@ constexpr float kTwoPiF = 0x1.921fb6p+2f;                  // fl32(2 pi), flux a
 constexpr int kFlatMax = 8;
 constexpr uint32_t kH3TabDigits = 6, kH3Tab = 729;
 
-template <int kB, bool kGen>
+template <int kB, bool kFlat>
 struct CoreSmem;
-template <int kB>
-struct StageSmem;
 template <int kB>
 struct FlatStageSmem;
 
@@ -68,11 +66,12 @@ struct Cfg {
     // arguments from shared memory)
     static constexpr bool kSched = kAccel_ == kAccelFlat && kDense_;
     using Args = std::conditional_t<kSched, TraceArgsK, TraceArgs>;
-    // element-list launches defer the direction of sun rays whose sun-plane point may reach an
-    // element box to full batches (the generation queue); the other rays provably miss
+    // every launch defers the direction of the sun rays whose sun-plane point may reach an element
+    // box to full batches (the generation queue); the other rays provably miss.  Element-list
+    // launches test the reach rectangles of their elements, the others the sun grid (SunGrid).
     using Core = CoreSmem<kB_, kFlat>;
-    // phase A record staging of dense launches
-    using Stage = std::conditional_t<kFlat, FlatStageSmem<kB_>, StageSmem<kB_>>;
+    // phase A record staging of dense element-list launches
+    using Stage = FlatStageSmem<kB_>;
 };
 
 // Coherent ray order: position kk of a launch of `count` rays -> ray offset.  Rays come in blocks
@@ -92,34 +91,47 @@ constexpr uint64_t kCoherentS1 = 256u * 243u, kCoherentB1 = 32u * kCoherentS1;
 constexpr uint64_t kCoherentS2 = 128u * 81u, kCoherentB2 = 32u * kCoherentS2;
 
 // warp position m in a block of S warps for the warp at index r >> 5 of the block (G | S)
-template <int G>
-__device__ __forceinline__ uint64_t coherent_warp(uint64_t r, uint64_t S) {
-    const uint64_t w = r >> 5;
+template <int G, class U>
+__device__ __forceinline__ U coherent_warp(U r, U S) {
+    const U w = r >> 5;
     if constexpr (G == 1) return w;
     else return (w % G) * (S / G) + w / G;
 }
 
-template <bool kFine, int G>
-__device__ __forceinline__ uint64_t coherent_order(uint64_t kk, uint64_t count) {
+template <bool kFine, int G, class U>
+__device__ __forceinline__ U coherent_order_t(U kk, U count) {
     static_assert(G == 1 || G == 2 || G == 4 || G == 8 || G == 16, "warp groups must divide every S");
-    const uint64_t full0 = kFine ? (count / kCoherentB0) * kCoherentB0 : 0;
-    if (kk < full0) {
-        const uint64_t blk = kk / kCoherentB0, r = kk - blk * kCoherentB0;
-        return blk * kCoherentB0 + coherent_warp<G>(r, kCoherentS0) + (r & 31u) * kCoherentS0;
+    constexpr U B0 = (U)kCoherentB0, S0 = (U)kCoherentS0, B1 = (U)kCoherentB1, S1 = (U)kCoherentS1;
+    constexpr U B2 = (U)kCoherentB2, S2 = (U)kCoherentS2;
+    U full0 = 0;
+    if constexpr (kFine) {
+        full0 = (count / B0) * B0;
+        if (kk < full0) {
+            const U blk = kk / B0, r = kk - blk * B0;
+            return blk * B0 + (U)coherent_warp<G>(r, S0) + (r & 31u) * S0;
+        }
     }
-    const uint64_t k1 = kk - full0, c1 = count - full0;
-    const uint64_t full1 = (c1 / kCoherentB1) * kCoherentB1;
+    const U k1 = kk - full0, c1 = count - full0;
+    const U full1 = (c1 / B1) * B1;
     if (k1 < full1) {
-        const uint64_t blk = k1 / kCoherentB1, r = k1 - blk * kCoherentB1;
-        return full0 + blk * kCoherentB1 + coherent_warp<G>(r, kCoherentS1) + (r & 31u) * kCoherentS1;
+        const U blk = k1 / B1, r = k1 - blk * B1;
+        return full0 + blk * B1 + (U)coherent_warp<G>(r, S1) + (r & 31u) * S1;
     }
-    const uint64_t k2 = k1 - full1;
-    const uint64_t full2 = ((c1 - full1) / kCoherentB2) * kCoherentB2;
+    const U k2 = k1 - full1;
+    const U full2 = ((c1 - full1) / B2) * B2;
     if (k2 < full2) {
-        const uint64_t blk = k2 / kCoherentB2, r = k2 - blk * kCoherentB2;
-        return full0 + full1 + blk * kCoherentB2 + coherent_warp<G>(r, kCoherentS2) + (r & 31u) * kCoherentS2;
+        const U blk = k2 / B2, r = k2 - blk * B2;
+        return full0 + full1 + blk * B2 + (U)coherent_warp<G>(r, S2) + (r & 31u) * S2;
     }
     return kk;
+}
+
+// Launches of fewer than 2^32 rays (all but the largest) take the 32-bit form: the same
+// arithmetic, without the cost of 64-bit division by the block sizes.
+template <bool kFine, int G>
+__device__ __forceinline__ uint64_t coherent_order(uint64_t kk, uint64_t count) {
+    if (count <= 0xFFFFFFFFull) return coherent_order_t<kFine, G, uint32_t>((uint32_t)kk, (uint32_t)count);
+    return coherent_order_t<kFine, G, uint64_t>(kk, count);
 }
 
 // ------------------------------------------------------------------------------ sun plane -----
@@ -227,13 +239,13 @@ __device__ void sun_frame_block(const Aabb* __restrict__ aabbs, int n, float3 s,
 
 // ------------------------------------------------------------------------------ sampling ------
 // Halton radical inverse, cuda/sun.cu:16-24: f /= b; r += f * (i mod b); i /= b, in float.
+// The loop's partial sum after its first 24 digits (the low 24 bits of i) is a dyadic fraction of
+// at most 24 bits, so every step so far was exact and the sum equals the bit-reversed low bits
+// scaled by 2^-32; the loop then goes on from that state (f = 2^-24) over the remaining digits.
 __device__ __forceinline__ float halton2(uint64_t i) {
-    if (i < (1ull << 24)) {
-        // every partial sum is a dyadic fraction of at most 24 bits, so the float loop is exact and
-        // equals the bit-reversed index scaled by 2^-32
-        return (float)__brev((uint32_t)i) * 0x1p-32f;
-    }
-    float f = 1.0f, r = 0.0f;
+    float r = (float)__brev((uint32_t)i & 0xFFFFFFu) * 0x1p-32f;
+    i >>= 24;
+    float f = 0x1p-24f;
     while (i > 0) {
         f = f * 0.5f;  // f / 2 is exact
         r = r + f * (float)(uint32_t)(i & 1u);
@@ -585,6 +597,56 @@ __device__ __forceinline__ int traverse_grid(const GridDesc& G, const Prim* __re
     return best;
 }
 
+// ------------------------------------------------------------------------------ sun grid ------
+// Cell index of a Halton coordinate x in [0, 1] along an axis of n cells (f = n as a float).  The
+// build registers a rectangle [lo, hi] in cells sg_cell(max(lo, 0)) .. sg_cell(min(hi, 1)); float
+// multiplication and truncation are monotonic, so a point x with lo <= x <= hi lies in one of them.
+__device__ __forceinline__ int sg_cell(float x, float f, int n) { return min((int)(x * f), n - 1); }
+
+__device__ __forceinline__ bool in_rect(float4 r, float u, float v) {
+    return (u >= r.x) & (u <= r.y) & (v >= r.z) & (v <= r.w);
+}
+
+// Whether some element's reach rectangle holds the sun-plane point (u, v): only then can the ray
+// meet an element box (otherwise its record is the sun-plane point alone).
+__device__ __forceinline__ bool sun_reach_any(const SunGrid& G, float u, float v) {
+    const int c = sg_cell(v, G.fnv, G.nv) * G.nu + sg_cell(u, G.fnu, G.nu);
+    uint32_t j = __ldg(G.cell_start + c);
+    const uint32_t e = __ldg(G.cell_start + c + 1);
+    for (; j < e; ++j)
+        if (in_rect(__ldg(G.item_rect + j), u, v)) return true;
+    for (int k = 0; k < G.n_global; ++k)
+        if (in_rect(__ldg(G.rect + __ldg(G.global_id + k)), u, v)) return true;
+    return false;
+}
+
+// Closest hit of the sun ray leaving the plane at (u, v) = o with direction d: the elements of its
+// cell and of the global list whose reach rectangles hold (u, v), each through the exact AABB test
+// and its intersection program (test_box).  Every element whose box the ray meets is among them,
+// so this is the closest hit over all elements (equal t keeps the lower element index).
+__device__ __forceinline__ int sun_closest(const SunGrid& G, const Prim* __restrict__ prims, float u, float v,
+                                           float3 o, float3 d, bool acc, float& best_t, uint32_t& best_type) {
+    const float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    int best = -1;
+    best_t = __int_as_float(0x7f800000);
+    float prune = kTmax;
+    const int c = sg_cell(v, G.fnv, G.nv) * G.nu + sg_cell(u, G.fnu, G.nu);
+    uint32_t j = __ldg(G.cell_start + c);
+    const uint32_t e = __ldg(G.cell_start + c + 1);
+    for (; j < e; ++j) {
+        if (!in_rect(__ldg(G.item_rect + j), u, v)) continue;
+        const float4* q = reinterpret_cast<const float4*>(G.aabbs + __ldg(G.item_id + j));
+        test_box(__ldg(q), __ldg(q + 1), prims, o, d, inv, kTminSun, acc, best, best_t, best_type, prune);
+    }
+    for (int k = 0; k < G.n_global; ++k) {
+        const uint32_t id = __ldg(G.global_id + k);
+        if (!in_rect(__ldg(G.rect + id), u, v)) continue;
+        const float4* q = reinterpret_cast<const float4*>(G.aabbs + id);
+        test_box(__ldg(q), __ldg(q + 1), prims, o, d, inv, kTminSun, acc, best, best_t, best_type, prune);
+    }
+    return best;
+}
+
 // ------------------------------------------------------------------------------ flux bins -----
 // Bin of a receiver record at world point p, or -1 for a cylinder cap hit (see FluxTarget).
 __device__ __forceinline__ int flux_bin(const FluxTarget& F, float3 p) {
@@ -768,13 +830,6 @@ __device__ __forceinline__ float3 sun_direction(const typename C::Args& A, const
     return dir;
 }
 
-template <class C>
-__device__ __forceinline__ Segment generate(const typename C::Args& A, const SunFrame& S, uint64_t ray,
-                                           const float* t6) {
-    const float hu = halton2(ray), hv = halton3_tab(ray, t6, A.h3t12);
-    return Segment{sun_point(S, hu, hv), sun_direction<C>(A, S, ray), kTminSun, 0};
-}
-
 // Reach rectangle of one element box: Halton coordinates (u in [x, y], v in [z, w]) outside which
 // no sun ray can meet the box.  A ray leaves the sun plane at o = v0 + u e1 + v e2 with a direction
 // at most a from the cone axis w; at depth h below the plane it has moved at most h tan a across
@@ -829,22 +884,23 @@ constexpr int kDepthShift = 56;
 constexpr uint64_t kRayMask = (1ull << kDepthShift) - 1u;
 static_assert((1ull << kDepthShift) == kRayIndexLimit, "the host ray-window check must match the packing");
 
-// Shared memory of one CTA: the ray queue, the Halton table, the sun frame and the kFlat scene;
-// with kGen also the generation queue (sun rays waiting for their direction) and the reach
-// rectangles of the elements.
-template <int kB, bool kGen>
+// Shared memory of one CTA: the bounce queue, the generation queue (sun rays waiting for their
+// direction: kFlat launches keep the sun-plane point, the others its Halton coordinates), the
+// Halton table, the sun frame, and the kFlat scene with its elements' reach rectangles or the
+// descriptors of the grids of the other launches.
+template <int kB, bool kFlat>
 struct CoreSmem {
-    static constexpr int kG = kGen ? 2 * kB : 1;
     float qo[3][2 * kB], qd[3][2 * kB], qt[2 * kB];
     uint32_t qw[2 * kB];  // kFlat: candidate mask; BVH: element | type << 28 of the pending mirror hit
     uint64_t qray[2 * kB];
-    float go[3][kG];
-    uint64_t gray[kG];
-    float4 reach[kGen ? kFlatMax : 1];
+    float go[3][2 * kB];
+    uint64_t gray[2 * kB];
+    float4 reach[kFlat ? kFlatMax : 1];
     float t6[kH3Tab];
     FlatScene flat;
     SunFrame sun;
     GridDesc grid;
+    SunGrid sg;
     // next free queue positions (shared atomics hand them out); every thread also carries the
     // sizes in registers, updated at the barriers that close each append
     int qsize;
@@ -860,15 +916,8 @@ __device__ __forceinline__ int find_closest(const typename C::Args& A, const typ
     else return traverse(A.nodes, A.prims, o, d, tmin, acc, t, type);
 }
 
-// Phase A record staging of the kDense sink, ray-major per warp.
-template <int kB>
-struct StageSmem {
-    float4 hits[kB * kMaxDepth];
-    uint32_t ids[kB * kMaxDepth];
-};
-
-// kFlat launches: phase A produces slot 0 of each row only (the sun-plane record); the other slots
-// are empty until phase B writes them straight to global memory.
+// Dense element-list launches: phase A produces slot 0 of each row only (the sun-plane record);
+// the other slots are empty until phase B writes them straight to global memory.
 template <int kB>
 struct FlatStageSmem {
     float4 rec0[kB];
@@ -1055,52 +1104,77 @@ __device__ __forceinline__ int bounce_batch(const typename C::Args& A, const Sin
     }
 }
 
-// One batch of up to kB rays from the top of the generation queue (gs entries, kFlat launches):
-// sun direction and box tests; the rays that meet a box go to the bounce queue (qs entries, fewer
-// than kB on entry) with their candidate mask.  Updates gs and qs, the same in every thread (the
-// closing barrier counts the rays queued).
+// One batch of up to kB rays from the top of the generation queue (gs entries): sun direction and
+// the closest-hit search of the first segment, on full warps.  Element-list launches run the box
+// tests and queue the rays that meet a box with their candidate mask; the others find the closest
+// hit among the sun-grid candidates, emit its record and queue mirror hits for shading.  Both append
+// to the bounce queue (qs entries, fewer than kB on entry).  Updates gs and qs, the same in every
+// thread (the closing barrier counts the rays queued).
 template <class C>
-__device__ __forceinline__ void gen_batch(const typename C::Args& A, typename C::Core& sm, int& gs, int& qs) {
+__device__ __forceinline__ void gen_batch(const typename C::Args& A, const Sink& k, typename C::Core& sm, int& gs,
+                                          int& qs) {
     const int n = min(gs, C::kB);
     const int base = gs - n;
     const bool have = (int)threadIdx.x < n;
-    float3 o = f3(0.f, 0.f, 0.f), d = f3(0.f, 0.f, 1.f);
+    float a = 0.f, b = 0.f, c = 0.f;
     uint64_t ray = 0;
     if (have) {
         const int q = base + threadIdx.x;
-        o = f3(sm.go[0][q], sm.go[1][q], sm.go[2][q]);
+        a = sm.go[0][q];
+        b = sm.go[1][q];
+        c = sm.go[2][q];
         ray = sm.gray[q];
     }
     __syncthreads();
     if (threadIdx.x == 0) sm.gsize = base;
-    uint32_t m = 0;
-    if (have) {
-        d = sun_direction<C>(A, sm.sun, ray);
-        m = candidates(sm.flat, o, d, kTminSun);
+    if constexpr (C::kFlat) {
+        const float3 o = f3(a, b, c);
+        float3 d = f3(0.f, 0.f, 1.f);
+        uint32_t m = 0;
+        if (have) {
+            d = sun_direction<C>(A, sm.sun, ray);
+            m = candidates(sm.flat, o, d, kTminSun);
+        }
+        push(sm, m != 0u, ray, o, d, 0.0f, m);
+        qs += __syncthreads_count(m != 0u);
+    } else {
+        // (a, b) = the Halton coordinates of the ray's sun-plane point
+        bool again = false;
+        Segment g{f3(0.f, 0.f, 0.f), f3(0.f, 0.f, 1.f), kTminSun, 0};
+        Hit h{-1, 0.f, 0u};
+        if (have) {
+            g.o = sun_point(sm.sun, a, b);
+            g.d = sun_direction<C>(A, sm.sun, ray);
+            h.best = sun_closest(sm.sg, A.prims, a, b, g.o, g.d, (sm.sun.shape & 2) != 0, h.t, h.type);
+            if (h.best >= 0) {
+                const Prim p = load_prim(A.prims, (uint32_t)h.best);
+                float4 rec;
+                int s;
+                again = classify(p, g, h, rec, s);
+                if (s >= 0) emit<C>(A, k, ray, s, rec, (uint32_t)h.best);
+            }
+        }
+        push(sm, again, ray, g.o, g.d, h.t, (uint32_t)h.best | (h.type << kTypeShift));
+        qs += __syncthreads_count(again);
     }
-    push(sm, m != 0u, ray, o, d, 0.0f, m);
-    qs += __syncthreads_count(m != 0u);
     gs = base;
 }
 
-// Phase B: run full batches of queued rays (all = also the remainders).  kFlat launches keep the
-// bounce queue below kB before each generation batch, so neither queue exceeds 2 kB.  qs and gs
+// Phase B: run full batches of queued rays (all = also the remainders).  The bounce queue is below
+// kB before each generation batch (a bounce batch never grows it), so neither queue exceeds 2 kB.  qs and gs
 // are the sizes of the bounce and generation queues, carried in registers by every thread of the
 // CTA (equal in all of them); the caller has passed a barrier since the last append.
 template <class C>
 __device__ void drain(const typename C::Args& A, const Sink& k, typename C::Core& sm, bool all, int& qs, int& gs) {
-    if constexpr (C::kFlat) {
-        for (;;) {
-            if (qs >= C::kB || (all && qs > 0 && gs == 0)) qs = bounce_batch<C>(A, k, sm, qs);
-            else if (gs >= C::kB || (all && gs > 0)) gen_batch<C>(A, sm, gs, qs);
-            else break;
-        }
-    } else {
-        while (qs >= C::kB || (all && qs > 0)) qs = bounce_batch<C>(A, k, sm, qs);
+    for (;;) {
+        if (qs >= C::kB || (all && qs > 0 && gs == 0)) qs = bounce_batch<C>(A, k, sm, qs);
+        else if (gs >= C::kB || (all && gs > 0)) gen_batch<C>(A, k, sm, gs, qs);
+        else break;
     }
 }
 
-// Per-CTA setup of an instance: sun frame and (kFlat) the element list into shared memory.
+// Per-CTA setup of an instance: sun frame and the kFlat element list or the grid descriptors into
+// shared memory.
 // Callers synchronise before the first use.
 template <class C>
 __device__ __forceinline__ void load_instance_smem(const typename C::Args& A, typename C::Core& sm) {
@@ -1123,98 +1197,69 @@ __device__ __forceinline__ void load_instance_smem(const typename C::Args& A, ty
     }
     if (C::kAccel == kAccelGrid && threadIdx.x < sizeof(GridDesc) / 4)
         reinterpret_cast<uint32_t*>(&sm.grid)[threadIdx.x] = reinterpret_cast<const uint32_t*>(A.grid)[threadIdx.x];
+    if (!C::kFlat && threadIdx.x >= 64 && threadIdx.x < 64 + sizeof(SunGrid) / 4)
+        reinterpret_cast<uint32_t*>(&sm.sg)[threadIdx.x - 64] =
+            reinterpret_cast<const uint32_t*>(A.sgrid)[threadIdx.x - 64];
 }
 
 // Phase A of one tile (rays A.ray_begin + tile * kB ...) followed by phase B on full batches.
-// `stage` is the kDense staging area (unused otherwise); qs, gs: the queue sizes (see drain).
+// `stage` is the kDense staging area of element-list launches (unused otherwise); qs, gs: the queue
+// sizes (see drain).
 template <class C>
 __device__ __forceinline__ void trace_tile(const typename C::Args& A, const Sink& k, typename C::Core& sm,
                                            typename C::Stage* stage, uint64_t tile, int& qs, int& gs) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float4* wh = nullptr;
-    uint32_t* wi = nullptr;
-    float4* slot = nullptr;
-    uint32_t* id = nullptr;
-    if constexpr (C::kDense && C::kFlat) {
-        wh = stage->rec0 + warp * 32;
-    } else if constexpr (C::kDense) {
-        wh = stage->hits + warp * 32 * kMaxDepth;
-        wi = stage->ids + warp * 32 * kMaxDepth;
-        slot = wh + lane * kMaxDepth;
-        id = wi + lane * kMaxDepth;
-    }
     const uint64_t kk = tile * C::kB + threadIdx.x;
     uint64_t pos = kk;
     // dense launches group warps in pairs: larger groups scatter their record rows more than the
     // shared cells save
     if constexpr (C::kCoherent) pos = coherent_order<!C::kDense, C::kDense ? 2 : C::kB / 32>(kk, A.count);
     const uint64_t ray = A.ray_begin + pos;
-    if constexpr (C::kDense && !C::kFlat) {
-#pragma unroll
-        for (int s = 0; s < kMaxDepth; ++s) slot[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (A.ids) {
-#pragma unroll
-            for (int s = 0; s < kMaxDepth; ++s) id[s] = kNoElement;
-        }
-    }
+    // sun-plane point; the direction waits in the generation queue unless the point lies outside
+    // every reach rectangle (then the ray meets no element box and its record is the point alone)
     bool want = false;
-    Segment g;
-    float qt = 0.f;
-    uint32_t qw = 0;
+    float hu = 0.f, hv = 0.f;
+    float3 o = f3(0.f, 0.f, 0.f);
     if (kk < A.count) {
+        hu = halton2(ray);
+        hv = halton3_tab(ray, sm.t6, A.h3t12);
+        o = sun_point(sm.sun, hu, hv);
         if constexpr (C::kFlat) {
-            // sun-plane point; the direction waits in the generation queue unless the point lies
-            // outside every reach rectangle (then the ray meets no element box)
-            const float hu = halton2(ray), hv = halton3_tab(ray, sm.t6, A.h3t12);
-            g.o = sun_point(sm.sun, hu, hv);
-            if constexpr (C::kDense) wh[lane] = make_float4(0.0f, g.o.x, g.o.y, g.o.z);
             const int nr = sm.flat.n;
 #pragma unroll
             for (int e = 0; e < kFlatMax; ++e) {
                 if (e >= nr) break;
-                const float4 r = sm.reach[e];
-                want |= (hu >= r.x) & (hu <= r.y) & (hv >= r.z) & (hv <= r.w);
+                want |= in_rect(sm.reach[e], hu, hv);
             }
         } else {
-            g = generate<C>(A, sm.sun, ray, sm.t6);
-            if constexpr (C::kDense) slot[0] = make_float4(0.0f, g.o.x, g.o.y, g.o.z);
-            Hit h;
-            h.best = find_closest<C>(A, sm, g.o, g.d, g.tmin, h.t, h.type);
-            if (h.best >= 0) {
-                const Prim p = load_prim(A.prims, (uint32_t)h.best);
-                float4 rec;
-                int s;
-                want = classify(p, g, h, rec, s);
-                if (s >= 0) {
-                    if constexpr (C::kDense) {
-                        slot[s] = rec;
-                        if (A.ids) id[s] = (uint32_t)h.best;
-                    }
-                    if constexpr (C::kFlux) flux_record(k, rec, s);
-                }
-                qt = h.t;
-                qw = (uint32_t)h.best | (h.type << kTypeShift);
-            }
+            want = sun_reach_any(sm.sg, hu, hv);
         }
     }
     __syncwarp();
-    if constexpr (C::kFlat) push_gen(sm, want, ray, g.o);
-    else push(sm, want, ray, g.o, g.d, qt, qw);
+    // element-list launches queue the point, the others its Halton coordinates (their batch looks
+    // up the cell again)
+    if constexpr (C::kFlat) push_gen(sm, want, ray, o);
+    else push_gen(sm, want, ray, f3(hu, hv, 0.f));
     if constexpr (C::kDense && C::kCoherent) {
-        // each lane writes its own ray's 80 B row
+        // each lane writes its own ray's 80 B row: the sun-plane record, then empty slots (the
+        // generation and bounce batches overwrite the slots they fill, after the barriers between)
         if (kk < A.count) {
             float4* gh = A.hits + pos * kMaxDepth;
+            gh[0] = make_float4(0.0f, o.x, o.y, o.z);
 #pragma unroll
-            for (int s = 0; s < kMaxDepth; ++s) gh[s] = slot[s];
+            for (int s = 1; s < kMaxDepth; ++s) gh[s] = make_float4(0.f, 0.f, 0.f, 0.f);
             if (A.ids) {
                 uint32_t* gi = A.ids + pos * kMaxDepth;
 #pragma unroll
-                for (int s = 0; s < kMaxDepth; ++s) gi[s] = id[s];
+                for (int s = 0; s < kMaxDepth; ++s) gi[s] = kNoElement;
             }
         }
-    } else if constexpr (C::kDense && C::kFlat) {
+    } else if constexpr (C::kDense) {
         // the warp's 32 x 80 B of records leave as 5 fully coalesced 512-byte rows: record e of the
         // warp is slot e mod 5 of ray e / 5, the staged sun-plane record for slot 0, else empty
+        float4* wh = stage->rec0 + warp * 32;
+        wh[lane] = make_float4(0.0f, o.x, o.y, o.z);
+        __syncwarp();
         const uint64_t warp_first = tile * C::kB + (uint64_t)warp * 32;
         if (warp_first < A.count) {
             const uint32_t n_rec = (uint32_t)min((uint64_t)32, A.count - warp_first) * kMaxDepth;
@@ -1234,33 +1279,9 @@ __device__ __forceinline__ void trace_tile(const typename C::Args& A, const Sink
                 }
             }
         }
-    } else if constexpr (C::kDense) {
-        // the warp's 32 x 80 B of records leave as 5 fully coalesced 512-byte rows (stride 80 B per
-        // lane in shared memory: the 16-byte stores of each quarter warp hit distinct banks)
-        const uint64_t warp_first = tile * C::kB + (uint64_t)warp * 32;
-        if (warp_first < A.count) {
-            const uint64_t n_rec = min((uint64_t)32, A.count - warp_first) * kMaxDepth;
-            float4* gh = A.hits + warp_first * kMaxDepth;
-#pragma unroll
-            for (int s = 0; s < kMaxDepth; ++s) {
-                const uint32_t e = (uint32_t)(s * 32 + lane);
-                if (e < n_rec) gh[e] = wh[e];
-            }
-            if (A.ids) {
-                uint32_t* gi = A.ids + warp_first * kMaxDepth;
-#pragma unroll
-                for (int s = 0; s < kMaxDepth; ++s) {
-                    const uint32_t e = (uint32_t)(s * 32 + lane);
-                    if (e < n_rec) gi[e] = wi[e];
-                }
-            }
-        }
     }
-    // the barrier before phase B counts this tile's appends (the bounce queue of BVH/grid launches,
-    // the generation queue of element-list launches)
-    const int added = __syncthreads_count(want);
-    if constexpr (C::kFlat) gs += added;
-    else qs += added;
+    // the barrier before phase B counts this tile's appends to the generation queue
+    gs += __syncthreads_count(want);
     drain<C>(A, k, sm, false, qs, gs);
 }
 
