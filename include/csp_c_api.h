@@ -322,6 +322,26 @@ CSP_API int csp_server_wait(csp_server s, uint64_t request_id, double timeout_s,
  * steps. */
 CSP_API int csp_server_stats(csp_server s, double* out);
 
+/* ---- Diagnostics and tuning (no counterpart in the reference, which stops the process on any
+ * CUDA error, lib/util_check.hpp:54-63, and has no tunable launches) ----
+ * Allocation-failure injection, for tests of the error paths: the device or pinned-host
+ * allocation of this library that follows `after` further successful ones fails as if the device
+ * were out of memory, once (the call that made it returns CSP_ERR_OUT_OF_MEMORY, or a served
+ * request fails with it); -1 cancels.  Handles stay usable after such a failure. */
+CSP_API int csp_debug_fail_allocation(int64_t after);
+/* Persistent cache of the batched mode's autotuner: a JSON file of tuned launch parameters per
+ * (device, kernel build, kernel group, ray-count class), read now (a missing file is an empty
+ * cache) and rewritten after every autotuning.  NULL or "" keeps tunings in this process only, the
+ * default unless the environment variable CSP_TUNE_CACHE names a file.  csp_tune_cache_entries: the
+ * tunings known now. */
+CSP_API int csp_set_tune_cache(const char* path);
+CSP_API int csp_tune_cache_entries(uint32_t* entries);
+/* Builds with -DCSP_BOUNDS_CHECK check the queue, record-row, flux-bin and grid indices of every
+ * launch against their buffers and skip the access that fails: `sites` receives the mask of the
+ * checks that failed on the device since the last call (0 = none) and clears it.  CSP_ERR_STATE in
+ * a build without the checks. */
+CSP_API int csp_bounds_check_status(int device, uint32_t* sites);
+
 #ifdef __cplusplus
 }
 #endif

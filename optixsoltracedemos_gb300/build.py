@@ -18,6 +18,9 @@ CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB_NAME = "libcsp_gb300.so"
 LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
+# the bounds-check build (-DCSP_BOUNDS_CHECK): every launch checks its queue, record-row, flux-bin
+# and grid indices against their buffers (csp_bounds_check_status); for tests on small cases
+CHECK_LIB_PATH = os.path.join(OUT_DIR, "libcsp_gb300_check.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = [
@@ -54,9 +57,10 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libcsp_gb300.so")
 
 
-def _compile(src: str, verbose: bool) -> str:
-    obj = os.path.join(OUT_DIR, "obj", os.path.basename(src) + ".o")
-    cmd = [nvcc(), *ARCH, *COMMON, "-c", os.path.join(CSRC, src), "-o", obj]
+def _compile(src: str, verbose: bool, check: bool = False) -> str:
+    obj = os.path.join(OUT_DIR, "obj_check" if check else "obj", os.path.basename(src) + ".o")
+    cmd = [nvcc(), *ARCH, *COMMON, *(["-DCSP_BOUNDS_CHECK"] if check else []), "-c", os.path.join(CSRC, src),
+           "-o", obj]
     if verbose and src.endswith(".cu"):
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -67,30 +71,31 @@ def _compile(src: str, verbose: bool) -> str:
     return obj
 
 
-def _stale() -> bool:
-    if not os.path.exists(LIB_PATH):
+def _stale(lib: str) -> bool:
+    if not os.path.exists(lib):
         return True
-    t = os.path.getmtime(LIB_PATH)
+    t = os.path.getmtime(lib)
     deps = []
     for d in (CSRC, os.path.join(ROOT, "include"), os.path.join(PKG, "cpp", "include"), os.path.join(PKG, "cpp", "src")):
         deps += [os.path.join(d, f) for f in os.listdir(d) if os.path.isfile(os.path.join(d, f))]
     return any(os.path.getmtime(d) > t for d in deps) or os.path.getmtime(__file__) > t
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    if not force and not _stale():
-        return LIB_PATH
-    os.makedirs(os.path.join(OUT_DIR, "obj"), exist_ok=True)
+def build(force: bool = False, verbose: bool = False, bounds_check: bool = False) -> str:
+    lib = CHECK_LIB_PATH if bounds_check else LIB_PATH
+    if not force and not _stale(lib):
+        return lib
+    os.makedirs(os.path.join(OUT_DIR, "obj_check" if bounds_check else "obj"), exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
-    tmp = LIB_PATH + ".tmp"
+        objs = list(ex.map(lambda s: _compile(s, verbose, bounds_check), SOURCES))
+    tmp = lib + ".tmp"
     cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-Xcompiler", "-fPIC"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, bounds_check="--bounds-check" in sys.argv))

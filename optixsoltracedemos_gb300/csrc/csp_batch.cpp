@@ -26,7 +26,10 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <new>
@@ -41,9 +44,102 @@ namespace {
 
 size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
-// tuned launch parameters, per (device, scene class, ray-count class)
+// Tuned launch parameters per (device model, kernel build, kernel group, ray-count class), shared
+// by every batch of the process and, when a cache file is set (csp_set_tune_cache, or the
+// CSP_TUNE_CACHE environment variable), by every process that uses that file.  The device model is
+// "name ccM.m smN"; the kernel build is a fingerprint of both block sizes' register, shared and
+// local memory use, so a rebuilt kernel is tuned afresh.
+struct TuneKey {
+    std::string device;
+    uint32_t build = 0;
+    int group = 0, cls = 0;
+    bool operator<(const TuneKey& o) const {
+        return std::tie(device, build, group, cls) < std::tie(o.device, o.build, o.group, o.cls);
+    }
+};
 std::mutex g_tune_mu;
-std::map<std::tuple<int, int, int>, BatchTuning> g_tune_cache;
+std::map<TuneKey, BatchTuning> g_tune_cache;
+std::string g_tune_path;
+bool g_tune_path_set = false;  // set by the API or taken from the environment at first use
+
+// "key": "string" or "key": integer on one line of the cache file.
+bool json_str(const char* line, const char* key, std::string& out) {
+    const char* p = std::strstr(line, key);
+    if (!p) return false;
+    p = std::strchr(p + std::strlen(key), '"');
+    if (!p) return false;
+    const char* q = std::strchr(p + 1, '"');
+    if (!q) return false;
+    out.assign(p + 1, q);
+    return true;
+}
+
+bool json_int(const char* line, const char* key, long long& out) {
+    const char* p = std::strstr(line, key);
+    if (!p) return false;
+    p = std::strchr(p + std::strlen(key), ':');
+    if (!p) return false;
+    char* end = nullptr;
+    out = std::strtoll(p + 1, &end, 10);
+    return end != p + 1;
+}
+
+// Entries of a cache file into g_tune_cache (caller holds g_tune_mu); malformed entries are skipped.
+void tune_load_locked(const std::string& path) {
+    FILE* f = std::fopen(path.c_str(), "r");
+    if (!f) return;
+    char line[1024];
+    while (std::fgets(line, sizeof line, f)) {
+        TuneKey k;
+        long long build, group, cls, block, ctas, chunk;
+        if (!json_str(line, "\"device\"", k.device) || !json_int(line, "\"build\"", build) ||
+            !json_int(line, "\"group\"", group) || !json_int(line, "\"ray_class\"", cls) ||
+            !json_int(line, "\"block\"", block) || !json_int(line, "\"ctas_per_sm\"", ctas) ||
+            !json_int(line, "\"chunk\"", chunk))
+            continue;
+        if (group < 0 || group >= kBatchGroups || (block != 128 && block != 256) || ctas < 0 || ctas > 64 ||
+            chunk < 1 || chunk > 1 << 20)
+            continue;
+        k.build = (uint32_t)build;
+        k.group = (int)group;
+        k.cls = (int)cls;
+        g_tune_cache[k] = BatchTuning{(int)block, (int)ctas, (int)chunk};
+    }
+    std::fclose(f);
+}
+
+// The whole cache to the file (caller holds g_tune_mu): written to a temporary file next to it and
+// renamed over it, so a reader never sees half a file.
+void tune_save_locked() {
+    if (g_tune_path.empty()) return;
+    const std::string tmp = g_tune_path + ".tmp." + std::to_string((unsigned long long)std::hash<std::thread::id>()(
+                                                         std::this_thread::get_id()));
+    FILE* f = std::fopen(tmp.c_str(), "w");
+    if (!f) return;  // an unwritable cache only costs the next process its tuning runs
+    std::fprintf(f, "{\"format\": \"csp_gb300 batch tuning cache\", \"version\": 1, \"entries\": [\n");
+    size_t i = 0;
+    for (const auto& kv : g_tune_cache) {
+        std::fprintf(f,
+                     "  {\"device\": \"%s\", \"build\": %u, \"group\": %d, \"ray_class\": %d, \"block\": %d, "
+                     "\"ctas_per_sm\": %d, \"chunk\": %d}%s\n",
+                     kv.first.device.c_str(), kv.first.build, kv.first.group, kv.first.cls, kv.second.block,
+                     kv.second.ctas_per_sm, kv.second.chunk, ++i < g_tune_cache.size() ? "," : "");
+    }
+    std::fprintf(f, "]}\n");
+    const bool ok = std::fclose(f) == 0;
+    if (!ok || std::rename(tmp.c_str(), g_tune_path.c_str()) != 0) std::remove(tmp.c_str());
+}
+
+// First use: the file named by CSP_TUNE_CACHE, unless the API chose one (caller holds g_tune_mu).
+void tune_init_locked() {
+    if (g_tune_path_set) return;
+    g_tune_path_set = true;
+    const char* env = std::getenv("CSP_TUNE_CACHE");
+    if (env && *env) {
+        g_tune_path = env;
+        tune_load_locked(g_tune_path);
+    }
+}
 
 int ray_class(uint64_t mean_rays) {
     int c = 0;
@@ -99,6 +195,12 @@ int Batch::ensure_stream() {
     if (stream) return CSP_OK;
     int rc = cuda_status(cudaSetDevice(device), "cudaSetDevice");
     if (rc) return rc;
+    cudaDeviceProp prop;
+    if ((rc = cuda_status(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties"))) return rc;
+    device_model = std::string(prop.name) + " cc" + std::to_string(prop.major) + "." + std::to_string(prop.minor) +
+                   " sm" + std::to_string(prop.multiProcessorCount);
+    for (char& c : device_model)
+        if (c == '"' || c == '\\') c = '_';
     h3t12 = halton3_table();
     if ((rc = cuda_status(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate"))) return rc;
     if ((rc = cuda_status(cudaEventCreate(&ev0), "cudaEventCreate"))) return rc;
@@ -123,7 +225,7 @@ int Batch::add_scene(const csp_element* el, uint32_t n, uint32_t* id) {
     if (!s.flat) build_grid(s.base, s.grid);
     auto put = [&](auto*& dptr, const auto& host, const char* what) {
         const size_t bytes = std::max<size_t>(1, host.size()) * sizeof(host[0]);
-        int r = cuda_status(cudaMalloc((void**)&dptr, bytes), what);
+        int r = cuda_status(dev_alloc((void**)&dptr, bytes), what);
         if (!r && !host.empty())
             r = cuda_status(cudaMemcpy(dptr, host.data(), host.size() * sizeof(host[0]), cudaMemcpyHostToDevice), what);
         return r;
@@ -266,7 +368,7 @@ int Batch::layout(int si) {
         size_t free_b = 0, total_b = 0;
         cudaMemGetInfo(&free_b, &total_b);
         if (total > free_b) return set_error(CSP_ERR_OUT_OF_MEMORY, "batch does not fit in free device memory");
-        if ((rc = cuda_status(cudaMalloc((void**)&d_arena, total), "cudaMalloc batch arena"))) return rc;
+        if ((rc = cuda_status(dev_alloc((void**)&d_arena, total), "cudaMalloc batch arena"))) return rc;
         arena_cap = total;
     }
     // the slot is not in flight; if it holds the current results, this run replaces them
@@ -279,7 +381,7 @@ int Batch::layout(int si) {
         if (S.h_stage) cudaFreeHost(S.h_stage);
         S.h_stage = nullptr;
         S.stage_cap = 0;
-        if ((rc = cuda_status(cudaHostAlloc((void**)&S.h_stage, up_bytes, cudaHostAllocDefault), "cudaHostAlloc staging")))
+        if ((rc = cuda_status(host_alloc((void**)&S.h_stage, up_bytes), "cudaHostAlloc staging")))
             return rc;
         S.stage_cap = up_bytes;
     }
@@ -287,8 +389,7 @@ int Batch::layout(int si) {
         if (S.h_result) cudaFreeHost(S.h_result);
         S.h_result = nullptr;
         S.result_cap = 0;
-        if ((rc = cuda_status(cudaHostAlloc((void**)&S.h_result, std::max<size_t>(res_bytes, 16), cudaHostAllocDefault),
-                              "cudaHostAlloc results")))
+        if ((rc = cuda_status(host_alloc((void**)&S.h_result, std::max<size_t>(res_bytes, 16)), "cudaHostAlloc results")))
             return rc;
         S.result_cap = res_bytes;
     }
@@ -465,6 +566,7 @@ int Batch::enqueue_scene_setup(cudaStream_t st) {
 // Time the candidate launch parameters of group g on a sample of its instances and keep the
 // fastest.  Needs the scene setup on the device (prefix + refit + sun frames) done.
 int Batch::autotune(int g, BatchTuning& best) {
+    NvtxRange nvtx("csp batch autotune");
     std::vector<BatchTuning> cands;
     for (int block : {128, 256}) {
         const int occ = batch_occupancy(g, block);
@@ -472,7 +574,7 @@ int Batch::autotune(int g, BatchTuning& best) {
         std::vector<int> ctas = {occ};
         if (occ > 1) ctas.push_back(std::max(1, occ * 2 / 3));
         for (int c : ctas)
-            for (int chunk : {1, 4, 16}) cands.push_back(BatchTuning{block, c, chunk});
+            for (int chunk : {1, 4, 16, 64}) cands.push_back(BatchTuning{block, c, chunk});
     }
     if (cands.empty()) return set_error(CSP_ERR_CUDA, "no launchable configuration of the batch kernel");
     uint64_t total = 0;
@@ -531,9 +633,14 @@ int Batch::resolve_tuning() {
             used[g] = user;
             continue;
         }
-        const auto key = std::make_tuple(device, g, ray_class(rays[g] / (uint64_t)n_group[g]));
+        TuneKey key;
+        key.device = device_model;
+        key.build = batch_kernel_build(g);
+        key.group = g;
+        key.cls = ray_class(rays[g] / (uint64_t)n_group[g]);
         {
             std::lock_guard<std::mutex> lk(g_tune_mu);
+            tune_init_locked();
             auto it = g_tune_cache.find(key);
             if (it != g_tune_cache.end()) {
                 used[g] = it->second;
@@ -550,11 +657,13 @@ int Batch::resolve_tuning() {
         used[g] = best;
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_tune_cache[key] = best;
+        tune_save_locked();
     }
     return CSP_OK;
 }
 
 int Batch::run_async() {
+    NvtxRange nvtx("csp batch build and launch");
     if (inst.empty()) return set_error(CSP_ERR_STATE, "batch has no instances");
     if (flight.size() >= 2) return set_error(CSP_ERR_STATE, "two runs in flight: wait for one first");
     const auto t0 = std::chrono::steady_clock::now();
@@ -674,6 +783,7 @@ int Batch::run_async() {
 }
 
 int Batch::wait() {
+    NvtxRange nvtx("csp batch wait");
     if (flight.empty()) return set_error(CSP_ERR_STATE, "no batch run in flight");
     const int si = flight.front();
     flight.pop_front();
@@ -720,6 +830,22 @@ using csp::Batch;
     } while (0)
 
 extern "C" {
+
+int csp_set_tune_cache(const char* path) {
+    std::lock_guard<std::mutex> lk(csp::g_tune_mu);
+    csp::g_tune_path_set = true;
+    csp::g_tune_path = path ? path : "";
+    if (!csp::g_tune_path.empty()) csp::tune_load_locked(csp::g_tune_path);
+    return CSP_OK;
+}
+
+int csp_tune_cache_entries(uint32_t* entries) {
+    if (!entries) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "null output");
+    std::lock_guard<std::mutex> lk(csp::g_tune_mu);
+    csp::tune_init_locked();
+    *entries = (uint32_t)csp::g_tune_cache.size();
+    return CSP_OK;
+}
 
 int csp_batch_create(csp_batch* out, int device) {
     if (!out) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "null output handle");

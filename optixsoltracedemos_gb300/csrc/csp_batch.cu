@@ -237,6 +237,34 @@ int batch_occupancy(int accel, int block) {
     }
 }
 
+namespace {
+
+template <int kB, int kAccel>
+uint32_t build_of() {
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, batch_kernel<kB, kAccel>) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    // FNV-1a over the numbers that change when the kernel's code generation changes
+    uint32_t h = 2166136261u;
+    for (uint64_t v : {(uint64_t)a.numRegs, (uint64_t)a.sharedSizeBytes, (uint64_t)a.localSizeBytes,
+                       (uint64_t)a.maxThreadsPerBlock, (uint64_t)a.constSizeBytes, (uint64_t)batch_smem<kB, kAccel>()})
+        for (int b = 0; b < 8; ++b) h = (h ^ (uint32_t)((v >> (8 * b)) & 0xffu)) * 16777619u;
+    return h;
+}
+
+}  // namespace
+
+uint32_t batch_kernel_build(int accel) {
+    switch (accel) {
+        case kAccelFlat: return build_of<128, kAccelFlat>() ^ (build_of<256, kAccelFlat>() * 3u);
+        case kAccelBvh: return build_of<128, kAccelBvh>() ^ (build_of<256, kAccelBvh>() * 3u);
+        case kAccelGrid: return build_of<128, kAccelGrid>() ^ (build_of<256, kAccelGrid>() * 3u);
+        default: return 0;
+    }
+}
+
 cudaError_t launch_trace_batch(const BatchLaunch& L, int accel, const BatchTuning& t, cudaStream_t stream) {
     if (L.total_tiles == 0 || L.n_inst <= 0) return cudaSuccess;
     if (t.chunk <= 0) return cudaErrorInvalidValue;
@@ -250,5 +278,7 @@ cudaError_t launch_trace_batch(const BatchLaunch& L, int accel, const BatchTunin
         default: return cudaErrorInvalidValue;
     }
 }
+
+uint32_t bounds_sites_batch() { return take_bounds_sites(); }
 
 }  // namespace csp

@@ -73,6 +73,7 @@ struct RunSlot {
 
 struct Batch {
     int device = -1;
+    std::string device_model;  // "name ccM.m smN": the autotuner cache key's device part
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // autotuner timing
     const float* h3t12 = nullptr;  // Halton table of the device

@@ -2,6 +2,7 @@
 #include "csp_c_api.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -32,6 +33,37 @@ namespace csp {
 
 int set_error(int status, const std::string& msg) { return fail(status, msg); }
 
+namespace {
+
+// Allocations left before the injected failure (csp_debug_fail_allocation); -1: none pending.
+std::atomic<long long> g_fail_after{-1};
+
+bool injected_failure() {
+    long long v = g_fail_after.load();
+    while (v >= 0) {
+        if (g_fail_after.compare_exchange_weak(v, v == 0 ? -1 : v - 1)) return v == 0;
+    }
+    return false;
+}
+
+}  // namespace
+
+cudaError_t dev_alloc(void** p, size_t bytes) {
+    if (injected_failure()) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes);
+}
+
+cudaError_t host_alloc(void** p, size_t bytes) {
+    if (injected_failure()) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaHostAlloc(p, bytes, cudaHostAllocDefault);
+}
+
 int cuda_status(cudaError_t e, const char* what) {
     if (e == cudaSuccess) return CSP_OK;
     const int st = (e == cudaErrorMemoryAllocation) ? CSP_ERR_OUT_OF_MEMORY : CSP_ERR_CUDA;
@@ -46,7 +78,7 @@ static int upload(T*& dptr, size_t& cap, const std::vector<T>& host, cudaStream_
         if (dptr) cudaFree(dptr);
         dptr = nullptr;
         cap = 0;
-        int rc = cuda_status(cudaMalloc((void**)&dptr, std::max<size_t>(n, 1) * sizeof(T)), what);
+        int rc = cuda_status(dev_alloc((void**)&dptr, std::max<size_t>(n, 1) * sizeof(T)), what);
         if (rc) return rc;
         cap = n;
     }
@@ -120,7 +152,7 @@ int System::upload_scene() {
     if ((rc = upload(d_aabbs, cap_aabbs, scene.aabbs, stream, "upload aabbs"))) return rc;
     if ((rc = upload(d_nodes, cap_nodes, scene.nodes, stream, "upload bvh"))) return rc;
     if (!d_sun) {
-        if ((rc = cuda_status(cudaMalloc((void**)&d_sun, sizeof(SunFrame)), "cudaMalloc sun"))) return rc;
+        if ((rc = cuda_status(dev_alloc((void**)&d_sun, sizeof(SunFrame)), "cudaMalloc sun"))) return rc;
     }
     return CSP_OK;
 }
@@ -134,7 +166,7 @@ int System::upload_grid(bool arrays) {
         if ((rc = upload(d_items, cap_items, grid.items, stream, "upload grid items"))) return rc;
         if ((rc = upload(d_global, cap_global, grid.global, stream, "upload grid globals"))) return rc;
     }
-    if (!d_grid && (rc = cuda_status(cudaMalloc((void**)&d_grid, sizeof(GridDesc)), "cudaMalloc grid"))) return rc;
+    if (!d_grid && (rc = cuda_status(dev_alloc((void**)&d_grid, sizeof(GridDesc)), "cudaMalloc grid"))) return rc;
     grid_host = csp::grid_desc(grid, d_cells, d_items, d_global);
     return cuda_status(cudaMemcpyAsync(d_grid, &grid_host, sizeof(GridDesc), cudaMemcpyHostToDevice, stream),
                        "upload grid");
@@ -167,10 +199,10 @@ int System::build_sungrid() {
         cudaFree(d_sgrid);
         d_sgrid = nullptr;
         cap_sgrid = 0;
-        if ((rc = cuda_status(cudaMalloc((void**)&d_sgrid, bytes), "cudaMalloc sun grid"))) return rc;
+        if ((rc = cuda_status(dev_alloc((void**)&d_sgrid, bytes), "cudaMalloc sun grid"))) return rc;
         cap_sgrid = bytes;
     }
-    if (!d_sgjob && (rc = cuda_status(cudaMalloc((void**)&d_sgjob, sizeof(SunGridJob)), "cudaMalloc sun grid job")))
+    if (!d_sgjob && (rc = cuda_status(dev_alloc((void**)&d_sgjob, sizeof(SunGridJob)), "cudaMalloc sun grid job")))
         return rc;
     sungrid_place(d_sgrid, n, sgjob_host);
     sgjob_host.sun = d_sun;
@@ -190,10 +222,10 @@ int System::ensure_hit_buffers() {
         cap_rays = 0;
         ids_allocated = false;
         const size_t n = std::max<uint64_t>(num_rays, 1);
-        int rc = cuda_status(cudaMalloc((void**)&d_hits, n * kMaxDepth * sizeof(float4)), "cudaMalloc hit buffer");
+        int rc = cuda_status(dev_alloc((void**)&d_hits, n * kMaxDepth * sizeof(float4)), "cudaMalloc hit buffer");
         if (rc) return rc;
         if (record_ids) {
-            rc = cuda_status(cudaMalloc((void**)&d_ids, n * kMaxDepth * sizeof(uint32_t)), "cudaMalloc id buffer");
+            rc = cuda_status(dev_alloc((void**)&d_ids, n * kMaxDepth * sizeof(uint32_t)), "cudaMalloc id buffer");
             if (rc) return rc;
             ids_allocated = true;
         }
@@ -203,6 +235,7 @@ int System::ensure_hit_buffers() {
 }
 
 int System::initialize() {
+    NvtxRange nvtx("csp initialize");
     const auto t0 = std::chrono::steady_clock::now();
     int rc = ensure_streams();
     if (rc) return rc;
@@ -226,6 +259,7 @@ int System::initialize() {
 }
 
 int System::update() {
+    NvtxRange nvtx("csp update");
     if (!initialized) return fail(CSP_ERR_STATE, "update() before initialize()");
     if (elements.size() != scene.prims.size())
         return fail(CSP_ERR_STATE, "update() needs the element count of initialize(); call initialize() again");
@@ -273,6 +307,7 @@ int System::trace_async(cudaStream_t st) {
 }
 
 int System::run() {
+    NvtxRange nvtx("csp run");
     if (!initialized) return fail(CSP_ERR_STATE, "run() before initialize()");
     int rc = ensure_hit_buffers();
     if (rc) return rc;
@@ -287,6 +322,7 @@ int System::run() {
 }
 
 int System::run_to_host(float* dst, uint32_t* ids_dst) {
+    NvtxRange nvtx("csp run_to_host");
     if (!initialized) return fail(CSP_ERR_STATE, "run() before initialize()");
     int rc = ensure_hit_buffers();
     if (rc) return rc;
@@ -336,6 +372,7 @@ void counts_to_flux(const uint32_t* counts, size_t n, double dni, double sun_are
 }
 
 int System::flux_map(uint32_t nx, uint32_t ny, uint32_t* counts, double dni, double* flux, bool staged) {
+    NvtxRange nvtx("csp flux_map");
     if (!initialized || !d_hits) return fail(CSP_ERR_STATE, "flux map before initialize()/run()");
     if (nx == 0 || ny == 0 || (uint64_t)nx * ny > (1u << 26)) return fail(CSP_ERR_INVALID_ARGUMENT, "bad flux grid");
     const size_t nb = (size_t)nx * ny;
@@ -344,10 +381,10 @@ int System::flux_map(uint32_t nx, uint32_t ny, uint32_t* counts, double dni, dou
         cudaFree(d_flux);
         d_flux = nullptr;
         cap_flux = 0;
-        if ((rc = cuda_status(cudaMalloc((void**)&d_flux, nb * sizeof(uint32_t)), "cudaMalloc flux map"))) return rc;
+        if ((rc = cuda_status(dev_alloc((void**)&d_flux, nb * sizeof(uint32_t)), "cudaMalloc flux map"))) return rc;
         cap_flux = nb;
     }
-    if (!d_fstats && (rc = cuda_status(cudaMalloc((void**)&d_fstats, 4 * sizeof(unsigned long long)), "cudaMalloc")))
+    if (!d_fstats && (rc = cuda_status(dev_alloc((void**)&d_fstats, 4 * sizeof(unsigned long long)), "cudaMalloc")))
         return rc;
     FluxTarget F;
     flux_target(elements.back(), nx, ny, F);
@@ -385,6 +422,26 @@ extern "C" {
 
 const char* csp_last_error(void) { return t_last_error.c_str(); }
 int csp_abi_version(void) { return CSP_ABI_VERSION; }
+
+int csp_bounds_check_status(int device, uint32_t* sites) {
+    if (!sites) return fail(CSP_ERR_INVALID_ARGUMENT, "null output");
+    *sites = 0;
+    if (!csp::kBoundsCheckBuild) return fail(CSP_ERR_STATE, "not a bounds-check build (-DCSP_BOUNDS_CHECK)");
+    int prev = -1;
+    cudaGetDevice(&prev);
+    int rc = csp::cuda_status(cudaSetDevice(device), "cudaSetDevice");
+    if (rc) return rc;
+    if ((rc = csp::cuda_status(cudaDeviceSynchronize(), "cudaDeviceSynchronize"))) return rc;
+    *sites = csp::bounds_sites_trace() | csp::bounds_sites_batch() | csp::bounds_sites_sungrid();
+    if (prev >= 0 && prev != device) cudaSetDevice(prev);
+    return CSP_OK;
+}
+
+int csp_debug_fail_allocation(int64_t after) {
+    if (after < -1) return fail(CSP_ERR_INVALID_ARGUMENT, "after must be >= -1");
+    csp::g_fail_after.store((long long)after);
+    return CSP_OK;
+}
 
 int csp_create(csp_handle* out, int device, uint64_t num_rays) {
     if (!out) return fail(CSP_ERR_INVALID_ARGUMENT, "null output handle");

@@ -141,7 +141,7 @@ const float* halton3_table() {
     if (!tried[dev]) {
         tried[dev] = true;
         float* t = nullptr;
-        if (cudaMalloc((void**)&t, kH3T12 * sizeof(float)) == cudaSuccess) {
+        if (dev_alloc((void**)&t, kH3T12 * sizeof(float)) == cudaSuccess) {
             halton3_table_kernel<<<(kH3T12 + 255) / 256, 256>>>(t);
             if (cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess) tables[dev] = t;
             else cudaFree(t);
@@ -175,5 +175,7 @@ cudaError_t launch_flux_records(const float4* hits, uint64_t n_records, const Fl
     flux_records_kernel<<<(unsigned)blocks, kFluxBlock, 0, stream>>>(hits, n_records, F);
     return cudaGetLastError();
 }
+
+uint32_t bounds_sites_trace() { return take_bounds_sites(); }
 
 }  // namespace csp

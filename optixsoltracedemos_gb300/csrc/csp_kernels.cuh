@@ -8,6 +8,22 @@
 
 namespace csp {
 
+// Bounds-check builds (-DCSP_BOUNDS_CHECK): the failed-check sites recorded on the current device by
+// the kernels of each translation unit, read and cleared (0 in other builds).
+#ifdef CSP_BOUNDS_CHECK
+constexpr bool kBoundsCheckBuild = true;
+#else
+constexpr bool kBoundsCheckBuild = false;
+#endif
+uint32_t bounds_sites_trace();
+uint32_t bounds_sites_batch();
+uint32_t bounds_sites_sungrid();
+
+// Every device and pinned-host allocation of the library goes through these (csp_c_api.cpp): the
+// allocation-failure injection of csp_debug_fail_allocation lives there.
+cudaError_t dev_alloc(void** p, size_t bytes);
+cudaError_t host_alloc(void** p, size_t bytes);
+
 // Closest-hit search of a launch: the element list in shared memory (<= 8 elements), the BVH, or
 // the field grid (GridDesc).
 enum Accel : int { kAccelFlat = 0, kAccelBvh = 1, kAccelGrid = 2 };
@@ -143,6 +159,9 @@ cudaError_t launch_prepare_sun_batch(const SunJob* jobs, int n_jobs, cudaStream_
 constexpr int kBatchGroups = 3;
 // Occupancy limit of the multi-instance kernel for (accel, block); 0 if unsupported.
 int batch_occupancy(int accel, int block);
+// Fingerprint of the multi-instance kernels of a group as built (registers, shared and local memory
+// of both block sizes): part of the autotuner cache key.
+uint32_t batch_kernel_build(int accel);
 cudaError_t launch_trace_batch(const BatchLaunch& L, int accel, const BatchTuning& t, cudaStream_t stream);
 
 }  // namespace csp

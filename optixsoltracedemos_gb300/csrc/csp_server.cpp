@@ -261,19 +261,19 @@ int Server::start(int dev, size_t budget_bytes, int max_act, uint64_t step_targe
     if ((rc = cuda_status(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo"))) return rc;
     budget = budget_bytes ? budget_bytes : std::min<size_t>(free_b / 2, (size_t)8 << 30);
     if (budget > free_b) return set_error(CSP_ERR_OUT_OF_MEMORY, "server memory budget exceeds free device memory");
-    if ((rc = cuda_status(cudaMalloc((void**)&d_arena, budget), "cudaMalloc server arena"))) return rc;
+    if ((rc = cuda_status(dev_alloc((void**)&d_arena, budget), "cudaMalloc server arena"))) return rc;
     arena.reset(budget);
     step_bytes = align256((size_t)max_active * sizeof(InstanceDesc)) * kBatchGroups +
                  align256((size_t)(max_active + 1) * sizeof(uint64_t)) * kBatchGroups;
-    if ((rc = cuda_status(cudaMalloc((void**)&d_step, step_bytes), "cudaMalloc step tables"))) return rc;
-    if ((rc = cuda_status(cudaHostAlloc((void**)&h_step, step_bytes, cudaHostAllocDefault), "cudaHostAlloc"))) return rc;
-    if ((rc = cuda_status(cudaMalloc((void**)&d_counter, kBatchGroups * sizeof(unsigned long long)), "cudaMalloc")))
+    if ((rc = cuda_status(dev_alloc((void**)&d_step, step_bytes), "cudaMalloc step tables"))) return rc;
+    if ((rc = cuda_status(host_alloc((void**)&h_step, step_bytes), "cudaHostAlloc"))) return rc;
+    if ((rc = cuda_status(dev_alloc((void**)&d_counter, kBatchGroups * sizeof(unsigned long long)), "cudaMalloc")))
         return rc;
     jobs_cap = align256((size_t)max_active * sizeof(RefitJob)) + align256((size_t)max_active * sizeof(SunJob)) +
                align256((size_t)max_active * sizeof(SunGridJob));
-    if ((rc = cuda_status(cudaMalloc((void**)&d_jobs, jobs_cap), "cudaMalloc job tables"))) return rc;
+    if ((rc = cuda_status(dev_alloc((void**)&d_jobs, jobs_cap), "cudaMalloc job tables"))) return rc;
     res_slot_bytes = align256((size_t)nx * ny * sizeof(uint32_t) + 4 * sizeof(unsigned long long) + sizeof(SunFrame));
-    if ((rc = cuda_status(cudaHostAlloc((void**)&h_res, res_slot_bytes * max_active, cudaHostAllocDefault),
+    if ((rc = cuda_status(host_alloc((void**)&h_res, res_slot_bytes * max_active),
                           "cudaHostAlloc results")))
         return rc;
     for (int k = max_active - 1; k >= 0; --k) free_res_slots.push_back(k);
@@ -292,7 +292,7 @@ int Server::add_scene(const csp_element* el, uint32_t n, uint32_t* id) {
     s->group = n <= kFlatListMax ? kAccelFlat : (s->grid.valid ? kAccelGrid : kAccelBvh);
     auto put = [&](auto*& dptr, const auto& host, const char* what) {
         const size_t bytes = std::max<size_t>(1, host.size()) * sizeof(host[0]);
-        int r = cuda_status(cudaMalloc((void**)&dptr, bytes), what);
+        int r = cuda_status(dev_alloc((void**)&dptr, bytes), what);
         if (!r && !host.empty())
             r = cuda_status(cudaMemcpy(dptr, host.data(), host.size() * sizeof(host[0]), cudaMemcpyHostToDevice), what);
         return r;
@@ -377,6 +377,7 @@ int Server::submit(const SRequest& in, uint64_t* id) {
 // Move pending requests into device memory while slots and memory last; queue their uploads,
 // refits and sun planes on the stream.  Called with the lock NOT held.
 int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
+    NvtxRange nvtx("csp server admit");
     {
         std::lock_guard<std::mutex> lk(mu);
         while (!hold && !pending.empty() && (int)(active.size() + admitted.size()) < max_active &&
@@ -453,7 +454,18 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
         if (h_adm) cudaFreeHost(h_adm);
         h_adm = nullptr;
         adm_cap = 0;
-        int rc = cuda_status(cudaHostAlloc((void**)&h_adm, stage, cudaHostAllocDefault), "cudaHostAlloc admission");
+        int rc = cuda_status(host_alloc((void**)&h_adm, stage), "cudaHostAlloc admission");
+        if (rc == CSP_ERR_OUT_OF_MEMORY) {
+            // nothing of this round is queued yet: its requests fail, the server goes on (the
+            // worker releases their blocks and slots after the step)
+            std::lock_guard<std::mutex> lk(mu);
+            for (SRequest* r : admitted) {
+                r->state = kFailed;
+                r->error = "no pinned host memory for the request's upload";
+                r->error_status = CSP_ERR_OUT_OF_MEMORY;
+            }
+            return CSP_OK;
+        }
         if (rc) return rc;
         adm_cap = stage;
     }
@@ -572,6 +584,7 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
 constexpr BatchTuning kServeTuning[kBatchGroups] = {{256, 0, 16}, {128, 0, 4}, {256, 0, 16}};
 
 int Server::step_launch(std::vector<SRequest*>& finishing, uint64_t& rays) {
+    NvtxRange nvtx("csp server step launch");
     rays = 0;
     finishing.clear();
     if (active.empty()) return CSP_OK;
@@ -687,7 +700,10 @@ void Server::run_worker() {
             cv_work.wait_for(lk, std::chrono::milliseconds(1));
         }
         // 3. wait for the step (and the admissions' setup queued behind it)
-        if (!rc) rc = cuda_status(cudaStreamSynchronize(stream), "server step");
+        if (!rc) {
+            NvtxRange nvtx("csp server step wait");
+            rc = cuda_status(cudaStreamSynchronize(stream), "server step");
+        }
         const Clock::time_point now = Clock::now();
         std::lock_guard<std::mutex> lk(mu);
         if (rc) {

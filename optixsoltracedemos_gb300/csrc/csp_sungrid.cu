@@ -152,11 +152,13 @@ __global__ void __launch_bounds__(kElemBlock) sungrid_count_kernel(const SunGrid
     int iu0, iu1, iv0, iv1;
     if (!sg_range(J.rect[e], (float)nu, (float)nv, nu, nv, iu0, iu1, iv0, iv1)) return;
     if ((long long)(iu1 - iu0 + 1) * (iv1 - iv0 + 1) > kSunGridMaxCells) {
-        J.global_id[atomicAdd(&J.desc->n_global, 1)] = (uint32_t)e;
+        const int k = atomicAdd(&J.desc->n_global, 1);
+        if (CSP_BOUNDS(6, k < J.n)) J.global_id[k] = (uint32_t)e;
         return;
     }
     for (int iv = iv0; iv <= iv1; ++iv)
-        for (int iu = iu0; iu <= iu1; ++iu) atomicAdd(J.cell_start + iv * nu + iu, 1u);
+        for (int iu = iu0; iu <= iu1; ++iu)
+            if (CSP_BOUNDS(6, iv * nu + iu < J.cap_cells)) atomicAdd(J.cell_start + iv * nu + iu, 1u);
 }
 
 __global__ void __launch_bounds__(kScanBlock) sungrid_scan_kernel(const SunGridJob* __restrict__ jobs) {
@@ -197,13 +199,17 @@ __global__ void __launch_bounds__(kElemBlock) sungrid_fill_kernel(const SunGridJ
     if ((long long)(iu1 - iu0 + 1) * (iv1 - iv0 + 1) > kSunGridMaxCells) return;
     for (int iv = iv0; iv <= iv1; ++iv)
         for (int iu = iu0; iu <= iu1; ++iu) {
+            if (!CSP_BOUNDS(6, iv * nu + iu < J.cap_cells)) continue;
             const uint32_t k = atomicAdd(J.cursor + iv * nu + iu, 1u);
+            if (!CSP_BOUNDS(6, k < J.cap_items)) continue;
             J.item_rect[k] = r;
             J.item_id[k] = (uint32_t)e;
         }
 }
 
 }  // namespace
+
+uint32_t bounds_sites_sungrid() { return take_bounds_sites(); }
 
 SunGridCaps sungrid_caps(uint32_t n) {
     SunGridCaps c;

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "csp_c_api.h"
 #include "csp_kernels.cuh"
@@ -14,6 +15,16 @@
 namespace csp {
 
 int set_error(int status, const std::string& msg);
+
+// A named range on the NVTX timeline (Nsight Systems, Nsight Compute's range filters) for the
+// lifetime of the object: the host stages of the library (setup, update, trace, copies, batch runs,
+// server steps).  Without a tool attached the calls do nothing.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 int cuda_status(cudaError_t e, const char* what);
 
 // Sun shapes the ABI accepts: pillbox or Gaussian, with or without CSP_SUN_ACCURATE.

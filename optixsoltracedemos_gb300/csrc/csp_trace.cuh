@@ -41,6 +41,34 @@
 namespace csp {
 namespace {
 
+// Index checks of the bounds-check build (-DCSP_BOUNDS_CHECK): CSP_BOUNDS(site, cond) is cond, and a
+// false cond sets bit `site` of this translation unit's device word (the caller skips the access);
+// read and cleared by the host through csp_bounds_check_status.  Sites: 0 bounce-queue append,
+// 1 generation-queue append, 2 record row, 3 flux bin, 4 field-grid cell, 5 sun-grid cell and item
+// range, 6 sun-grid build, 7 Halton table.  In other builds CSP_BOUNDS(site, cond) is true and cond is
+// not evaluated.
+#ifdef CSP_BOUNDS_CHECK
+__device__ unsigned int g_bounds_sites;
+__device__ __forceinline__ bool bounds_ok(int site, bool ok) {
+    if (!ok) atomicOr(&g_bounds_sites, 1u << site);
+    return ok;
+}
+#define CSP_BOUNDS(site, cond) bounds_ok((site), (cond))
+// Host: the sites this translation unit's kernels recorded on the current device, cleared.
+inline uint32_t take_bounds_sites() {
+    unsigned int v = 0, z = 0;
+    if (cudaMemcpyFromSymbol(&v, g_bounds_sites, sizeof v) != cudaSuccess ||
+        cudaMemcpyToSymbol(g_bounds_sites, &z, sizeof z) != cudaSuccess) {
+        cudaGetLastError();
+        return 0x80000000u;  // unreadable: reported as a failed check
+    }
+    return v;
+}
+#else
+#define CSP_BOUNDS(site, cond) true
+inline uint32_t take_bounds_sites() { return 0; }
+#endif
+
 constexpr float kTwoPi = 2.0f * 3.14159265358979323846f;  // 2.0f * M_PIf, cuda/sun.cu:85
 constexpr float kTwoPiF = 0x1.921fb6p+2f;                  // fl32(2 pi), flux angle wrap
 constexpr int kFlatMax = 8;
@@ -284,6 +312,7 @@ __device__ __forceinline__ float halton3_tab(uint64_t i, const float* __restrict
     int k;
     if (t12) {
         const uint32_t q = j / kH3T12;
+        if (!CSP_BOUNDS(7, j - kH3T12 * q < kH3T12)) return 0.0f;
         r = __ldg(t12 + (j - kH3T12 * q));
         k = kH3T12Digits;
         j = q;
@@ -576,6 +605,7 @@ __device__ __forceinline__ int traverse_grid(const GridDesc& G, const Prim* __re
         }
         if (!next || ctc > tb || ctc > prune || step > G.nx + G.ny) break;
         const int c = iy * G.nx + ix;
+        if (!CSP_BOUNDS(4, c >= 0 && c < G.nx * G.ny)) break;
         list = G.items;
         j = __ldg(G.cell_start + c);
         e = __ldg(G.cell_start + c + 1);
@@ -611,8 +641,10 @@ __device__ __forceinline__ bool in_rect(float4 r, float u, float v) {
 // meet an element box (otherwise its record is the sun-plane point alone).
 __device__ __forceinline__ bool sun_reach_any(const SunGrid& G, float u, float v) {
     const int c = sg_cell(v, G.fnv, G.nv) * G.nu + sg_cell(u, G.fnu, G.nu);
+    if (!CSP_BOUNDS(5, c >= 0 && c < G.nu * G.nv)) return true;
     uint32_t j = __ldg(G.cell_start + c);
     const uint32_t e = __ldg(G.cell_start + c + 1);
+    if (!CSP_BOUNDS(5, j <= e && e <= __ldg(G.cell_start + G.nu * G.nv))) return true;
     for (; j < e; ++j)
         if (in_rect(__ldg(G.item_rect + j), u, v)) return true;
     for (int k = 0; k < G.n_global; ++k)
@@ -631,8 +663,10 @@ __device__ __forceinline__ int sun_closest(const SunGrid& G, const Prim* __restr
     best_t = __int_as_float(0x7f800000);
     float prune = kTmax;
     const int c = sg_cell(v, G.fnv, G.nv) * G.nu + sg_cell(u, G.fnu, G.nu);
+    if (!CSP_BOUNDS(5, c >= 0 && c < G.nu * G.nv)) return best;
     uint32_t j = __ldg(G.cell_start + c);
     const uint32_t e = __ldg(G.cell_start + c + 1);
+    if (!CSP_BOUNDS(5, j <= e && e <= __ldg(G.cell_start + G.nu * G.nv))) return best;
     for (; j < e; ++j) {
         if (!in_rect(__ldg(G.item_rect + j), u, v)) continue;
         const float4* q = reinterpret_cast<const float4*>(G.aabbs + __ldg(G.item_id + j));
@@ -945,7 +979,7 @@ __device__ __noinline__ void flux_record(const Sink& k, float4 rec, int slot) {
     if (slot == 1 && k.F->staged) return;  // direct sun on the receiver: not a staged result
     warp_count(k.stat + 2);
     const int b = flux_bin(*k.F, make_float3(rec.y, rec.z, rec.w));
-    if (b >= 0) {
+    if (b >= 0 && CSP_BOUNDS(3, b < k.F->nx * k.F->ny)) {
         atomicAdd(k.F->counts + b, 1u);
         warp_count(k.stat + 3);
     }
@@ -953,6 +987,7 @@ __device__ __noinline__ void flux_record(const Sink& k, float4 rec, int slot) {
 
 __device__ __forceinline__ void store_record(const TraceArgs& A, uint64_t ray, int slot, float4 rec, uint32_t id) {
     const uint64_t row = (ray - A.ray_begin) * kMaxDepth + (uint64_t)slot;
+    if (!CSP_BOUNDS(2, ray >= A.ray_begin && row < A.count * kMaxDepth)) return;
     A.hits[row] = rec;
     if (A.ids) A.ids[row] = id;
 }
@@ -974,7 +1009,7 @@ __device__ __forceinline__ void push_gen(Core& sm, bool want, uint64_t ray, floa
     int base = 0;
     if (lane == __ffs(mask) - 1) base = atomicAdd(&sm.gsize, __popc(mask));
     base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
-    if (want) {
+    if (want && CSP_BOUNDS(1, base + __popc(mask & ((1u << lane) - 1u)) < (int)(sizeof(sm.gray) / sizeof(sm.gray[0])))) {
         const int k = base + __popc(mask & ((1u << lane) - 1u));
         sm.go[0][k] = o.x;
         sm.go[1][k] = o.y;
@@ -993,7 +1028,7 @@ __device__ __forceinline__ void push(Core& sm, bool want, uint64_t ray, float3 o
     int base = 0;
     if (lane == __ffs(mask) - 1) base = atomicAdd(&sm.qsize, __popc(mask));
     base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
-    if (want) {
+    if (want && CSP_BOUNDS(0, base + __popc(mask & ((1u << lane) - 1u)) < (int)(sizeof(sm.qray) / sizeof(sm.qray[0])))) {
         const int k = base + __popc(mask & ((1u << lane) - 1u));
         sm.qo[0][k] = o.x;
         sm.qo[1][k] = o.y;
@@ -1243,7 +1278,7 @@ __device__ __forceinline__ void trace_tile(const typename C::Args& A, const Sink
     if constexpr (C::kDense && C::kCoherent) {
         // each lane writes its own ray's 80 B row: the sun-plane record, then empty slots (the
         // generation and bounce batches overwrite the slots they fill, after the barriers between)
-        if (kk < A.count) {
+        if (kk < A.count && CSP_BOUNDS(2, pos < A.count)) {
             float4* gh = A.hits + pos * kMaxDepth;
             gh[0] = make_float4(0.0f, o.x, o.y, o.z);
 #pragma unroll

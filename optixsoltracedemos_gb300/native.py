@@ -103,6 +103,10 @@ SIGNATURES = {
     "csp_server_wait": (ctypes.c_int, [_H, ctypes.c_uint64, ctypes.c_double, _P, _P, _P]),
     "csp_server_hold": (ctypes.c_int, [_H, ctypes.c_int]),
     "csp_server_stats": (ctypes.c_int, [_H, _P]),
+    "csp_debug_fail_allocation": (ctypes.c_int, [ctypes.c_int64]),
+    "csp_set_tune_cache": (ctypes.c_int, [ctypes.c_char_p]),
+    "csp_tune_cache_entries": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint32)]),
+    "csp_bounds_check_status": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_uint32)]),
 }
 STINPUT_APPLY_OPTICS = 1
 OUT_STAGED = 1  # staged results: rays straight from the sun to the receiver left out
@@ -120,12 +124,13 @@ class CspError(RuntimeError):
 
 
 def load(path: str | None = None) -> ctypes.CDLL:
-    """Load the native library (no fallback)."""
+    """Load the native library (no fallback): `path`, else the file CSP_NATIVE_LIB names (the
+    bounds-check build, for instance), else the in-tree build."""
     global _lib
     with _lock:
         if _lib is not None:
             return _lib
-        p = path or LIB_PATH
+        p = path or os.environ.get("CSP_NATIVE_LIB") or LIB_PATH
         if not os.path.exists(p):
             raise RuntimeError(f"native library {p} is missing: run optixsoltracedemos_gb300.build.build()")
         lib = ctypes.CDLL(p)
@@ -474,6 +479,34 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def debug_fail_allocation(after: int) -> None:
+    """Make the library's allocation after `after` further successful ones fail (out of memory),
+    once; -1 cancels."""
+    _check(load().csp_debug_fail_allocation(int(after)))
+
+
+def set_tune_cache(path: str | None) -> int:
+    """Use `path` as the batched autotuner's persistent cache (None: this process only); returns the
+    tunings known after reading it."""
+    lib = load()
+    _check(lib.csp_set_tune_cache(path.encode() if path else None))
+    return tune_cache_entries()
+
+
+def tune_cache_entries() -> int:
+    n = ctypes.c_uint32()
+    _check(load().csp_tune_cache_entries(ctypes.byref(n)))
+    return n.value
+
+
+def bounds_check_status(device: int = 0) -> int:
+    """Bit mask of the index checks that failed on the device since the last call (bounds-check
+    builds only; CspError otherwise)."""
+    v = ctypes.c_uint32()
+    _check(load().csp_bounds_check_status(int(device), ctypes.byref(v)))
+    return v.value
 
 
 def flux_target(receiver: np.ndarray, nx: int = 100, ny: int = 100) -> np.ndarray:
