@@ -339,7 +339,36 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def measure_plain(args, sc, local, world, pg, steps, warmup, e2e_steps, accuracy, cpu_seconds):
+def measure_write_output(sc, local, n):
+    """The reference's write_output end to end (lib/soltrace_system.cpp:208-264): trace, records to
+    the host, the CSV file written; dense records (csp_run_to_host + csp_write_hits_csv) against
+    compact ones (csp_run_to_host_compact + csp_write_compact_csv), the file the same."""
+    import numpy as np
+    from optixsoltracedemos_gb300 import native
+    tr = native.tracer_for(sc, device=local, record_ids=False, num_rays=n)
+    out = {"rays": n, "unit": "rays/s"}
+    with tempfile.TemporaryDirectory() as d:
+        dense = np.empty((n, 5, 4), np.float32)
+        pts, cnt, rec = np.empty((n, 3), np.float32), np.empty(n, np.uint8), np.empty((4 * n, 4), np.float32)
+        best_d = best_c = 1e30
+        for _ in range(2):
+            t0 = time.perf_counter()
+            tr.run_to_host(dense.reshape(-1))
+            native.write_hits_csv(dense, os.path.join(d, "dense.csv"))
+            best_d = min(best_d, time.perf_counter() - t0)
+            t0 = time.perf_counter()
+            p, c, r = tr.run_to_host_compact(pts, cnt, rec)
+            native.write_compact_csv(p, c, r, os.path.join(d, "compact.csv"))
+            best_c = min(best_c, time.perf_counter() - t0)
+        size = os.path.getsize(os.path.join(d, "dense.csv"))
+        same = open(os.path.join(d, "dense.csv"), "rb").read() == open(os.path.join(d, "compact.csv"), "rb").read()
+    tr.close()
+    out.update({"dense_rays_per_s": n / best_d, "compact_rays_per_s": n / best_c, "csv_bytes": size,
+                "csv_identical": same, "host_threads": os.cpu_count()})
+    return out
+
+
+def measure_plain(args, sc, local, world, pg, steps, warmup, e2e_steps, accuracy, cpu_seconds, write_output_rays=0):
     """Plain trace of one scene: K launches with the scene resident (CUDA events on the launching
     stream), the end-to-end rate through the C ABI with host buffers, the HBM roofline of the dense
     record stream, and the flux-map L2 against the FP64 oracle."""
@@ -408,6 +437,27 @@ def measure_plain(args, sc, local, world, pg, steps, warmup, e2e_steps, accuracy
         e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, pg, f"cuda:{local}")
         line["e2e"] = {"value": world * N / e2e_s, "unit": "rays/s", "h2d_bytes_per_step": int(elements.nbytes + 3 * 8),
                        "d2h_bytes_per_step": int(N * BYTES_PER_RAY)}
+        # the same end to end with the compact record transfer (csp_run_to_host_compact): per ray its
+        # sun-plane point and record count, then only the records that exist
+        pts = torch.empty(N * 3, dtype=torch.float32, pin_memory=True)
+        cnt = torch.empty(N, dtype=torch.uint8, pin_memory=True)
+        cap = 4 * N
+        rec = torch.empty(cap * 4, dtype=torch.float32, pin_memory=True)
+        nrec = tr.run_to_host_compact_ptr(pts.data_ptr(), cnt.data_ptr(), rec.data_ptr(), cap)
+        if pg:
+            pg.barrier()
+        t0 = time.perf_counter()
+        for k in range(e2e_steps):
+            tr.set_seed(5000 + k, rank)
+            tr.set_elements(elements)
+            tr.update()
+            nrec = tr.run_to_host_compact_ptr(pts.data_ptr(), cnt.data_ptr(), rec.data_ptr(), cap)
+        ec_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, pg, f"cuda:{local}")
+        line["e2e_compact"] = {"value": world * N / ec_s, "unit": "rays/s",
+                               "h2d_bytes_per_step": int(elements.nbytes + 3 * 8),
+                               "d2h_bytes_per_step": int(13 * N + 16 * nrec),
+                               "path": "csp_run_to_host_compact: sun-plane points, record counts, existing records"}
+        del pts, cnt, rec
     if rank == 0 and world == 1 and accuracy and host is not None:
         try:
             from oracle import oracle
@@ -422,6 +472,8 @@ def measure_plain(args, sc, local, world, pg, steps, warmup, e2e_steps, accuracy
             del oh
         except Exception as exc:  # accuracy is reported, not required for the timing line
             line["flux_l2_vs_fp64"] = f"unavailable: {exc}"
+    if rank == 0 and world == 1 and write_output_rays > 0:
+        line["write_output"] = measure_write_output(sc, local, min(N, write_output_rays))
     if rank == 0 and world == 1 and cpu_seconds > 0:
         sample = min(1 << 20, N) if len(sc.elements) < 64 else 1 << 12
         line["cpu_baseline"] = cpu_baseline(cpu_seconds, [(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, N)],
@@ -666,7 +718,8 @@ def measure_served(args, local, world):
 
 
 def _plain_summary(line):
-    keep = ("value", "ms_per_step", "roofline", "e2e", "flux_l2_vs_fp64", "cpu_baseline", "clocks")
+    keep = ("value", "ms_per_step", "roofline", "e2e", "e2e_compact", "write_output", "flux_l2_vs_fp64", "cpu_baseline",
+            "clocks")
     out = {"workload": line["config"]["workload"], "rays": line["config"]["rays"], "unit": "rays/s"}
     out.update({k: line[k] for k in keep if k in line})
     out["rays_per_s"] = out.pop("value")
@@ -714,7 +767,7 @@ def run_ours(args):
             sc = make_scene("single_parabolic", None)
             line["single_parabolic"] = _plain_summary(measure_plain(
                 sub, sc, local, world, pg, steps=200, warmup=10, e2e_steps=5, accuracy=not args.no_accuracy,
-                cpu_seconds=0.0 if args.no_cpu_baseline else 3.0))
+                cpu_seconds=0.0 if args.no_cpu_baseline else 3.0, write_output_rays=1 << 22))
             sc = make_scene("large_field", None)
             line["large_field"] = _plain_summary(measure_plain(
                 sub, sc, local, world, pg, steps=5, warmup=3, e2e_steps=0, accuracy=False, cpu_seconds=0.0))
@@ -726,7 +779,8 @@ def run_ours(args):
         e2e_steps = args.e2e_steps if sc.num_rays <= (1 << 26) else 0
         line = measure_plain(args, sc, local, world, pg, args.steps, args.warmup, e2e_steps,
                              not args.no_accuracy and sc.num_rays <= (1 << 24),
-                             0.0 if args.no_cpu_baseline else args.cpu_seconds)
+                             0.0 if args.no_cpu_baseline else args.cpu_seconds,
+                             write_output_rays=(1 << 22) if e2e_steps > 0 else 0)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if pg:

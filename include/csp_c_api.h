@@ -161,6 +161,18 @@ CSP_API int csp_run_to_host(csp_handle h, float* dst, uint32_t* ids);
  * the device can address (the kernel then stores the records across the host link directly).
  * ids may be NULL.  No host synchronisation; the handle's own hit buffer is not touched. */
 CSP_API int csp_trace_into(csp_handle h, void* hits, void* ids, uint64_t first_ray, uint64_t count, void* stream);
+/* Trace all rays, then move the records in compact form for consumers of the reference's
+ * write_output (lib/soltrace_system.cpp:208-264), which need every record but not the empty slots:
+ * points[3 num_rays] = each ray's sun-plane point (its stage-0 record), counts[num_rays] = the
+ * number of its further records (0..4), records[4 capacity] = those records {stage, x, y, z} in ray
+ * order -- instead of 80 bytes per ray.  *n_records = their number; when it exceeds `capacity`
+ * (4 num_rays always suffices) nothing is copied and CSP_ERR_INVALID_ARGUMENT is returned.
+ * csp_write_compact_csv writes the same CSV from them as csp_write_hits_csv from the dense
+ * records. */
+CSP_API int csp_run_to_host_compact(csp_handle h, float* points, uint8_t* counts, float* records, uint64_t capacity,
+                                    uint64_t* n_records);
+CSP_API int csp_write_compact_csv(const float* points, const uint8_t* counts, const float* records, uint64_t num_rays,
+                                  const char* path, int flags);
 /* One trace that allocates no memory (no counterpart in the reference).  For callers that cannot
  * call cudaMalloc -- a framework whose allocator already holds the device memory, a real-time
  * tracking loop that cannot take cudaMalloc's device-wide synchronisation: the caller passes the

@@ -110,6 +110,15 @@ void System::release() {
     d_sgrid = nullptr;
     d_sgjob = nullptr;
     cap_sgrid = 0;
+    cudaFree(d_cpoints);
+    cudaFree(d_ccounts);
+    cudaFree(d_csums);
+    cudaFree(d_crecords);
+    d_cpoints = nullptr;
+    d_ccounts = nullptr;
+    d_csums = nullptr;
+    d_crecords = nullptr;
+    cap_compact_rays = cap_crecords = 0;
     cudaFree(d_flux);
     cudaFree(d_fstats);
     d_flux = nullptr;
@@ -354,6 +363,68 @@ int System::run_to_host(float* dst, uint32_t* ids_dst) {
     if (rc) return rc;
     if (sync_rc) return sync_rc;
     if (sync_rc2) return sync_rc2;
+    time_trace = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return CSP_OK;
+}
+
+// Trace, then move the records in compact form: per ray its sun-plane point and the number of its
+// further records, and those records in ray order (kernels in csp_kernels.cu).  Nothing is copied
+// when the records exceed `capacity`; *n_records then tells how many there are.
+int System::run_to_host_compact(float* points, uint8_t* counts, float* records, uint64_t capacity,
+                                uint64_t* n_records) {
+    NvtxRange nvtx("csp run_to_host_compact");
+    if (!initialized) return fail(CSP_ERR_STATE, "run() before initialize()");
+    int rc = ensure_hit_buffers();
+    if (rc) return rc;
+    const uint64_t n = num_rays;
+    if (n > cap_compact_rays) {
+        cudaFree(d_cpoints);
+        cudaFree(d_ccounts);
+        cudaFree(d_csums);
+        d_cpoints = nullptr;
+        d_ccounts = nullptr;
+        d_csums = nullptr;
+        cap_compact_rays = 0;
+        if ((rc = cuda_status(dev_alloc((void**)&d_cpoints, std::max<uint64_t>(n, 1) * 3 * sizeof(float)), "cudaMalloc")))
+            return rc;
+        if ((rc = cuda_status(dev_alloc((void**)&d_ccounts, std::max<uint64_t>(n, 1)), "cudaMalloc"))) return rc;
+        if ((rc = cuda_status(dev_alloc((void**)&d_csums, (compact_blocks(n) + 1) * sizeof(unsigned long long)),
+                              "cudaMalloc")))
+            return rc;
+        cap_compact_rays = n;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    if ((rc = cuda_status(launch_trace(args(0, n), (int)scene.prims.size(), stream), "trace_kernel"))) return rc;
+    if ((rc = cuda_status(launch_compact_count(d_hits, n, d_ccounts, d_csums, stream), "compact_count_kernel")))
+        return rc;
+    unsigned long long total = 0;
+    if ((rc = cuda_status(cudaMemcpyAsync(&total, d_csums + compact_blocks(n), sizeof total, cudaMemcpyDeviceToHost,
+                                          stream),
+                          "D2H record count")))
+        return rc;
+    if ((rc = cuda_status(cudaStreamSynchronize(stream), "compact count"))) return rc;
+    if (n_records) *n_records = total;
+    if (total > capacity) return fail(CSP_ERR_INVALID_ARGUMENT, "the run's records exceed the capacity");
+    if (total > cap_crecords) {
+        cudaFree(d_crecords);
+        d_crecords = nullptr;
+        cap_crecords = 0;
+        if ((rc = cuda_status(dev_alloc((void**)&d_crecords, total * sizeof(float4)), "cudaMalloc compact records")))
+            return rc;
+        cap_crecords = total;
+    }
+    if ((rc = cuda_status(launch_compact_write(d_hits, n, d_csums, d_cpoints, d_crecords, stream), "compact_write_kernel")))
+        return rc;
+    if (n && (rc = cuda_status(cudaMemcpyAsync(points, d_cpoints, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, stream),
+                               "D2H points")))
+        return rc;
+    if (n && (rc = cuda_status(cudaMemcpyAsync(counts, d_ccounts, n, cudaMemcpyDeviceToHost, stream), "D2H counts")))
+        return rc;
+    if (total && (rc = cuda_status(cudaMemcpyAsync(records, d_crecords, total * sizeof(float4), cudaMemcpyDeviceToHost,
+                                                   stream),
+                                   "D2H records")))
+        return rc;
+    if ((rc = cuda_status(cudaStreamSynchronize(stream), "compact copy"))) return rc;
     time_trace = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return CSP_OK;
 }
@@ -611,6 +682,15 @@ int csp_trace_into(csp_handle h, void* hits, void* ids, uint64_t first, uint64_t
     a.count = count;
     cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : s->stream;
     return csp::cuda_status(csp::launch_trace(a, (int)s->scene.prims.size(), st), "trace_kernel");
+}
+
+int csp_run_to_host_compact(csp_handle h, float* points, uint8_t* counts, float* records, uint64_t capacity,
+                            uint64_t* n_records) {
+    CSP_GUARD(h);
+    System* s = reinterpret_cast<System*>(h);
+    if (s->num_rays && (!points || !counts)) return fail(CSP_ERR_INVALID_ARGUMENT, "null output");
+    if (capacity && !records) return fail(CSP_ERR_INVALID_ARGUMENT, "null records with a capacity");
+    return s->run_to_host_compact(points, counts, records, capacity, n_records);
 }
 
 int csp_run_to_host(csp_handle h, float* dst, uint32_t* ids) {

@@ -347,9 +347,92 @@ int write_hits_csv(const float* hits, uint64_t n, const char* path, bool staged,
     return CSP_OK;
 }
 
+// The CSV of compact records (csp_run_to_host_compact): blocks of rays are expanded back into their
+// dense rows (sun-plane record, the ray's records, empty slots) and written by the dense writer's
+// state machine and formatter, so the file is the one write_hits_csv makes from the dense buffer.
+int write_compact_csv(const float* points, const uint8_t* counts, const float* records, uint64_t n, const char* path,
+                      bool staged, std::string& err) {
+    for (uint64_t r = 0; r < n; ++r)
+        if (counts[r] >= kMaxDepth) {
+            err = "ray " + std::to_string(r) + " has more than " + std::to_string(kMaxDepth - 1) + " records";
+            return CSP_ERR_INVALID_ARGUMENT;
+        }
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) {
+        err = std::string("could not open ") + path + " for writing";
+        return CSP_ERR_IO;
+    }
+    const char* header = "number,stage,loc_x,loc_y,loc_z\n";
+    std::fwrite(header, 1, std::strlen(header), fp);
+    const unsigned nt = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    const uint64_t block = 1u << 16;
+    WriterState st;
+    uint64_t rec = 0;  // first record of the next block
+    std::vector<std::string> bufs(nt);
+    std::vector<std::vector<float>> dense(nt);
+    for (uint64_t base = 0; base < n; base += block * nt) {
+        std::vector<uint64_t> bb(nt), ee(nt), r0(nt);
+        for (unsigned t = 0; t < nt; ++t) {
+            bb[t] = std::min(n, base + t * block);
+            ee[t] = std::min(n, bb[t] + block);
+            r0[t] = rec;
+            for (uint64_t r = bb[t]; r < ee[t]; ++r) rec += counts[r];
+        }
+        auto expand = [&](unsigned t) {
+            std::vector<float>& d = dense[t];
+            d.assign((ee[t] - bb[t]) * kMaxDepth * 4, 0.0f);
+            uint64_t k = r0[t];
+            for (uint64_t r = bb[t]; r < ee[t]; ++r) {
+                float* row = d.data() + (r - bb[t]) * kMaxDepth * 4;
+                row[1] = points[3 * r];
+                row[2] = points[3 * r + 1];
+                row[3] = points[3 * r + 2];
+                for (uint32_t c = 0; c < counts[r]; ++c, ++k) std::memcpy(row + 4 * (1 + c), records + 4 * k, 16);
+            }
+        };
+        std::vector<std::thread> th;
+        for (unsigned t = 0; t < nt; ++t)
+            if (bb[t] < ee[t]) th.emplace_back(expand, t);
+        for (auto& x : th) x.join();
+        th.clear();
+        std::vector<WriterState> starts(nt);
+        for (unsigned t = 0; t < nt; ++t) {
+            starts[t] = st;
+            if (bb[t] < ee[t]) advance(dense[t].data(), 0, ee[t] - bb[t], st);
+        }
+        for (unsigned t = 0; t < nt; ++t)
+            if (bb[t] < ee[t])
+                th.emplace_back(format, dense[t].data(), 0, ee[t] - bb[t], starts[t], staged, std::ref(bufs[t]));
+        for (auto& x : th) x.join();
+        for (unsigned t = 0; t < nt; ++t)
+            if (bb[t] < ee[t] && std::fwrite(bufs[t].data(), 1, bufs[t].size(), fp) != bufs[t].size()) {
+                std::fclose(fp);
+                err = std::string("short write to ") + path;
+                return CSP_ERR_IO;
+            }
+    }
+    if (std::fclose(fp) != 0) {
+        err = std::string("could not close ") + path;
+        return CSP_ERR_IO;
+    }
+    return CSP_OK;
+}
+
 }  // namespace csp
 
 extern "C" {
+
+int csp_write_compact_csv(const float* points, const uint8_t* counts, const float* records, uint64_t num_rays,
+                          const char* path, int flags) {
+    if (!path || (num_rays && (!points || !counts))) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "null argument");
+    if (flags & ~CSP_OUT_STAGED) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "unknown output flags");
+    uint64_t total = 0;
+    for (uint64_t r = 0; r < num_rays; ++r) total += counts[r];
+    if (total && !records) return csp::set_error(CSP_ERR_INVALID_ARGUMENT, "null records");
+    std::string err;
+    const int rc = csp::write_compact_csv(points, counts, records, num_rays, path, (flags & CSP_OUT_STAGED) != 0, err);
+    return rc ? csp::set_error(rc, err) : CSP_OK;
+}
 
 int csp_parse_stinput(const char* path, csp_element* out, uint32_t capacity, uint32_t* count, double* sun_dir,
                       double* sun_angle, int flags) {

@@ -120,6 +120,96 @@ __global__ void __launch_bounds__(kFluxBlock) flux_records_kernel(const float4* 
     if (threadIdx.x < 4 && threadIdx.x > 0 && stat[threadIdx.x]) atomicAdd(F.stats + threadIdx.x, stat[threadIdx.x]);
 }
 
+// Compact records (csp_run_to_host_compact): a row of the dense buffer is the sun-plane record in
+// slot 0, then the ray's further records in slots 1.. (stage 1 or 2, so x != 0), then empty slots.
+constexpr int kCompactBlock = 256;
+
+__device__ __forceinline__ uint32_t row_records(const float4* __restrict__ hits, uint64_t r) {
+    uint32_t c = 0;
+#pragma unroll
+    for (int s = 1; s < kMaxDepth; ++s) c += __ldg(&hits[r * kMaxDepth + s].x) != 0.0f ? 1u : 0u;
+    return c;
+}
+
+// Block-wide exclusive prefix of v (kCompactBlock threads); `total` receives the block's sum.
+__device__ uint32_t block_exclusive(uint32_t v, uint32_t* scratch, uint32_t& total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) scratch[warp] = x;
+    __syncthreads();
+    uint32_t before = 0;
+    total = 0;
+    for (int w = 0; w < kCompactBlock / 32; ++w) {
+        if (w < warp) before += scratch[w];
+        total += scratch[w];
+    }
+    return before + x - v;
+}
+
+// Records beyond slot 0 of every ray, and their sum per block.
+__global__ void __launch_bounds__(kCompactBlock) compact_count_kernel(const float4* __restrict__ hits, uint64_t n,
+                                                                      uint8_t* __restrict__ counts,
+                                                                      unsigned long long* __restrict__ block_sums) {
+    __shared__ uint32_t scratch[kCompactBlock / 32];
+    const uint64_t r = (uint64_t)blockIdx.x * kCompactBlock + threadIdx.x;
+    uint32_t c = 0;
+    if (r < n) {
+        c = row_records(hits, r);
+        counts[r] = (uint8_t)c;
+    }
+    uint32_t total;
+    block_exclusive(c, scratch, total);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+// In place: block sums -> exclusive block offsets, the grand total after the last block.
+__global__ void __launch_bounds__(1024) compact_scan_kernel(unsigned long long* __restrict__ sums, uint64_t nb) {
+    __shared__ unsigned long long part[1024];
+    const uint64_t chunk = (nb + 1023) / 1024;
+    const uint64_t c0 = min(nb, (uint64_t)threadIdx.x * chunk), c1 = min(nb, c0 + chunk);
+    unsigned long long s = 0;
+    for (uint64_t c = c0; c < c1; ++c) s += sums[c];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const unsigned long long v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0ull;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    unsigned long long run = part[threadIdx.x] - s;
+    for (uint64_t c = c0; c < c1; ++c) {
+        const unsigned long long k = sums[c];
+        sums[c] = run;
+        run += k;
+    }
+    if (threadIdx.x == 1023) sums[nb] = part[1023];
+}
+
+// Sun-plane points (3 floats per ray) and the records beyond slot 0, in ray order.
+__global__ void __launch_bounds__(kCompactBlock) compact_write_kernel(const float4* __restrict__ hits, uint64_t n,
+                                                                      const unsigned long long* __restrict__ offsets,
+                                                                      float* __restrict__ points,
+                                                                      float4* __restrict__ records) {
+    __shared__ uint32_t scratch[kCompactBlock / 32];
+    const uint64_t r = (uint64_t)blockIdx.x * kCompactBlock + threadIdx.x;
+    uint32_t c = 0;
+    if (r < n) c = row_records(hits, r);
+    uint32_t total;
+    const uint32_t ex = block_exclusive(c, scratch, total);
+    if (r >= n) return;
+    const float4 p = __ldg(&hits[r * kMaxDepth]);
+    points[3 * r] = p.y;
+    points[3 * r + 1] = p.z;
+    points[3 * r + 2] = p.w;
+    const uint64_t o = offsets[blockIdx.x] + ex;
+    for (uint32_t s = 0; s < c; ++s) records[o + s] = __ldg(&hits[r * kMaxDepth + 1 + s]);
+}
+
 __global__ void __launch_bounds__(256) halton3_table_kernel(float* __restrict__ t) {
     const uint32_t m = blockIdx.x * 256u + threadIdx.x;
     if (m < kH3T12) t[m] = halton3(m);
@@ -163,6 +253,26 @@ cudaError_t launch_trace(const TraceArgs& args, int n_prims, cudaStream_t stream
     if (!args.sgrid) return cudaErrorInvalidValue;  // scenes above the element list need their sun grid
     if (args.grid) return launch_trace_t<kAccelGrid>(args, stream);
     return launch_trace_t<kAccelBvh>(args, stream);
+}
+
+uint64_t compact_blocks(uint64_t n) { return (n + kCompactBlock - 1) / kCompactBlock; }
+
+cudaError_t launch_compact_count(const float4* hits, uint64_t n, uint8_t* counts, unsigned long long* block_sums,
+                                 cudaStream_t stream) {
+    const uint64_t nb = compact_blocks(n);
+    if (nb == 0) return cudaSuccess;
+    if (nb > 0x7FFFFFFFull) return cudaErrorInvalidValue;
+    compact_count_kernel<<<(unsigned)nb, kCompactBlock, 0, stream>>>(hits, n, counts, block_sums);
+    compact_scan_kernel<<<1, 1024, 0, stream>>>(block_sums, nb);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_compact_write(const float4* hits, uint64_t n, const unsigned long long* block_offsets, float* points,
+                                 float4* records, cudaStream_t stream) {
+    const uint64_t nb = compact_blocks(n);
+    if (nb == 0) return cudaSuccess;
+    compact_write_kernel<<<(unsigned)nb, kCompactBlock, 0, stream>>>(hits, n, block_offsets, points, records);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_flux_records(const float4* hits, uint64_t n_records, const FluxTarget& F, cudaStream_t stream) {

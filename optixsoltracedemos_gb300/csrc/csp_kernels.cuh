@@ -100,6 +100,16 @@ cudaError_t launch_sungrid_build(const SunGridJob* jobs, int n_jobs, int max_n, 
 // larger ones need args.sgrid.
 cudaError_t launch_trace(const TraceArgs& args, int n_prims, cudaStream_t stream);
 
+// Compact form of a dense hit buffer of n rays (csp_run_to_host_compact): count pass -- per ray the
+// number of records after slot 0 (uint8) and, in block_sums[compact_blocks(n) + 1], the exclusive
+// offsets of the 256-ray blocks with the total at the end -- then the write pass: the sun-plane
+// point of every ray (3 floats) and the records after slot 0, in ray order.
+uint64_t compact_blocks(uint64_t n);
+cudaError_t launch_compact_count(const float4* hits, uint64_t n, uint8_t* counts, unsigned long long* block_sums,
+                                 cudaStream_t stream);
+cudaError_t launch_compact_write(const float4* hits, uint64_t n, const unsigned long long* block_offsets, float* points,
+                                 float4* records, cudaStream_t stream);
+
 // Bin the stage-2 records of a dense hit buffer into F.counts and count records into F.stats[1..3]
 // (both zeroed by the caller).
 cudaError_t launch_flux_records(const float4* hits, uint64_t n_records, const FluxTarget& F, cudaStream_t stream);

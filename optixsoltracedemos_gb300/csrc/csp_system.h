@@ -76,6 +76,12 @@ struct System {
     size_t cap_sgrid = 0;
     SunGridJob* d_sgjob = nullptr;
     SunGridJob sgjob_host{};
+    // compact records (csp_run_to_host_compact): points, counts, block offsets, records
+    float* d_cpoints = nullptr;
+    uint8_t* d_ccounts = nullptr;
+    unsigned long long* d_csums = nullptr;
+    float4* d_crecords = nullptr;
+    uint64_t cap_compact_rays = 0, cap_crecords = 0;
     uint32_t* d_flux = nullptr;              // csp_flux_map counts
     unsigned long long* d_fstats = nullptr;  // [4]
     size_t cap_flux = 0;
@@ -105,6 +111,7 @@ struct System {
     int trace_async(cudaStream_t st);
     int run();
     int run_to_host(float* dst, uint32_t* ids);
+    int run_to_host_compact(float* points, uint8_t* counts, float* records, uint64_t capacity, uint64_t* n_records);
     int flux_map(uint32_t nx, uint32_t ny, uint32_t* counts, double dni, double* flux, bool staged = false);
 };
 

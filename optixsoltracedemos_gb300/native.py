@@ -103,6 +103,8 @@ SIGNATURES = {
     "csp_server_wait": (ctypes.c_int, [_H, ctypes.c_uint64, ctypes.c_double, _P, _P, _P]),
     "csp_server_hold": (ctypes.c_int, [_H, ctypes.c_int]),
     "csp_server_stats": (ctypes.c_int, [_H, _P]),
+    "csp_run_to_host_compact": (ctypes.c_int, [_H, _P, _P, _P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
+    "csp_write_compact_csv": (ctypes.c_int, [_P, _P, _P, ctypes.c_uint64, ctypes.c_char_p, ctypes.c_int]),
     "csp_debug_fail_allocation": (ctypes.c_int, [ctypes.c_int64]),
     "csp_set_tune_cache": (ctypes.c_int, [ctypes.c_char_p]),
     "csp_tune_cache_entries": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint32)]),
@@ -241,6 +243,27 @@ class Tracer:
         count = self.num_rays - first if count is None else count
         _check(self.lib.csp_trace_into(self.h, ctypes.c_void_p(hits_ptr), ctypes.c_void_p(ids_ptr or 0), int(first),
                                        int(count), ctypes.c_void_p(stream or 0)))
+
+    def run_to_host_compact(self, points: np.ndarray | None = None, counts: np.ndarray | None = None,
+                            records: np.ndarray | None = None):
+        """Trace and copy the records in compact form: (points [N, 3] float32, counts [N] uint8,
+        records [R, 4] float32).  Arrays given are filled (records sized for 4 N)."""
+        n = self.num_rays
+        points = np.empty((n, 3), np.float32) if points is None else points
+        counts = np.empty(n, np.uint8) if counts is None else counts
+        records = np.empty((4 * n, 4), np.float32) if records is None else records
+        nr = ctypes.c_uint64()
+        _check(self.lib.csp_run_to_host_compact(self.h, _ptr(points), _ptr(counts), _ptr(records), records.shape[0],
+                                                ctypes.byref(nr)))
+        return points, counts, records[:nr.value]
+
+    def run_to_host_compact_ptr(self, points_ptr: int, counts_ptr: int, records_ptr: int, capacity: int) -> int:
+        """run_to_host_compact into caller memory (pinned host memory for full link speed); returns
+        the number of records."""
+        nr = ctypes.c_uint64()
+        _check(self.lib.csp_run_to_host_compact(self.h, ctypes.c_void_p(points_ptr), ctypes.c_void_p(counts_ptr),
+                                                ctypes.c_void_p(records_ptr), int(capacity), ctypes.byref(nr)))
+        return nr.value
 
     def run_to_host_ptr(self, hits_ptr: int, ids_ptr: int | None = None):
         _check(self.lib.csp_run_to_host(self.h, ctypes.c_void_p(hits_ptr), ctypes.c_void_p(ids_ptr or 0)))
@@ -479,6 +502,16 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def write_compact_csv(points: np.ndarray, counts: np.ndarray, records: np.ndarray, path: str,
+                      staged: bool = False) -> None:
+    """The reference CSV (write_output) of compact records, host only."""
+    p = np.ascontiguousarray(points, np.float32)
+    c = np.ascontiguousarray(counts, np.uint8)
+    r = np.ascontiguousarray(records, np.float32)
+    _check(load().csp_write_compact_csv(_ptr(p), _ptr(c), _ptr(r), len(c), path.encode(),
+                                        OUT_STAGED if staged else 0))
 
 
 def debug_fail_allocation(after: int) -> None:

@@ -123,3 +123,29 @@ def test_staged_device_outputs(gpu, oracle32, tmp_path):
         np.testing.assert_array_equal(srv.wait(c)[0], want_plain)
     finally:
         srv.close()
+
+
+@pytest.mark.gpu
+def test_compact_transfer_matches_dense(gpu, tmp_path):
+    """csp_run_to_host_compact moves the same records as the dense copy (points, counts and records
+    expand back to the dense rows, bit for bit), fewer bytes, and its CSV is the dense CSV."""
+    from optixsoltracedemos_gb300 import native
+    from tests.test_compact_cpu import to_compact
+    for sc in (scenes.three_heliostats(num_rays=300000),
+               scenes.large_field(n_heliostats=300, sun=scenes.sun_vector(35.0, 20.0), num_rays=200000)):
+        t = native.tracer_for(sc, device=0, seed=4, record_ids=False)
+        try:
+            dense = np.zeros((sc.num_rays, 5, 4), np.float32)
+            t.run_to_host(dense.reshape(-1))
+            points, counts, records = t.run_to_host_compact()
+        finally:
+            t.close()
+        p2, c2, r2 = to_compact(dense)
+        assert np.array_equal(points, p2) and np.array_equal(counts, c2) and np.array_equal(records, r2)
+        assert records.shape[0] > 0
+        # compact bytes: 13 per ray + 16 per record, against 80 per ray
+        assert 13 * sc.num_rays + 16 * records.shape[0] < 0.5 * 80 * sc.num_rays
+        a, b = tmp_path / "dense.csv", tmp_path / "compact.csv"
+        native.write_hits_csv(dense, str(a))
+        native.write_compact_csv(points, counts, records, str(b))
+        assert a.read_bytes() == b.read_bytes()
