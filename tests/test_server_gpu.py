@@ -108,16 +108,22 @@ def test_server_admission_by_memory(gpu):
     admitted as memory frees up, and all complete."""
     from optixsoltracedemos_gb300 import native
     field = scenes.large_field(n_heliostats=2000, num_rays=1).elements
-    a256 = lambda x: (x + 255) // 256 * 256  # noqa: E731
-    # sun frame, grid descriptor, flux map, counters, prims, optics, two AABB arrays (grid scene: no nodes)
-    per_request = (a256(208) + a256(80) + a256(100 * 100 * 4) + a256(32) + a256(2001 * 64) + a256(2001 * 16)
-                   + 2 * a256(2001 * 32))
-    srv = native.Server(0, memory_budget=3 * per_request + 1024, max_active=64, step_rays=8 << 20)
+    rs = np.random.default_rng(1)
+    suns = [scenes.sun_vector(rs.uniform(20, 70), rs.uniform(-90, 90)) for _ in range(10)]
+    poses = [scenes.reaim(field, s) for s in suns]
+    # a request's device block (records, grids, candidate lists, flux map), measured on one alone;
+    # the poses change its grids by a few per cent, so 3.5 blocks hold three requests, never four
+    probe = native.Server(0, memory_budget=256 << 20, max_active=4)
+    try:
+        sid = probe.add_scene(field)
+        probe.wait(probe.submit(sid, suns[0], 0, 4.65e-3, 1 << 20, poses=poses[0]), timeout=120)
+        per_request = int(probe.stats()["peak_arena_bytes"])
+    finally:
+        probe.close()
+    budget = int(3.5 * per_request)
+    srv = native.Server(0, memory_budget=budget, max_active=64, step_rays=8 << 20)
     try:
         sid = srv.add_scene(field)
-        rs = np.random.default_rng(1)
-        suns = [scenes.sun_vector(rs.uniform(20, 70), rs.uniform(-90, 90)) for _ in range(10)]
-        poses = [scenes.reaim(field, s) for s in suns]
         ids = [srv.submit(sid, suns[k], 0, 4.65e-3, 6_000_000, seed=k, instance=k, poses=poses[k]) for k in range(10)]
         for rid in ids:
             c, st, _ = srv.wait(rid, timeout=120)
@@ -125,7 +131,7 @@ def test_server_admission_by_memory(gpu):
         stats = srv.stats()
         assert stats["completed"] == 10
         assert 1 <= stats["peak_active"] <= 3
-        assert stats["peak_arena_bytes"] <= 3 * per_request + 1024
+        assert stats["peak_arena_bytes"] <= budget
     finally:
         srv.close()
 
