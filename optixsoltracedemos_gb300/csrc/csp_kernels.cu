@@ -44,12 +44,12 @@ struct TraceSmem {
     typename PlainCfg<kAccel>::Core core;
 };
 
-// Resident 128-thread CTAs per SM the register budget is cut for: six for the element-list kernel
-// (short latency chains), eight for the BVH and grid kernels (64 registers: more warps to cover
-// the dependent loads of the candidate and cell lists).
+// Resident 128-thread CTAs per SM the register budget is cut for: eight (64 registers), which
+// measured faster than six or seven for every kernel -- more warps to cover the record stream of the
+// element-list kernel and the dependent loads of the candidate and cell lists of the others.
 template <int kAccel>
 constexpr int trace_min_blocks() {
-    return kAccel == kAccelFlat ? 6 : 8;
+    return 8;
 }
 
 // Persistent kernel over the tiles of one launch (static round robin); dense records out.
