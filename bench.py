@@ -54,17 +54,20 @@ sys.path.insert(0, ROOT)
 
 METRIC = "rays/s on 1 GB300 (batched/served vs plain trace) at flux L2<=1%; p50/p99 latency"
 BYTES_PER_RAY = 80  # 5 float4 hit records per ray, fully rewritten by every plain trace
-# dram__bytes_read.sum + dram__bytes_write.sum of one full-size trace_kernel launch of the single
-# parabolic workload (34,487,552 + 1,318,957,568 bytes), from an ncu capture of
-# `python bench.py --workload single_parabolic --steps 3 --warmup 2` (kernel trace_kernel, one launch)
-NCU_TRAFFIC_PER_LAUNCH = 1371278592
+# dram__bytes_read.sum + dram__bytes_write.sum of the single parabolic workload's trace_kernel per
+# launch of 16,777,216 rays: 4 x (8,776,704 + 291,551,232) bytes, scaled by the rays from
+# `ncu --set full -k regex:^trace_kernel -s 2 -c 1` of `python bench.py --workload single_parabolic
+# --rays 4194304 --steps 2 --warmup 2 --no-cpu-baseline --no-accuracy --e2e-steps 0` (the record
+# stream grows with the rays; at that size ~35 MB of the last records are still in L2 when the
+# kernel ends)
+NCU_TRAFFIC_PER_LAUNCH = 4 * (8776704 + 291551232)
 # Batch kernel (field grid) on the batched workload: warp instructions and DRAM bytes per traced ray,
-# from `ncu --set full` of `python bench.py --workload batched --instances 8 --tuning 256,0,16
-# --steps 1 --warmup 3 --no-systems --no-cpu-baseline --plain-instances 1` (kernel batch_kernel,
-# one launch): smsp__inst_executed.sum and dram__bytes_read.sum + dram__bytes_write.sum divided by
-# that launch's rays.  None until captured for the current kernel.
-BATCH_WARP_INST_PER_RAY = None
-BATCH_DRAM_BYTES_PER_RAY = None
+# from `ncu --set full -k regex:^batch_kernel -s 2 -c 1` of `python bench.py --workload batched
+# --instances 8 --tuning 256,4,16 --steps 1 --warmup 3 --no-systems --no-cpu-baseline
+# --plain-instances 1` (one launch over 42,028,566 rays): smsp__inst_executed.sum = 3,451,210,565
+# and dram__bytes_read.sum + dram__bytes_write.sum = 25,467,136 + 33,280 bytes, per ray.
+BATCH_WARP_INST_PER_RAY = 3451210565 / 42028566
+BATCH_DRAM_BYTES_PER_RAY = (25467136 + 33280) / 42028566
 ISSUE_PER_SM_PER_CYCLE = 4  # one warp instruction per cycle per scheduler, 4 schedulers per SM
 
 
@@ -413,6 +416,8 @@ def measure_plain(args, sc, local, world, pg, steps, warmup, e2e_steps, accuracy
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config(sc),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": NCU_TRAFFIC_PER_LAUNCH if (N == 1 << 24 and sc.name == "single_parabolic") else None,
+                     "traffic_source": "ncu dram bytes of a 4,194,304-ray launch x 4" if (
+                         N == 1 << 24 and sc.name == "single_parabolic") else None,
                      "peak_source": peak_kind, "algorithmic_bytes_per_launch": BYTES_PER_RAY * N,
                      "launch_ms": launch_s * 1e3},
         "gpu_launches": steps, "clocks": clocks,

@@ -465,9 +465,9 @@ void Batch::fill_instance(size_t i) {
     }
 }
 
-// Instance descriptors and tile tables of both groups for the given tile sizes; `sample` > 0
-// limits every instance to its first rays (autotuner), 0 = all rays.
-void Batch::fill_descs(const int* block, double sample, std::vector<InstanceDesc>* out_desc,
+// Instance descriptors and tile tables of both groups for the given tile sizes; `sample` (the
+// autotuner's): the instances traced whole, the others get no rays; nullptr = all of every instance.
+void Batch::fill_descs(const int* block, const std::vector<bool>* sample, std::vector<InstanceDesc>* out_desc,
                        std::vector<uint64_t>* out_tb) {
     const size_t n = inst.size();
     for (int g = 0; g < kBatchGroups; ++g) {
@@ -480,7 +480,7 @@ void Batch::fill_descs(const int* block, double sample, std::vector<InstanceDesc
         const Place& p = place[i];
         const int g = p.group;
         uint64_t rays = b.rays;
-        if (sample > 0) rays = std::min<uint64_t>(rays, (uint64_t)std::ceil(rays * sample) + (uint64_t)block[g]);
+        if (sample && !(*sample)[i]) rays = 0;
         InstanceDesc& d = out_desc[g][p.slot];
         d.args.nodes = reinterpret_cast<const Node*>(d_arena + p.nodes);
         d.args.prims = reinterpret_cast<const Prim*>(d_arena + p.prims);
@@ -577,11 +577,30 @@ int Batch::autotune(int g, BatchTuning& best) {
             for (int chunk : {1, 4, 16, 64}) cands.push_back(BatchTuning{block, c, chunk});
     }
     if (cands.empty()) return set_error(CSP_ERR_CUDA, "no launchable configuration of the batch kernel");
-    uint64_t total = 0;
-    for (size_t i = 0; i < inst.size(); ++i)
-        if (place[i].group == g) total += inst[i].rays;
+    // the sample: whole instances of the group, spread over the batch, until the ray budget of a
+    // candidate is reached (whole instances, so that the grabs and instance switches of a candidate
+    // are the full run's)
     const double budget = g == kAccelFlat ? 256e6 : (g == kAccelGrid ? 96e6 : 32e6);  // rays per candidate
-    const double sample = std::min(1.0, std::max(1e-4, budget / std::max<double>(1.0, (double)total)));
+    std::vector<size_t> members;
+    for (size_t i = 0; i < inst.size(); ++i)
+        if (place[i].group == g) members.push_back(i);
+    std::vector<bool> sample(inst.size(), false);
+    {
+        // members in bit-reversed order of their position: any prefix is spread over the batch
+        std::vector<std::pair<uint32_t, size_t>> order;
+        for (size_t k = 0; k < members.size(); ++k) {
+            uint32_t r = 0;
+            for (int b = 0; b < 32; ++b) r |= (uint32_t)((k >> b) & 1u) << (31 - b);
+            order.emplace_back(r, members[k]);
+        }
+        std::sort(order.begin(), order.end());
+        double taken = 0.0;
+        for (const auto& o : order) {
+            if (taken >= budget) break;
+            sample[o.second] = true;
+            taken += (double)inst[o.second].rays;
+        }
+    }
     std::vector<unsigned char> img(up_bytes);
     double best_ms = 1e30;
     int rc = CSP_OK;
@@ -589,7 +608,7 @@ int Batch::autotune(int g, BatchTuning& best) {
         const int block[kBatchGroups] = {t.block, t.block, t.block};
         std::vector<InstanceDesc> desc[kBatchGroups];
         std::vector<uint64_t> tb[kBatchGroups];
-        fill_descs(block, sample, desc, tb);
+        fill_descs(block, &sample, desc, tb);
         // descs and tile tables only: the element records already on the device stay
         const size_t lo = desc_off[0], hi = refit_off;
         write_descs(desc, tb, img.data());
@@ -717,7 +736,7 @@ int Batch::run_async() {
     for (int g = 0; g < kBatchGroups; ++g) block[g] = used[g].block;
     std::vector<InstanceDesc> desc[kBatchGroups];
     std::vector<uint64_t> tb[kBatchGroups];
-    fill_descs(block, 0.0, desc, tb);
+    fill_descs(block, nullptr, desc, tb);
     write_descs(desc, tb, h_stage);
     builds.clear();  // everything the device needs is in the staging image now
     builds.shrink_to_fit();

@@ -115,7 +115,8 @@ struct Batch {
     const HostScene& scene_of(size_t i) const;
     const HostGrid& grid_of(size_t i) const;
     void fill_instance(size_t i);
-    void fill_descs(const int* block, double sample, std::vector<InstanceDesc>* desc, std::vector<uint64_t>* tb);
+    void fill_descs(const int* block, const std::vector<bool>* sample, std::vector<InstanceDesc>* desc,
+                    std::vector<uint64_t>* tb);
     void write_descs(const std::vector<InstanceDesc>* desc, const std::vector<uint64_t>* tb, unsigned char* img);
     BatchLaunch launch_of(int g, uint64_t total_tiles, int chunk) const;
     int enqueue_prefix(cudaStream_t st);
