@@ -61,6 +61,11 @@ BYTES_PER_RAY = 80  # 5 float4 hit records per ray, fully rewritten by every pla
 # stream grows with the rays; at that size ~35 MB of the last records are still in L2 when the
 # kernel ends)
 NCU_TRAFFIC_PER_LAUNCH = 4 * (8776704 + 291551232)
+# The same for the field kernel (trace_kernel<grid>) of the 10,000-heliostat field per launch of
+# 268,435,456 rays: 64 x (9,310,208 + 297,519,360) bytes from `ncu --set full -k regex:^trace_kernel
+# -s 2 -c 1` of `python bench.py --workload large_field --rays 4194304 --steps 2 --warmup 2
+# --no-cpu-baseline`, scaled by the rays
+NCU_TRAFFIC_PER_LAUNCH_FIELD = 64 * (9310208 + 297519360)
 # Batch kernel (field grid) on the batched workload: warp instructions and DRAM bytes per traced ray,
 # from `ncu --set full -k regex:^batch_kernel -s 2 -c 1` of `python bench.py --workload batched
 # --instances 8 --tuning 256,4,16 --steps 1 --warmup 3 --no-systems --no-cpu-baseline
@@ -415,9 +420,11 @@ def measure_plain(args, sc, local, world, pg, steps, warmup, e2e_steps, accuracy
         "warmup": warmup, "ms_per_step": total_s / steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config(sc),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": NCU_TRAFFIC_PER_LAUNCH if (N == 1 << 24 and sc.name == "single_parabolic") else None,
-                     "traffic_source": "ncu dram bytes of a 4,194,304-ray launch x 4" if (
-                         N == 1 << 24 and sc.name == "single_parabolic") else None,
+                     "traffic": (NCU_TRAFFIC_PER_LAUNCH if (N == 1 << 24 and sc.name == "single_parabolic") else
+                                 NCU_TRAFFIC_PER_LAUNCH_FIELD if (N == 1 << 28 and sc.name == "large_field") else None),
+                     "traffic_source": ("ncu dram bytes of a 4,194,304-ray launch x 4" if (
+                         N == 1 << 24 and sc.name == "single_parabolic") else "ncu dram bytes of a 4,194,304-ray launch x 64"
+                         if (N == 1 << 28 and sc.name == "large_field") else None),
                      "peak_source": peak_kind, "algorithmic_bytes_per_launch": BYTES_PER_RAY * N,
                      "launch_ms": launch_s * 1e3},
         "gpu_launches": steps, "clocks": clocks,
