@@ -100,6 +100,35 @@ def test_reach_pretest_edges_bit_exact(gpu, oracle32, name):
         assert (oh[:, 1:, 0] != 0).any()
 
 
+def _sungrid_edge_configs():
+    """Field scenes at the edges of the sun-ray candidate grid (one cell of reach rectangles per sun
+    ray, rectangles of more than 64 cells in a global list every ray scans): a sun 3 degrees above
+    the horizon (rectangles stretched along the plane's steep axis), a wide Gaussian sun and a wide
+    pillbox (rectangles widened by the cone, many of them global), a collimated zenith sun
+    (axis-parallel rays), and a parabolic field at a low sun."""
+    low = scenes.large_field(n_heliostats=300, sun=scenes.sun_vector(3.0, 40.0))
+    gauss = scenes.large_field(n_heliostats=300, sun=scenes.sun_vector(30.0, -20.0))
+    gauss.sun_shape, gauss.sun_param = scenes.SUN_GAUSSIAN, 40e-3
+    wide = scenes.large_field(n_heliostats=300, sun=scenes.sun_vector(50.0, 100.0), sun_angle=0.2)
+    zenith = scenes.large_field(n_heliostats=300, sun=np.array([0.0, 0.0, 1.0]), sun_angle=0.0)
+    par_low = scenes.large_field(n_heliostats=300, sun=scenes.sun_vector(8.0, -150.0), parabolic=True)
+    return {"sun_3deg": low, "gaussian_40mrad": gauss, "pillbox_0.2rad": wide, "collimated_zenith": zenith,
+            "parabolic_sun_8deg": par_low}
+
+
+@pytest.mark.parametrize("name", list(_sungrid_edge_configs()))
+def test_sungrid_edges_bit_exact(gpu, oracle32, name):
+    sc = _sungrid_edge_configs()[name]
+    n = 60000
+    for seed, inst in ((7, 0), (31, 4)):
+        oh, oi = oracle32.trace(sc.elements, sc.sun_dir, sc.sun_shape, sc.sun_param, count=n, seed=seed, instance=inst)
+        for accel in (native.ACCEL_AUTO, native.ACCEL_BVH):
+            hits, ids = gpu_trace(sc, n, seed=seed, instance=inst, accel=accel)
+            np.testing.assert_array_equal(ids, oi, err_msg=f"{name} accel {accel}")
+            np.testing.assert_array_equal(hits, oh.astype(np.float32), err_msg=f"{name} accel {accel}")
+        assert (oh[:, 1:, 0] != 0).any()
+
+
 @pytest.mark.parametrize("first", [(1 << 32) - 5000, (1 << 40) + 12345], ids=["2^32-5000", "2^40+12345"])
 def test_ray_indices_beyond_32_bits(gpu, oracle32, first):
     """Ray windows starting near and far beyond 2^32 (csp_trace_into with a first ray): the Halton
