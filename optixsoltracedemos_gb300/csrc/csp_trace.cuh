@@ -1095,7 +1095,9 @@ __device__ __forceinline__ int bounce_batch(const typename C::Args& A, const Sin
             w = sm.qw[q];
             ray = sm.qray[q];
         }
-        __syncthreads();
+        // the barrier both ends the reads of the popped entries and publishes the new size: no
+        // thread appends (atomicAdd on qsize, then writes from `base` on) before it, and none read
+        // qsize since the barrier that closed the last append
         if (threadIdx.x == 0) sm.qsize = base;
         __syncthreads();
         if (have) {
