@@ -303,8 +303,9 @@ CSP_API int csp_batch_get_transfer(csp_batch b, uint64_t* h2d_bytes, uint64_t* d
  * queues a trace request: a scene, optional per-request poses (same count and surfaces: heliostat
  * tracking, refitted in place on the device), a sun, a ray count, seed and Philox instance id.
  * The worker admits requests as slots (max_active) and arena memory free up and traces every active
- * request's next slice of rays (step_rays across all active requests per step, 0 = 64M) in one
- * persistent launch per kernel group, so requests that arrive while others run share the GPU.
+ * request's next slice of rays (step_rays across all active requests per step, 0 = 64M, but at
+ * least 2^24 rays per request, or its remaining rays) in one persistent launch per kernel group,
+ * so requests that arrive while others run share the GPU.
  * Each request's flux map is accumulated on the device and equals the batch / plain result for the
  * same inputs, alone or in any mix.  Replaces the reference's one-scene run() loop
  * (lib/soltrace_system.cpp:145-184) for many concurrent callers. */

@@ -145,7 +145,7 @@ struct Server {
     uint32_t nx = 100, ny = 100;
     int out_flags = 0;  // CSP_OUT_* given to requests at submission
     int max_active = 64;
-    uint64_t step_rays = 64ull << 20;  // rays per step across all active requests (target)
+    uint64_t step_rays = 64ull << 20;  // rays per step across all active requests (target; see kMinSlice)
     size_t budget = 0;
 
     std::vector<std::unique_ptr<SScene>> scenes;
@@ -583,12 +583,22 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
 // mixed request workload (fields of 3 to 10,000 heliostats).
 constexpr BatchTuning kServeTuning[kBatchGroups] = {{256, 0, 16}, {128, 0, 4}, {256, 0, 16}};
 
+// Smallest slice of an active request in one step (its remaining rays if fewer).  The step's tiles
+// run request after request, so with small slices every 16-tile grab of a CTA lands in another
+// request than its last one, and each switch drains the CTA's queues in partial batches; a slice
+// of 2^24 rays spans ~6 grabs of every resident CTA.  On the mixed request workload (300 requests
+// over fields of 3 to 10,000 heliostats, 64 active) it measured 1.86e10 served rays/s at saturation
+// against 1.48e10 with 2^20-ray slices, saturation p50 / p99 latency 10.6 / 37 ms against 20.5 /
+// 135 ms, and the same latency at 200 requests/s (p50 0.61 ms, p99 6.3 ms), where few requests
+// are active and step_rays / active exceeds it anyway.
+constexpr uint64_t kMinSlice = 1ull << 24;
+
 int Server::step_launch(std::vector<SRequest*>& finishing, uint64_t& rays) {
     NvtxRange nvtx("csp server step launch");
     rays = 0;
     finishing.clear();
     if (active.empty()) return CSP_OK;
-    const uint64_t quantum = std::max<uint64_t>(1u << 20, step_rays / active.size());
+    const uint64_t quantum = std::max<uint64_t>(kMinSlice, step_rays / active.size());
     std::vector<InstanceDesc> desc[kBatchGroups];
     std::vector<uint64_t> tb[kBatchGroups];
     uint64_t tiles[kBatchGroups] = {};
