@@ -267,8 +267,10 @@ CSP_API int csp_batch_add_instance(csp_batch b, uint32_t scene_id, const csp_ele
 CSP_API int csp_batch_clear_instances(csp_batch b);
 CSP_API int csp_batch_num_instances(csp_batch b, uint32_t* count);
 /* Launch parameters: CTA/tile size (128 or 256 rays), resident CTAs per SM (0 = occupancy limit),
- * tiles per work grab.  block = 0 selects the autotuner (default), which times candidates on a
- * sample of the batch at the first run of each scene class and keeps the fastest per device. */
+ * the most tiles one work grab takes (grabs shrink towards single tiles as the work runs out).
+ * block = 0 selects the autotuner (default), which times tile sizes and CTAs per SM on a sample of
+ * the batch at the first run of each scene class (grabs of at most 256 tiles) and keeps the fastest
+ * per device. */
 CSP_API int csp_batch_set_tuning(csp_batch b, int block, int ctas_per_sm, int chunk);
 /* The parameters the last run used for one kernel group: CSP_ACCEL_LIST (<= 8 elements),
  * CSP_ACCEL_BVH or CSP_ACCEL_GRID instances (an instance whose poses move an origin or change a

@@ -127,10 +127,14 @@ __global__ void __launch_bounds__(kB, batch_threads_per_sm<kAccel>() / kB) batch
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) {
-            // chunks of L.chunk tiles while much work is left, single tiles near the end (a chunk
-            // taken last would otherwise run alone)
+            // guided grabs: a quarter of an even share of the tiles left (as this CTA last saw
+            // them), at most L.chunk and at least one, so grabs shrink towards single tiles at the
+            // end (a large grab taken last would otherwise run alone).  Large grabs early keep a CTA
+            // on one instance across consecutive grabs: each switch drains its queues in partial
+            // batches.
             const unsigned long long left = L.total_tiles > sm.grab ? L.total_tiles - sm.grab : 0;
-            const unsigned long long want = left > (unsigned long long)gridDim.x * L.chunk * 4 ? L.chunk : 1;
+            const unsigned long long want =
+                max(1ull, min((unsigned long long)L.chunk, left / ((unsigned long long)gridDim.x * 4)));
             sm.grab = atomicAdd(L.next_tile, want);
             sm.want = want;
         }
