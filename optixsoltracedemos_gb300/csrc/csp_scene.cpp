@@ -259,7 +259,9 @@ int pack_element(const csp_element& e, bool last, uint32_t& type, Aabb& box, Pri
     return CSP_OK;
 }
 
-int build_elements(const csp_element* el, uint32_t n, HostScene& s, std::string& err) {
+namespace {
+
+int check_count(uint32_t n, std::string& err) {
     if (n == 0) {
         err = "scene has no elements";
         return CSP_ERR_BAD_SCENE;
@@ -268,24 +270,64 @@ int build_elements(const csp_element* el, uint32_t n, HostScene& s, std::string&
         err = "too many elements";
         return CSP_ERR_BAD_SCENE;
     }
+    return CSP_OK;
+}
+
+void size_scene(uint32_t n, HostScene& s) {
     s.prims.assign(n, Prim{});
     s.optics.assign(n, Optics{});
     s.aabbs.assign(n, Aabb{});
     s.prune.assign(n, Aabb{});
     s.types.assign(n, 0);
-    for (uint32_t i = 0; i < n; ++i) {
-        const char* why = "";
-        const int rc = pack_element(el[i], i + 1 == n, s.types[i], s.aabbs[i], s.prims[i], s.optics[i], &s.prune[i], why);
+}
+
+// Packs elements [begin, end); returns the index of the first that fails (and its status and
+// message), or end.
+uint32_t pack_range(const csp_element* el, uint32_t n, uint32_t begin, uint32_t end, HostScene& s, int& rc,
+                    const char*& why) {
+    for (uint32_t i = begin; i < end; ++i) {
+        rc = pack_element(el[i], i + 1 == n, s.types[i], s.aabbs[i], s.prims[i], s.optics[i], &s.prune[i], why);
         // the exact box carries its element and entity type (the sun grid's candidate tests)
         s.aabbs[i].lo.w = u2f((s.types[i] << kTypeShift) | i);
-        if (rc) {
-            err = "element " + std::to_string(i) + ": " + why;
-            if (el[i].surface != CSP_SURFACE_FLAT && el[i].surface != CSP_SURFACE_PARABOLIC &&
-                el[i].surface != CSP_SURFACE_CYLINDER)
-                err += " " + std::to_string(el[i].surface);
-            return rc;
-        }
+        if (rc) return i;
     }
+    return end;
+}
+
+int pack_error(const csp_element* el, uint32_t i, int rc, const char* why, std::string& err) {
+    err = "element " + std::to_string(i) + ": " + why;
+    if (el[i].surface != CSP_SURFACE_FLAT && el[i].surface != CSP_SURFACE_PARABOLIC &&
+        el[i].surface != CSP_SURFACE_CYLINDER)
+        err += " " + std::to_string(el[i].surface);
+    return rc;
+}
+
+}  // namespace
+
+int build_elements(const csp_element* el, uint32_t n, HostScene& s, std::string& err) {
+    int rc = check_count(n, err);
+    if (rc) return rc;
+    size_scene(n, s);
+    const char* why = "";
+    const uint32_t bad = pack_range(el, n, 0, n, s, rc, why);
+    return bad < n ? pack_error(el, bad, rc, why, err) : CSP_OK;
+}
+
+int build_elements(const csp_element* el, uint32_t n, HostScene& s, std::string& err, const ParallelFor& pf) {
+    int rc = check_count(n, err);
+    if (rc) return rc;
+    size_scene(n, s);
+    const size_t chunks = (n + kBuildChunk - 1) / kBuildChunk;
+    std::vector<uint32_t> bad(chunks);
+    std::vector<int> status(chunks, CSP_OK);
+    std::vector<const char*> whys(chunks, "");
+    pf(chunks, [&](size_t c) {
+        const uint32_t b = (uint32_t)(c * kBuildChunk), e = std::min<uint32_t>(n, b + kBuildChunk);
+        bad[c] = pack_range(el, n, b, e, s, status[c], whys[c]);
+        if (bad[c] == e) bad[c] = n;
+    });
+    for (size_t c = 0; c < chunks; ++c)
+        if (bad[c] < n) return pack_error(el, bad[c], status[c], whys[c], err);
     return CSP_OK;
 }
 

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -26,6 +27,15 @@ struct HostScene {
 // with `err` filled.  The geometry arithmetic is the reference's (lib/element.cpp, lib/math_util.h,
 // cuda/GeometryDataST.h constructors), in the same double/float operation order.
 int build_elements(const csp_element* el, uint32_t n, HostScene& s, std::string& err);
+
+// Runs body(k) for every k in [0, tasks), possibly on several threads, and returns when all are
+// done.
+using ParallelFor = std::function<void(size_t tasks, const std::function<void(size_t)>& body)>;
+
+// build_elements with the elements packed in ranges of kBuildChunk through `pf`: the same records
+// (each element's packing reads only that element), and the same error (the lowest failing element).
+constexpr uint32_t kBuildChunk = 1024;
+int build_elements(const csp_element* el, uint32_t n, HostScene& s, std::string& err, const ParallelFor& pf);
 
 // The records of one element, as build_elements makes them: entity type, exact AABB, Prim, Optics
 // and (when `prune` is not null) the pruning box.  Allocates nothing.  Returns CSP_OK, or

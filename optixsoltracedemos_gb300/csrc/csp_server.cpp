@@ -7,10 +7,12 @@
 //      launch per kernel group (the batch kernels of csp_batch.cu), receiver records binned into the
 //      request's resident flux map; requests whose last slice is in the step copy their flux map,
 //      counters and sun frame to pinned host memory behind the launch;
-//   2. while the GPU runs: admit pending requests while slots and device memory allow -- host
-//      element builds (the reference's geometry arithmetic, as the single-scene path), upload,
-//      refit of the scene's BVH topology in place into the request's nodes, sun plane, sun-ray
-//      candidate grid; all queued on the stream behind step k, so the request joins step k+1;
+//   2. while the GPU runs: admit pending requests while slots and device memory allow -- one
+//      upload of each request's host part (its element records and field grid were built at
+//      submission: the reference's geometry arithmetic, as the single-scene path, in ranges of
+//      elements on the server's host threads), refit of the scene's BVH topology in place into the
+//      request's nodes, sun plane, sun-ray candidate grid; all on the admission stream, which the
+//      step stream waits for before step k+1, so the request joins step k+1;
 //   3. wait for the step, complete the finished requests (latency = completion - submission), free
 //      their device memory.
 // A request's result does not depend on what it was batched with or how its rays were sliced: its
@@ -25,6 +27,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -40,6 +43,78 @@
 
 namespace csp {
 namespace {
+
+// Fixed set of host threads for the parallel part of a submission (element records in ranges).
+// run() executes body(k) for k in [0, tasks) on the pool and the calling thread and returns when all
+// are done; concurrent callers take turns.
+class HostPool {
+public:
+    void start(unsigned threads) {
+        for (unsigned t = 0; t < threads; ++t) th_.emplace_back([this] { loop(); });
+    }
+    void stop() {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            quit_ = true;
+        }
+        cv_.notify_all();
+        for (auto& t : th_) t.join();
+        th_.clear();
+    }
+    void run(size_t tasks, const std::function<void(size_t)>& body) {
+        std::lock_guard<std::mutex> turn(run_mu_);
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            body_ = &body;
+            tasks_ = tasks;
+            next_ = 0;
+            left_ = tasks;
+            ++gen_;
+        }
+        cv_.notify_all();
+        work();
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_done_.wait(lk, [&] { return left_ == 0; });
+        body_ = nullptr;
+    }
+
+private:
+    // take tasks of the current job until none is left
+    void work() {
+        for (;;) {
+            size_t k;
+            const std::function<void(size_t)>* body;
+            {
+                std::lock_guard<std::mutex> lk(mu_);
+                if (!body_ || next_ >= tasks_) return;
+                k = next_++;
+                body = body_;
+            }
+            (*body)(k);
+            std::lock_guard<std::mutex> lk(mu_);
+            if (--left_ == 0) cv_done_.notify_all();
+        }
+    }
+    void loop() {
+        uint64_t seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return quit_ || gen_ != seen; });
+                if (quit_) return;
+                seen = gen_;
+            }
+            work();
+        }
+    }
+    std::mutex mu_, run_mu_;
+    std::condition_variable cv_, cv_done_;
+    std::vector<std::thread> th_;
+    const std::function<void(size_t)>* body_ = nullptr;
+    size_t tasks_ = 0, next_ = 0, left_ = 0;
+    uint64_t gen_ = 0;
+    bool quit_ = false;
+};
 
 using Clock = std::chrono::steady_clock;
 
@@ -142,6 +217,12 @@ struct Arena {
 struct Server {
     int device = -1;
     cudaStream_t stream = nullptr;
+    // admissions (uploads, refits, sun planes, sun-ray grids) go to their own stream: the uploads
+    // overlap the running step, the kernels fill its tail; the step stream waits on adm_done
+    // before the next step
+    cudaStream_t adm_stream = nullptr;
+    cudaEvent_t adm_done = nullptr;
+    HostPool pool;  // element records of large submissions, in ranges
     uint32_t nx = 100, ny = 100;
     int out_flags = 0;  // CSP_OUT_* given to requests at submission
     int max_active = 64;
@@ -208,6 +289,7 @@ void Server::stop() {
     }
     cv_work.notify_all();
     if (worker.joinable()) worker.join();
+    pool.stop();
     {
         // requests still queued (admission held, or the worker stopped on an error) will never
         // run: fail them, wake their waiters and let every waiter leave before anything is freed
@@ -223,6 +305,7 @@ void Server::stop() {
     }
     if (device >= 0) cudaSetDevice(device);
     if (stream) cudaStreamSynchronize(stream);
+    if (adm_stream) cudaStreamSynchronize(adm_stream);
     for (auto& s : scenes) {
         cudaFree(s->d_topo);
         cudaFree(s->d_cells);
@@ -245,6 +328,10 @@ void Server::stop() {
     d_arena = d_step = nullptr;
     d_counter = nullptr;
     h_step = h_adm = h_res = nullptr;
+    if (adm_done) cudaEventDestroy(adm_done);
+    adm_done = nullptr;
+    if (adm_stream) cudaStreamDestroy(adm_stream);
+    adm_stream = nullptr;
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
 }
@@ -257,6 +344,9 @@ int Server::start(int dev, size_t budget_bytes, int max_act, uint64_t step_targe
     if (rc) return rc;
     h3t12 = halton3_table();
     if ((rc = cuda_status(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate"))) return rc;
+    if ((rc = cuda_status(cudaStreamCreateWithFlags(&adm_stream, cudaStreamNonBlocking), "cudaStreamCreate"))) return rc;
+    if ((rc = cuda_status(cudaEventCreateWithFlags(&adm_done, cudaEventDisableTiming), "cudaEventCreate"))) return rc;
+    pool.start(std::min(7u, std::thread::hardware_concurrency() / 2));
     size_t free_b = 0, total_b = 0;
     if ((rc = cuda_status(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo"))) return rc;
     budget = budget_bytes ? budget_bytes : std::min<size_t>(free_b / 2, (size_t)8 << 30);
@@ -312,21 +402,47 @@ int Server::add_scene(const csp_element* el, uint32_t n, uint32_t* id) {
     return CSP_OK;
 }
 
-size_t Server::request_bytes(const SRequest& r) const {
+// Arena block of a request, offsets from its start.  Everything the host provides comes first and
+// leaves in one upload at admission: the grid descriptor, the flux map and counters (zeros), and
+// with per-request poses the element records and the field grid of the poses.  After it, what
+// kernels write: the sun frame, the refitted BVH nodes and the sun-ray candidate grid.
+struct BlockLayout {
+    size_t grid = 0, counts = 0, stats = 0, prims = 0, optics = 0, aabbs = 0, prune = 0, cells = 0, items = 0,
+           global = 0, upload = 0, sun = 0, nodes = 0, sgrid = 0, total = 0;
+};
+
+static BlockLayout block_layout(const SRequest& r, uint32_t nx, uint32_t ny) {
     const SScene& s = *r.sc;
     const size_t n = s.elements.size();
-    size_t b = align256(sizeof(SunFrame)) + align256(sizeof(GridDesc)) + align256((size_t)nx * ny * sizeof(uint32_t)) +
-               align256(4 * sizeof(unsigned long long));
-    if (r.group != kAccelFlat) b += align256(sungrid_bytes((uint32_t)n));
+    BlockLayout L;
+    size_t o = 0;
+    auto take = [&](size_t& at, size_t bytes) {
+        at = o;
+        o += align256(bytes);
+    };
+    take(L.grid, sizeof(GridDesc));
+    take(L.counts, (size_t)nx * ny * sizeof(uint32_t));
+    take(L.stats, 4 * sizeof(unsigned long long));
     if (!r.poses.empty()) {
-        b += align256(n * sizeof(Prim)) + align256(n * sizeof(Optics)) + 2 * align256(n * sizeof(Aabb));
-        if (r.group != kAccelGrid) b += align256(s.base.nodes.size() * sizeof(Node));
-        else
-            b += align256(r.grid.cell_start.size() * sizeof(uint32_t)) + align256(r.grid.items.size() * sizeof(Aabb)) +
-                 align256(std::max<size_t>(1, r.grid.global.size()) * sizeof(Aabb));
+        take(L.prims, n * sizeof(Prim));
+        take(L.optics, n * sizeof(Optics));
+        take(L.aabbs, n * sizeof(Aabb));
+        take(L.prune, n * sizeof(Aabb));
+        if (r.group == kAccelGrid) {
+            take(L.cells, r.grid.cell_start.size() * sizeof(uint32_t));
+            take(L.items, r.grid.items.size() * sizeof(Aabb));
+            take(L.global, std::max<size_t>(1, r.grid.global.size()) * sizeof(Aabb));
+        }
     }
-    return b;
+    L.upload = o;
+    take(L.sun, sizeof(SunFrame));
+    if (!r.poses.empty() && r.group != kAccelGrid) take(L.nodes, s.base.nodes.size() * sizeof(Node));
+    if (r.group != kAccelFlat) take(L.sgrid, sungrid_bytes((uint32_t)n));
+    L.total = o;
+    return L;
 }
+
+size_t Server::request_bytes(const SRequest& r) const { return block_layout(r, nx, ny).total; }
 
 int Server::submit(const SRequest& in, uint64_t* id) {
     const SScene* sp = nullptr;
@@ -343,9 +459,16 @@ int Server::submit(const SRequest& in, uint64_t* id) {
         for (size_t k = 0; k < s.elements.size(); ++k)
             if (in.poses[k].surface != s.elements[k].surface || in.poses[k].aperture != s.elements[k].aperture)
                 return set_error(CSP_ERR_BAD_SCENE, "request pose " + std::to_string(k) + " changes the surface type");
-        // host work of the request, in the submitting thread: element records and grid of its poses
+        // host work of the request, in the submitting thread (the element records of large requests in
+        // ranges on the server's host threads): element records and grid of its poses
         std::string err;
-        const int rc = build_elements(r->poses.data(), (uint32_t)r->poses.size(), r->hs, err);
+        const uint32_t n = (uint32_t)r->poses.size();
+        const int rc = n >= 4 * kBuildChunk
+                           ? build_elements(r->poses.data(), n, r->hs, err,
+                                            [this](size_t tasks, const std::function<void(size_t)>& body) {
+                                                pool.run(tasks, body);
+                                            })
+                           : build_elements(r->poses.data(), n, r->hs, err);
         if (rc) return set_error(rc, err);
         if (s.group != kAccelFlat) build_grid(r->hs, r->grid);
     }
@@ -375,7 +498,7 @@ int Server::submit(const SRequest& in, uint64_t* id) {
 }
 
 // Move pending requests into device memory while slots and memory last; queue their uploads,
-// refits and sun planes on the stream.  Called with the lock NOT held.
+// refits, sun planes and sun-ray grids on the admission stream.  Called with the lock NOT held.
 int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
     NvtxRange nvtx("csp server admit");
     {
@@ -393,55 +516,30 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
         }
     }
     if (admitted.empty()) return CSP_OK;
-    // layout inside each block; host builds into pinned staging
+    // layout inside each block; the host part of each block is staged (pinned) as it lies in the
+    // block and leaves in one upload
     size_t stage = 0;
-    std::vector<size_t> stage_off(admitted.size());
+    std::vector<size_t> stage_off(admitted.size()), upload(admitted.size());
     for (size_t i = 0; i < admitted.size(); ++i) {
         SRequest& r = *admitted[i];
-        const SScene& s = *r.sc;
-        const size_t n = s.elements.size();
-        size_t o = r.off;
-        r.o_sun = o;
-        o += align256(sizeof(SunFrame));
-        r.o_grid = o;
-        o += align256(sizeof(GridDesc));
-        r.o_counts = o;
-        o += align256((size_t)nx * ny * sizeof(uint32_t));
-        r.o_stats = o;
-        o += align256(4 * sizeof(unsigned long long));
-        if (r.group != kAccelFlat) {
-            r.o_sgrid = o;
-            o += align256(sungrid_bytes((uint32_t)n));
-        }
+        const BlockLayout L = block_layout(r, nx, ny);
+        r.o_grid = r.off + L.grid;
+        r.o_counts = r.off + L.counts;
+        r.o_stats = r.off + L.stats;
+        r.o_prims = r.off + L.prims;
+        r.o_optics = r.off + L.optics;
+        r.o_aabbs = r.off + L.aabbs;
+        r.o_prune = r.off + L.prune;
+        r.o_cells = r.off + L.cells;
+        r.o_items = r.off + L.items;
+        r.o_global = r.off + L.global;
+        r.o_sun = r.off + L.sun;
+        r.o_nodes = r.off + L.nodes;
+        r.o_sgrid = r.off + L.sgrid;
         r.own_records = !r.poses.empty();
-        if (r.own_records) {
-            r.o_prims = o;
-            o += align256(n * sizeof(Prim));
-            r.o_optics = o;
-            o += align256(n * sizeof(Optics));
-            r.o_aabbs = o;
-            o += align256(n * sizeof(Aabb));
-            r.o_prune = o;
-            o += align256(n * sizeof(Aabb));
-            if (r.group != kAccelGrid) {
-                r.o_nodes = o;
-                o += align256(s.base.nodes.size() * sizeof(Node));
-            } else {
-                r.o_cells = o;
-                o += align256(r.grid.cell_start.size() * sizeof(uint32_t));
-                r.o_items = o;
-                o += align256(r.grid.items.size() * sizeof(Aabb));
-                r.o_global = o;
-                o += align256(std::max<size_t>(1, r.grid.global.size()) * sizeof(Aabb));
-            }
-        }
         stage_off[i] = stage;
-        if (r.own_records) {
-            stage += n * (sizeof(Prim) + sizeof(Optics) + 2 * sizeof(Aabb));
-            if (r.group == kAccelGrid)
-                stage += r.grid.cell_start.size() * sizeof(uint32_t) + (r.grid.items.size() + r.grid.global.size()) * sizeof(Aabb);
-        }
-        stage = align256(stage + sizeof(GridDesc));
+        upload[i] = L.upload;
+        stage += align256(L.upload);
     }
     const size_t refit_at = stage;
     stage += align256(admitted.size() * sizeof(RefitJob));
@@ -477,21 +575,18 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
         SRequest& r = *admitted[i];
         const SScene& s = *r.sc;
         const uint32_t n = (uint32_t)s.elements.size();
+        // the block's host part as it lies on the device (offsets relative to the block)
         unsigned char* h = h_adm + stage_off[i];
+        auto at = [&](size_t o) { return h + (o - r.off); };
+        std::memset(at(r.o_counts), 0, (size_t)nx * ny * sizeof(uint32_t));
+        std::memset(at(r.o_stats), 0, 4 * sizeof(unsigned long long));
         const Aabb* d_aabbs = s.d_aabbs;
         if (r.own_records) {
             const HostScene& hs = r.hs;
-            const size_t bp = n * sizeof(Prim), bo = n * sizeof(Optics), ba = n * sizeof(Aabb);
-            std::memcpy(h, hs.prims.data(), bp);
-            std::memcpy(h + bp, hs.optics.data(), bo);
-            std::memcpy(h + bp + bo, hs.aabbs.data(), ba);
-            std::memcpy(h + bp + bo + ba, hs.prune.data(), ba);
-            int rc2 = cuda_status(cudaMemcpyAsync(d_arena + r.o_prims, h, bp, cudaMemcpyHostToDevice, stream), "upload");
-            if (!rc2) rc2 = cuda_status(cudaMemcpyAsync(d_arena + r.o_optics, h + bp, bo, cudaMemcpyHostToDevice, stream), "upload");
-            if (!rc2) rc2 = cuda_status(cudaMemcpyAsync(d_arena + r.o_aabbs, h + bp + bo, ba, cudaMemcpyHostToDevice, stream), "upload");
-            if (!rc2) rc2 = cuda_status(cudaMemcpyAsync(d_arena + r.o_prune, h + bp + bo + ba, ba, cudaMemcpyHostToDevice, stream), "upload");
-            if (rc2) return rc2;
-            h += bp + bo + 2 * ba;
+            std::memcpy(at(r.o_prims), hs.prims.data(), n * sizeof(Prim));
+            std::memcpy(at(r.o_optics), hs.optics.data(), n * sizeof(Optics));
+            std::memcpy(at(r.o_aabbs), hs.aabbs.data(), n * sizeof(Aabb));
+            std::memcpy(at(r.o_prune), hs.prune.data(), n * sizeof(Aabb));
             d_aabbs = reinterpret_cast<const Aabb*>(d_arena + r.o_aabbs);
             if (r.group != kAccelGrid) {
                 RefitJob& j = refits[n_refit++];
@@ -508,29 +603,20 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
             GridDesc g;
             if (r.own_records) {
                 const HostGrid& hg = r.grid;
-                const size_t bc = hg.cell_start.size() * sizeof(uint32_t), bi = hg.items.size() * sizeof(Aabb),
-                             bg = hg.global.size() * sizeof(Aabb);
-                std::memcpy(h, hg.cell_start.data(), bc);
-                std::memcpy(h + bc, hg.items.data(), bi);
-                if (bg) std::memcpy(h + bc + bi, hg.global.data(), bg);
-                int rc2 = cuda_status(cudaMemcpyAsync(d_arena + r.o_cells, h, bc, cudaMemcpyHostToDevice, stream), "upload");
-                if (!rc2 && bi)
-                    rc2 = cuda_status(cudaMemcpyAsync(d_arena + r.o_items, h + bc, bi, cudaMemcpyHostToDevice, stream), "upload");
-                if (!rc2 && bg)
-                    rc2 = cuda_status(cudaMemcpyAsync(d_arena + r.o_global, h + bc + bi, bg, cudaMemcpyHostToDevice, stream),
-                                      "upload");
-                if (rc2) return rc2;
-                h += bc + bi + bg;
+                std::memcpy(at(r.o_cells), hg.cell_start.data(), hg.cell_start.size() * sizeof(uint32_t));
+                if (!hg.items.empty()) std::memcpy(at(r.o_items), hg.items.data(), hg.items.size() * sizeof(Aabb));
+                if (!hg.global.empty()) std::memcpy(at(r.o_global), hg.global.data(), hg.global.size() * sizeof(Aabb));
                 g = grid_desc(hg, reinterpret_cast<const uint32_t*>(d_arena + r.o_cells),
                               reinterpret_cast<const Aabb*>(d_arena + r.o_items),
                               reinterpret_cast<const Aabb*>(d_arena + r.o_global));
             } else {
                 g = grid_desc(s.grid, s.d_cells, s.d_items, s.d_global);
             }
-            std::memcpy(h, &g, sizeof g);
-            int rc2 = cuda_status(cudaMemcpyAsync(d_arena + r.o_grid, h, sizeof g, cudaMemcpyHostToDevice, stream), "upload");
-            if (rc2) return rc2;
+            std::memcpy(at(r.o_grid), &g, sizeof g);
         }
+        const int rc2 = cuda_status(
+            cudaMemcpyAsync(d_arena + r.off, h, upload[i], cudaMemcpyHostToDevice, adm_stream), "upload request");
+        if (rc2) return rc2;
         float sv[3];
         sun_vector_f(r.sun, sv);
         SunJob& sj = suns[n_sun++];
@@ -550,27 +636,24 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
             gj.aabbs = d_aabbs;
             max_sg_n = std::max(max_sg_n, (int)n);
         }
-        int rc2 = cuda_status(cudaMemsetAsync(d_arena + r.o_counts, 0, (size_t)nx * ny * sizeof(uint32_t), stream), "memset");
-        if (!rc2) rc2 = cuda_status(cudaMemsetAsync(d_arena + r.o_stats, 0, 4 * sizeof(unsigned long long), stream), "memset");
-        if (rc2) return rc2;
         r.t_admit = Clock::now();
     }
     if (n_sun == 0) return CSP_OK;
     // job tables: an arena block released once the stream has passed the kernels that read them
     const size_t job_bytes = stage - refit_at;
     if (job_bytes > jobs_cap) return set_error(CSP_ERR_STATE, "admission job tables exceed their buffer");
-    int rc = cuda_status(cudaMemcpyAsync(d_jobs, h_adm + refit_at, job_bytes, cudaMemcpyHostToDevice, stream),
+    int rc = cuda_status(cudaMemcpyAsync(d_jobs, h_adm + refit_at, job_bytes, cudaMemcpyHostToDevice, adm_stream),
                          "upload admission jobs");
     if (!rc && n_refit)
-        rc = cuda_status(launch_refit(reinterpret_cast<const RefitJob*>(d_jobs), n_refit, max_nodes, stream),
+        rc = cuda_status(launch_refit(reinterpret_cast<const RefitJob*>(d_jobs), n_refit, max_nodes, adm_stream),
                          "refit_kernel");
     if (!rc)
         rc = cuda_status(
-            launch_prepare_sun_batch(reinterpret_cast<const SunJob*>(d_jobs + (sun_at - refit_at)), n_sun, stream),
+            launch_prepare_sun_batch(reinterpret_cast<const SunJob*>(d_jobs + (sun_at - refit_at)), n_sun, adm_stream),
             "prepare_sun_batch_kernel");
     if (!rc && n_sg)
         rc = cuda_status(launch_sungrid_build(reinterpret_cast<const SunGridJob*>(d_jobs + (sg_at - refit_at)), n_sg,
-                                              max_sg_n, stream),
+                                              max_sg_n, adm_stream),
                          "sun grid build");
     return rc;
 }
@@ -700,9 +783,14 @@ void Server::run_worker() {
         std::string err;
         // 1. launch the step over the requests already active
         int rc = step_launch(finishing, rays);
-        // 2. admit while it runs
+        // 2. admit while it runs (admission stream); the step stream waits for it, so the
+        //    synchronisation below covers both and the next step sees the admitted requests set up
         admitted.clear();
         if (!rc) rc = admit(admitted, err);
+        if (!rc && !admitted.empty()) {
+            rc = cuda_status(cudaEventRecord(adm_done, adm_stream), "cudaEventRecord");
+            if (!rc) rc = cuda_status(cudaStreamWaitEvent(stream, adm_done, 0), "cudaStreamWaitEvent");
+        }
         if (!rc && finishing.empty() && active.empty() && admitted.empty()) {
             // nothing fits yet (memory) and nothing runs: cannot happen, a request never exceeds
             // the budget; guard against a spin anyway

@@ -1,6 +1,8 @@
 """Host-side auxiliaries that need no GPU: the autotuner's persistent cache file and the switches
-of the allocation-failure injection and the bounds-check status."""
+of the allocation-failure injection and the bounds-check status, and the element records built in
+ranges on several threads."""
 import json
+import os
 
 import pytest
 
@@ -52,3 +54,25 @@ def test_bounds_check_status_in_a_normal_build(native_lib):
     with pytest.raises(native.CspError) as e:
         native.bounds_check_status(0)
     assert e.value.status == -6
+
+
+def test_element_records_built_in_ranges_equal_serial(tmp_path):
+    """The server builds the element records of large submissions in ranges on its host threads:
+    the same records and the same error as the serial build (a host program compiled from the scene
+    builder's source)."""
+    import shutil
+    import subprocess
+    from optixsoltracedemos_gb300 import scenes
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    csrc = os.path.join(root, "optixsoltracedemos_gb300", "csrc")
+    cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    exe = str(tmp_path / "scene_build_ranges")
+    cmd = [shutil.which("g++") or "g++", "-std=c++17", "-O2", "-ffp-contract=off", "-pthread", "-I", csrc, "-I",
+           os.path.join(root, "include"), "-I", cuda_inc, os.path.join(root, "tests", "cpp", "scene_build_ranges.cpp"),
+           os.path.join(csrc, "csp_scene.cpp"), "-o", exe]
+    subprocess.run(cmd, check=True)
+    field = str(tmp_path / "field.bin")
+    scenes.large_field(n_heliostats=10000, num_rays=1).elements.tofile(field)
+    r = subprocess.run([exe, field], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("OK 10001 elements, error 'element 1031:"), r.stdout
