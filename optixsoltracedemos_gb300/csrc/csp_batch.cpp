@@ -14,13 +14,15 @@
 // result buffers, graph, events): run_async builds the next run on the host while the previous one
 // executes, wait completes the oldest run in flight.
 //
-// Arena layout (one cudaMalloc, offsets 16-byte aligned):
+// Device layout (offsets 16-byte aligned):
 //   upload  [per instance: prims | optics | aabbs | prune (| own field grid)] [descs per group]
 //           [tile_begin per group] [refit jobs] [sun jobs] [sun grid jobs]
 //   nodes   per-instance refitted BVH nodes and sun grid (written on the device)
 //   zeroed  [work counters (2)] [stats, 4 x u64 per instance] [counts, nx*ny x u32 per instance]
 //   suns    per-instance SunFrame
-// The download region is [stats .. suns end), one copy.
+// The upload region is one copy into the run slot's own device buffer, on the copy stream, so that
+// it overlaps the kernels of the run before; the rest is one buffer shared by the runs, whose
+// kernels are ordered on the compute stream.  The download region is [stats .. suns end), one copy.
 #include "csp_batch.h"
 
 #include <algorithm>
@@ -169,8 +171,13 @@ void Batch::release() {
         if (S.ev0) cudaEventDestroy(S.ev0);
         if (S.ev1) cudaEventDestroy(S.ev1);
         if (S.done) cudaEventDestroy(S.done);
-        S.ev0 = S.ev1 = S.done = nullptr;
+        if (S.up_done) cudaEventDestroy(S.up_done);
+        S.ev0 = S.ev1 = S.done = S.up_done = nullptr;
+        cudaFree(S.d_up);
+        S.d_up = nullptr;
+        S.up_cap = 0;
     }
+    d_up = nullptr;
     h_stage = nullptr;
     for (BScene& s : scenes) {
         cudaFree(s.d_topo);
@@ -181,14 +188,15 @@ void Batch::release() {
         s.d_cells = nullptr;
         s.d_items = s.d_global = nullptr;
     }
-    cudaFree(d_arena);
-    d_arena = nullptr;
-    arena_cap = 0;
+    cudaFree(d_comp);
+    d_comp = nullptr;
+    comp_cap = 0;
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (stream) cudaStreamDestroy(stream);
+    if (copy_stream) cudaStreamDestroy(copy_stream);
     ev0 = ev1 = nullptr;
-    stream = nullptr;
+    stream = copy_stream = nullptr;
 }
 
 int Batch::ensure_stream() {
@@ -203,12 +211,16 @@ int Batch::ensure_stream() {
         if (c == '"' || c == '\\') c = '_';
     h3t12 = halton3_table();
     if ((rc = cuda_status(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate"))) return rc;
+    if ((rc = cuda_status(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "cudaStreamCreate")))
+        return rc;
     if ((rc = cuda_status(cudaEventCreate(&ev0), "cudaEventCreate"))) return rc;
     if ((rc = cuda_status(cudaEventCreate(&ev1), "cudaEventCreate"))) return rc;
     for (RunSlot& S : slot) {
         if ((rc = cuda_status(cudaEventCreate(&S.ev0), "cudaEventCreate"))) return rc;
         if ((rc = cuda_status(cudaEventCreate(&S.ev1), "cudaEventCreate"))) return rc;
         if ((rc = cuda_status(cudaEventCreateWithFlags(&S.done, cudaEventDisableTiming), "cudaEventCreate"))) return rc;
+        if ((rc = cuda_status(cudaEventCreateWithFlags(&S.up_done, cudaEventDisableTiming), "cudaEventCreate")))
+            return rc;
     }
     return CSP_OK;
 }
@@ -351,26 +363,41 @@ int Batch::layout(int si) {
         off += align16(sizeof(SunFrame));
     }
     res_bytes = off - res_off;
-    const size_t total = std::max<size_t>(off, 16);
+    const size_t comp = std::max<size_t>(off - up_bytes, 16);
 
     int rc;
     RunSlot& S = slot[si];
-    if (total > arena_cap) {
-        // the runs in flight read the arena: let them finish (their results stay in their slots)
+    if (comp > comp_cap) {
+        // the runs in flight use the shared region: let them finish (their results stay in their slots)
         if (!flight.empty() && (rc = cuda_status(cudaStreamSynchronize(stream), "batch run"))) return rc;
         for (RunSlot& o : slot) {
             if (o.graph) cudaGraphExecDestroy(o.graph);
             o.graph = nullptr;
         }
-        cudaFree(d_arena);
-        d_arena = nullptr;
-        arena_cap = 0;
+        cudaFree(d_comp);
+        d_comp = nullptr;
+        comp_cap = 0;
         size_t free_b = 0, total_b = 0;
         cudaMemGetInfo(&free_b, &total_b);
-        if (total > free_b) return set_error(CSP_ERR_OUT_OF_MEMORY, "batch does not fit in free device memory");
-        if ((rc = cuda_status(dev_alloc((void**)&d_arena, total), "cudaMalloc batch arena"))) return rc;
-        arena_cap = total;
+        if (comp > free_b) return set_error(CSP_ERR_OUT_OF_MEMORY, "batch does not fit in free device memory");
+        if ((rc = cuda_status(dev_alloc((void**)&d_comp, comp), "cudaMalloc batch arena"))) return rc;
+        comp_cap = comp;
     }
+    if (up_bytes > S.up_cap) {
+        // the slot is not in flight: nothing reads its upload region
+        if (S.graph) cudaGraphExecDestroy(S.graph);
+        S.graph = nullptr;
+        cudaFree(S.d_up);
+        S.d_up = nullptr;
+        S.up_cap = 0;
+        size_t free_b = 0, total_b = 0;
+        cudaMemGetInfo(&free_b, &total_b);
+        if (up_bytes > free_b) return set_error(CSP_ERR_OUT_OF_MEMORY, "batch does not fit in free device memory");
+        if ((rc = cuda_status(dev_alloc((void**)&S.d_up, std::max<size_t>(up_bytes, 16)), "cudaMalloc batch upload")))
+            return rc;
+        S.up_cap = up_bytes;
+    }
+    d_up = S.d_up;
     // the slot is not in flight; if it holds the current results, this run replaces them
     if (up_bytes > S.stage_cap || res_bytes > S.result_cap) {
         if (S.graph) cudaGraphExecDestroy(S.graph);
@@ -437,9 +464,9 @@ void Batch::fill_instance(size_t i) {
     }
     RefitJob rj;
     rj.topo = s.d_topo;
-    rj.aabbs = reinterpret_cast<const Aabb*>(d_arena + p.aabbs);
-    rj.prune = reinterpret_cast<const Aabb*>(d_arena + p.prune);
-    rj.out = reinterpret_cast<Node*>(d_arena + p.nodes);
+    rj.aabbs = reinterpret_cast<const Aabb*>(dev(p.aabbs));
+    rj.prune = reinterpret_cast<const Aabb*>(dev(p.prune));
+    rj.out = reinterpret_cast<Node*>(dev(p.nodes));
     rj.n_nodes = (int)s.base.nodes.size();
     rj.pad = 0;
     std::memcpy(h_stage + refit_off + i * sizeof(RefitJob), &rj, sizeof rj);
@@ -454,11 +481,11 @@ void Batch::fill_instance(size_t i) {
     sj.tan_pad = tanf((float)sun_pad_angle(b.shape, b.param));
     sj.shape = b.shape;
     sj.param = (float)b.param;
-    sj.out = reinterpret_cast<SunFrame*>(d_arena + p.sun);
+    sj.out = reinterpret_cast<SunFrame*>(dev(p.sun));
     std::memcpy(h_stage + sunjob_off + i * sizeof(SunJob), &sj, sizeof sj);
     if (p.sg_slot >= 0) {
         SunGridJob gj;
-        sungrid_place(d_arena + p.sgrid, ne, gj);
+        sungrid_place(dev(p.sgrid), ne, gj);
         gj.sun = sj.out;
         gj.aabbs = rj.aabbs;
         std::memcpy(h_stage + sgjob_off + (size_t)p.sg_slot * sizeof(SunGridJob), &gj, sizeof gj);
@@ -482,10 +509,10 @@ void Batch::fill_descs(const int* block, const std::vector<bool>* sample, std::v
         uint64_t rays = b.rays;
         if (sample && !(*sample)[i]) rays = 0;
         InstanceDesc& d = out_desc[g][p.slot];
-        d.args.nodes = reinterpret_cast<const Node*>(d_arena + p.nodes);
-        d.args.prims = reinterpret_cast<const Prim*>(d_arena + p.prims);
-        d.args.optics = reinterpret_cast<const Optics*>(d_arena + p.optics);
-        d.args.sun = reinterpret_cast<const SunFrame*>(d_arena + p.sun);
+        d.args.nodes = reinterpret_cast<const Node*>(dev(p.nodes));
+        d.args.prims = reinterpret_cast<const Prim*>(dev(p.prims));
+        d.args.optics = reinterpret_cast<const Optics*>(dev(p.optics));
+        d.args.sun = reinterpret_cast<const SunFrame*>(dev(p.sun));
         d.args.hits = nullptr;
         d.args.ids = nullptr;
         d.args.ray_begin = 0;
@@ -498,22 +525,22 @@ void Batch::fill_descs(const int* block, const std::vector<bool>* sample, std::v
         d.args.sgrid = nullptr;
         if (p.sg_slot >= 0) {
             SunGridJob gj;
-            sungrid_place(d_arena + p.sgrid, count_of(i), gj);
+            sungrid_place(dev(p.sgrid), count_of(i), gj);
             d.args.sgrid = gj.desc;
         }
         if (g == kAccelGrid) {
             const bool own = !b.poses.empty();
             const BScene& bs = scenes[b.scene];
-            d.grid = grid_desc(grid_of(i), own ? reinterpret_cast<const uint32_t*>(d_arena + p.cells) : bs.d_cells,
-                               own ? reinterpret_cast<const Aabb*>(d_arena + p.items) : bs.d_items,
-                               own ? reinterpret_cast<const Aabb*>(d_arena + p.global) : bs.d_global);
-            d.args.grid = reinterpret_cast<const GridDesc*>(d_arena + desc_off[g] + p.slot * sizeof(InstanceDesc) +
+            d.grid = grid_desc(grid_of(i), own ? reinterpret_cast<const uint32_t*>(dev(p.cells)) : bs.d_cells,
+                               own ? reinterpret_cast<const Aabb*>(dev(p.items)) : bs.d_items,
+                               own ? reinterpret_cast<const Aabb*>(dev(p.global)) : bs.d_global);
+            d.args.grid = reinterpret_cast<const GridDesc*>(dev(desc_off[g] + p.slot * sizeof(InstanceDesc)) +
                                                             offsetof(InstanceDesc, grid));
         }
         flux_target(elements_of(i)[count_of(i) - 1], nx, ny, d.flux);
         d.flux.staged = (out_flags & CSP_OUT_STAGED) ? 1 : 0;
-        d.flux.counts = reinterpret_cast<uint32_t*>(d_arena + p.counts);
-        d.flux.stats = reinterpret_cast<unsigned long long*>(d_arena + p.stats);
+        d.flux.counts = reinterpret_cast<uint32_t*>(dev(p.counts));
+        d.flux.stats = reinterpret_cast<unsigned long long*>(dev(p.stats));
         d.tile_begin = tiles[g];
         d.n_prims = (int)count_of(i);
         out_tb[g][p.slot] = tiles[g];
@@ -531,35 +558,35 @@ void Batch::write_descs(const std::vector<InstanceDesc>* desc, const std::vector
 
 BatchLaunch Batch::launch_of(int g, uint64_t total_tiles, int chunk) const {
     BatchLaunch L;
-    L.inst = reinterpret_cast<const InstanceDesc*>(d_arena + desc_off[g]);
-    L.tile_begin = reinterpret_cast<const uint64_t*>(d_arena + tb_off[g]);
+    L.inst = reinterpret_cast<const InstanceDesc*>(dev(desc_off[g]));
+    L.tile_begin = reinterpret_cast<const uint64_t*>(dev(tb_off[g]));
     L.n_inst = n_group[g];
     L.chunk = chunk;
     L.total_tiles = total_tiles;
-    L.next_tile = reinterpret_cast<unsigned long long*>(d_arena + counter_off) + g;
+    L.next_tile = reinterpret_cast<unsigned long long*>(dev(counter_off)) + g;
     return L;
 }
 
 // Device work of a run up to (not including) the trace launches.
-int Batch::enqueue_prefix(cudaStream_t st) {
-    int rc;
-    if ((rc = cuda_status(cudaMemcpyAsync(d_arena, h_stage, up_bytes, cudaMemcpyHostToDevice, st), "upload batch")))
-        return rc;
-    if ((rc = cuda_status(cudaMemsetAsync(d_arena + zero_off, 0, zero_bytes, st), "zero flux maps"))) return rc;
-    return CSP_OK;
+int Batch::enqueue_upload(cudaStream_t st) {
+    return cuda_status(cudaMemcpyAsync(d_up, h_stage, up_bytes, cudaMemcpyHostToDevice, st), "upload batch");
+}
+
+int Batch::enqueue_zero(cudaStream_t st) {
+    return cuda_status(cudaMemsetAsync(dev(zero_off), 0, zero_bytes, st), "zero flux maps");
 }
 
 int Batch::enqueue_scene_setup(cudaStream_t st) {
     int rc;
-    if ((rc = cuda_status(launch_refit(reinterpret_cast<const RefitJob*>(d_arena + refit_off), (int)inst.size(),
+    if ((rc = cuda_status(launch_refit(reinterpret_cast<const RefitJob*>(dev(refit_off)), (int)inst.size(),
                                        max_nodes, st),
                           "refit_kernel")))
         return rc;
-    if ((rc = cuda_status(launch_prepare_sun_batch(reinterpret_cast<const SunJob*>(d_arena + sunjob_off),
+    if ((rc = cuda_status(launch_prepare_sun_batch(reinterpret_cast<const SunJob*>(dev(sunjob_off)),
                                                    (int)inst.size(), st),
                           "prepare_sun_batch_kernel")))
         return rc;
-    return cuda_status(launch_sungrid_build(reinterpret_cast<const SunGridJob*>(d_arena + sgjob_off), n_sg, max_sg_n, st),
+    return cuda_status(launch_sungrid_build(reinterpret_cast<const SunGridJob*>(dev(sgjob_off)), n_sg, max_sg_n, st),
                        "sun grid build");
 }
 
@@ -614,13 +641,13 @@ int Batch::autotune(int g, BatchTuning& best) {
         // descs and tile tables only: the element records already on the device stay
         const size_t lo = desc_off[0], hi = refit_off;
         write_descs(desc, tb, img.data());
-        if ((rc = cuda_status(cudaMemcpyAsync(d_arena + lo, img.data() + lo, hi - lo, cudaMemcpyHostToDevice, stream),
+        if ((rc = cuda_status(cudaMemcpyAsync(dev(lo), img.data() + lo, hi - lo, cudaMemcpyHostToDevice, stream),
                               "upload sample descs")))
             break;
         const BatchLaunch L = launch_of(g, tb[g][n_group[g]], t.chunk);
         float ms_best = 1e30f;
         for (int rep = 0; rep < 2 && rc == CSP_OK; ++rep) {
-            rc = cuda_status(cudaMemsetAsync(d_arena + counter_off, 0, kBatchGroups * sizeof(unsigned long long), stream),
+            rc = cuda_status(cudaMemsetAsync(dev(counter_off), 0, kBatchGroups * sizeof(unsigned long long), stream),
                              "zero counters");
             if (!rc) rc = cuda_status(cudaEventRecord(ev0, stream), "cudaEventRecord");
             if (!rc) rc = cuda_status(launch_trace_batch(L, g, t, stream), "batch_kernel");
@@ -670,7 +697,8 @@ int Batch::resolve_tuning() {
         }
         int rc;
         if (need_setup) {
-            if ((rc = enqueue_prefix(stream)) || (rc = enqueue_scene_setup(stream))) return rc;
+            if ((rc = enqueue_upload(stream)) || (rc = enqueue_zero(stream)) || (rc = enqueue_scene_setup(stream)))
+                return rc;
             need_setup = false;
         }
         BatchTuning best{128, 0, 4};
@@ -746,7 +774,7 @@ int Batch::run_async() {
     for (int g = 0; g < kBatchGroups; ++g) tiles[g] = tb[g][n_group[g]];
 
     // graph signature: everything the captured launches depend on besides the staged contents
-    std::vector<uint64_t> sig = {(uint64_t)(uintptr_t)d_arena, (uint64_t)(uintptr_t)S.h_stage,
+    std::vector<uint64_t> sig = {(uint64_t)(uintptr_t)d_comp, (uint64_t)(uintptr_t)S.d_up, (uint64_t)(uintptr_t)S.h_stage,
                                  (uint64_t)(uintptr_t)S.h_result, up_bytes, zero_bytes, res_bytes, n, nx, ny,
                                  desc_off[0], zero_off, res_off};
     for (int g = 0; g < kBatchGroups; ++g) {
@@ -762,7 +790,7 @@ int Batch::run_async() {
         cudaGraph_t g = nullptr;
         if ((rc = cuda_status(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture")))
             return rc;
-        int crc = enqueue_prefix(stream);
+        int crc = enqueue_zero(stream);
         if (!crc) crc = cuda_status(cudaEventRecordWithFlags(S.ev0, stream, cudaEventRecordExternal), "event");
         if (!crc) crc = enqueue_scene_setup(stream);
         for (int gi = 0; gi < kBatchGroups && !crc; ++gi)
@@ -772,7 +800,7 @@ int Batch::run_async() {
         if (!crc) crc = cuda_status(cudaEventRecordWithFlags(S.ev1, stream, cudaEventRecordExternal), "event");
         if (!crc)
             crc = cuda_status(
-                cudaMemcpyAsync(S.h_result, d_arena + res_off, res_bytes, cudaMemcpyDeviceToHost, stream), "download");
+                cudaMemcpyAsync(S.h_result, dev(res_off), res_bytes, cudaMemcpyDeviceToHost, stream), "download");
         const int erc = cuda_status(cudaStreamEndCapture(stream, &g), "end capture");
         if (crc || erc) {
             if (g) cudaGraphDestroy(g);
@@ -797,6 +825,11 @@ int Batch::run_async() {
     S.time_setup = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     S.up_bytes = up_bytes;
     S.res_bytes = res_bytes;
+    // the upload on the copy stream (behind nothing but the uploads before it), the graph behind it
+    // and behind the run before on the compute stream
+    if ((rc = enqueue_upload(copy_stream))) return rc;
+    if ((rc = cuda_status(cudaEventRecord(S.up_done, copy_stream), "cudaEventRecord"))) return rc;
+    if ((rc = cuda_status(cudaStreamWaitEvent(stream, S.up_done, 0), "cudaStreamWaitEvent"))) return rc;
     if ((rc = cuda_status(cudaGraphLaunch(S.graph, stream), "cudaGraphLaunch"))) return rc;
     if ((rc = cuda_status(cudaEventRecord(S.done, stream), "cudaEventRecord"))) return rc;
     flight.push_back(si);

@@ -57,6 +57,9 @@ struct Place {
 struct RunSlot {
     unsigned char* h_stage = nullptr;  // pinned image of the upload region
     size_t stage_cap = 0;
+    unsigned char* d_up = nullptr;  // the slot's upload region on the device (see Batch::dev)
+    size_t up_cap = 0;
+    cudaEvent_t up_done = nullptr;  // the upload of the slot's run, on the copy stream
     unsigned char* h_result = nullptr;  // pinned copy of the download region
     size_t result_cap = 0;
     cudaGraphExec_t graph = nullptr;
@@ -75,6 +78,8 @@ struct Batch {
     int device = -1;
     std::string device_model;  // "name ccM.m smN": the autotuner cache key's device part
     cudaStream_t stream = nullptr;
+    // uploads of pipelined runs: run k + 1's upload overlaps run k's kernels on `stream`
+    cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // autotuner timing
     const float* h3t12 = nullptr;  // Halton table of the device
     uint32_t nx = 100, ny = 100;
@@ -84,8 +89,12 @@ struct Batch {
     BatchTuning user{0, 0, 0};  // block 0: autotune
     BatchTuning used[kBatchGroups] = {{128, 0, 4}, {128, 0, 4}, {128, 0, 4}};
 
-    unsigned char* d_arena = nullptr;
-    size_t arena_cap = 0;
+    // device memory: the upload region [0, up_bytes) of the layout lives in the run slot's d_up (two
+    // runs in flight upload into different memory), the rest, which the device writes, in d_comp
+    // (shared: the kernels of runs are ordered on `stream`)
+    unsigned char* d_comp = nullptr;
+    size_t comp_cap = 0;
+    unsigned char* d_up = nullptr;  // upload region of the run being built (its slot's)
     RunSlot slot[2];
     std::deque<int> flight;            // slots of the runs in flight, oldest first
     int cur = -1;                      // slot of the last completed run (its results), -1: none
@@ -119,7 +128,10 @@ struct Batch {
                     std::vector<uint64_t>* tb);
     void write_descs(const std::vector<InstanceDesc>* desc, const std::vector<uint64_t>* tb, unsigned char* img);
     BatchLaunch launch_of(int g, uint64_t total_tiles, int chunk) const;
-    int enqueue_prefix(cudaStream_t st);
+    // device address of layout offset `off`
+    unsigned char* dev(size_t off) const { return off < up_bytes ? d_up + off : d_comp + (off - up_bytes); }
+    int enqueue_upload(cudaStream_t st);
+    int enqueue_zero(cudaStream_t st);
     int enqueue_scene_setup(cudaStream_t st);
     int autotune(int g, BatchTuning& best);
     int resolve_tuning();
