@@ -75,7 +75,7 @@ struct SunGridJob {
     uint32_t* cursor;
     float4* rect;             // [n]
     float4* item_rect;        // [cap_items]
-    uint32_t* item_id;        // [cap_items]
+    Aabb* item_box;           // [cap_items]
     uint32_t* global_id;      // [n]
 };
 

@@ -669,7 +669,7 @@ __device__ __forceinline__ int sun_closest(const SunGrid& G, const Prim* __restr
     if (!CSP_BOUNDS(5, j <= e && e <= __ldg(G.cell_start + G.nu * G.nv))) return best;
     for (; j < e; ++j) {
         if (!in_rect(__ldg(G.item_rect + j), u, v)) continue;
-        const float4* q = reinterpret_cast<const float4*>(G.aabbs + __ldg(G.item_id + j));
+        const float4* q = reinterpret_cast<const float4*>(G.item_box + j);
         test_box(__ldg(q), __ldg(q + 1), prims, o, d, inv, kTminSun, acc, best, best_t, best_type, prune);
     }
     for (int k = 0; k < G.n_global; ++k) {

@@ -98,18 +98,19 @@ struct alignas(16) GridDesc {
 // Halton coordinates (u, v) of the sun plane, outside which no sun ray can meet its AABB (rect[e],
 // see reach_rect in csp_trace.cuh).  [0, 1]^2 is cut into nu x nv cells; cell (iu, iv) lists
 // (items[cell_start[iv nu + iu] .. cell_start[iv nu + iu + 1])) every element whose rectangle overlaps
-// it, with the rectangle inline (item_rect) and the element index (item_id).  Elements whose
+// it, with the rectangle (item_rect) and the element's exact box (item_box, lo.w = element | type
+// << kTypeShift) inline, so that a candidate's box test does not wait for an index.  Elements whose
 // rectangle covers more than kSunGridMaxCells cells are in the global list instead, tested by every
 // ray.  A sun ray at (u, v) can only meet the elements of its cell and the global list whose
 // rectangles hold (u, v); a ray that lies in none meets no element box at all.
 constexpr int kSunGridMaxCells = 64;     // cells of one element's rectangle before it goes global
-constexpr int kSunGridItemsPerElem = 8;  // item capacity per element (the sizing keeps the total below)
+constexpr int kSunGridItemsPerElem = 12;  // item capacity per element (the sizing keeps the total below)
 struct alignas(16) SunGrid {
     int nu, nv, n_global, n;
     float fnu, fnv, pad0, pad1;
     const uint32_t* cell_start;  // [nu nv + 1]
     const float4* item_rect;
-    const uint32_t* item_id;
+    const Aabb* item_box;
     const uint32_t* global_id;   // [n_global]
     const float4* rect;          // [n], every element's reach rectangle
     const Aabb* aabbs;           // exact element boxes, lo.w = element | type << kTypeShift (bits)
