@@ -68,11 +68,11 @@ NCU_TRAFFIC_PER_LAUNCH = 4 * (8776704 + 291551232)
 NCU_TRAFFIC_PER_LAUNCH_FIELD = 64 * (9310208 + 297519360)
 # Batch kernel (field grid) on the batched workload: warp instructions and DRAM bytes per traced ray,
 # from `ncu --set full -k regex:^batch_kernel -s 2 -c 1` of `python bench.py --workload batched
-# --instances 8 --tuning 256,4,16 --steps 1 --warmup 3 --no-systems --no-cpu-baseline
-# --plain-instances 1` (one launch over 42,028,566 rays): smsp__inst_executed.sum = 3,451,210,565
-# and dram__bytes_read.sum + dram__bytes_write.sum = 25,467,136 + 33,280 bytes, per ray.
-BATCH_WARP_INST_PER_RAY = 3451210565 / 42028566
-BATCH_DRAM_BYTES_PER_RAY = (25467136 + 33280) / 42028566
+# --instances 8 --tuning 256,4,256 --steps 1 --warmup 3 --no-systems --no-cpu-baseline
+# --plain-instances 1` (one launch over 42,028,566 rays): smsp__inst_executed.sum = 3,229,355,334
+# and dram__bytes_read.sum + dram__bytes_write.sum = 52,126,464 + 1,675,776 bytes, per ray.
+BATCH_WARP_INST_PER_RAY = 3229355334 / 42028566
+BATCH_DRAM_BYTES_PER_RAY = (52126464 + 1675776) / 42028566
 ISSUE_PER_SM_PER_CYCLE = 4  # one warp instruction per cycle per scheduler, 4 schedulers per SM
 
 
