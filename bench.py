@@ -22,7 +22,8 @@ persistent trace launch, receiver flux maps accumulated in the shading stage.
   cpu_baseline  the oracle port of the reference algorithm on all host cores, on ray samples of
              the batched workload's instances (brute-force closest hit over 10,001 elements).
   plain_loop the same instances through the drop-in handle one scene at a time (new poses,
-             csp_update, csp_run, csp_flux_map): the north star's "plain per-scene launch loop".
+             csp_update, csp_run, csp_flux_map): the plain per-scene launch loop the batched and
+             served modes are measured against.
 
 The default line also carries the plain trace workloads and the served workload as sub-objects:
 `single_parabolic` (one parabolic heliostat, 16M rays, the dense-record HBM roofline),

@@ -234,8 +234,8 @@ struct Server {
     std::deque<SRequest*> pending;
     std::vector<SRequest*> active;
     uint64_t next_id = 1;
-    // refit, sun-plane and sun-grid job tables of one admission round (at most max_active requests); the
-    // kernels that read them finish at the step synchronisation before the next round
+    // refit, sun-plane and sun-grid job tables of one admission pass (at most max_active requests);
+    // the kernels that read them finish at the step synchronisation before the next pass
     unsigned char* d_jobs = nullptr;
     size_t jobs_cap = 0;
 
@@ -548,13 +548,13 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
     const size_t sg_at = stage;
     stage += align256(admitted.size() * sizeof(SunGridJob));
     if (stage > adm_cap) {
-        // the previous round's uploads from h_adm finished at the step synchronisation before this call
+        // the previous pass's uploads from h_adm finished at the step synchronisation before this call
         if (h_adm) cudaFreeHost(h_adm);
         h_adm = nullptr;
         adm_cap = 0;
         int rc = cuda_status(host_alloc((void**)&h_adm, stage), "cudaHostAlloc admission");
         if (rc == CSP_ERR_OUT_OF_MEMORY) {
-            // nothing of this round is queued yet: its requests fail, the server goes on (the
+            // nothing of this pass is queued yet: its requests fail, the server goes on (the
             // worker releases their blocks and slots after the step)
             std::lock_guard<std::mutex> lk(mu);
             for (SRequest* r : admitted) {
