@@ -13,8 +13,9 @@
 //      elements on the server's host threads), refit of the scene's BVH topology in place into the
 //      request's nodes, sun plane, sun-ray candidate grid; all on the admission stream, which the
 //      step stream waits for before step k+1, so the request joins step k+1;
-//   3. wait for the step, complete the finished requests (latency = completion - submission), free
-//      their device memory.
+//   3. wait for step k - 1, complete its finished requests (latency = completion - submission), free
+//      their device memory.  Steps alternate between two streams: step k is launched before step
+//      k - 1 ends, so its CTAs fill the tail of step k - 1.
 // A request's result does not depend on what it was batched with or how its rays were sliced: its
 // rays are traced with the same (seed, instance, ray index) and its flux map is an integer sum.
 //
@@ -216,7 +217,10 @@ struct Arena {
 
 struct Server {
     int device = -1;
-    cudaStream_t stream = nullptr;
+    // steps alternate between two streams, each with its own descriptor tables and work counters:
+    // step k + 1 is launched before step k ends, so its CTAs fill step k's tail
+    cudaStream_t stream[2] = {nullptr, nullptr};
+    cudaEvent_t step_done[2] = {nullptr, nullptr};
     // admissions (uploads, refits, sun planes, sun-ray grids) go to their own stream: the uploads
     // overlap the running step, the kernels fill its tail; the step stream waits on adm_done
     // before the next step
@@ -242,8 +246,8 @@ struct Server {
     unsigned char* d_arena = nullptr;
     Arena arena;
     // per-step device tables and their pinned staging
-    unsigned char* d_step = nullptr;
-    unsigned char* h_step = nullptr;
+    unsigned char* d_step[2] = {nullptr, nullptr};
+    unsigned char* h_step[2] = {nullptr, nullptr};
     size_t step_bytes = 0;
     // admission staging (pinned) and results (pinned, one slot per active request)
     unsigned char* h_adm = nullptr;
@@ -251,7 +255,7 @@ struct Server {
     unsigned char* h_res = nullptr;
     size_t res_slot_bytes = 0;
     std::vector<int> free_res_slots;
-    unsigned long long* d_counter = nullptr;
+    unsigned long long* d_counter[2] = {nullptr, nullptr};
     const float* h3t12 = nullptr;  // Halton table of the device
 
     std::mutex mu;
@@ -277,7 +281,7 @@ struct Server {
     void run_worker();
     size_t request_bytes(const SRequest& r) const;
     int admit(std::vector<SRequest*>& admitted, std::string& err);
-    int step_launch(std::vector<SRequest*>& finishing, uint64_t& rays);
+    int step_launch(int par, bool after_other, std::vector<SRequest*>& finishing, uint64_t& rays);
 };
 
 Server::~Server() { stop(); }
@@ -304,7 +308,8 @@ void Server::stop() {
         cv_done.wait(lk, [&] { return waiting == 0; });
     }
     if (device >= 0) cudaSetDevice(device);
-    if (stream) cudaStreamSynchronize(stream);
+    for (cudaStream_t st : stream)
+        if (st) cudaStreamSynchronize(st);
     if (adm_stream) cudaStreamSynchronize(adm_stream);
     for (auto& s : scenes) {
         cudaFree(s->d_topo);
@@ -318,22 +323,29 @@ void Server::stop() {
     }
     scenes.clear();
     cudaFree(d_arena);
-    cudaFree(d_step);
-    cudaFree(d_counter);
+    for (int p = 0; p < 2; ++p) {
+        cudaFree(d_step[p]);
+        cudaFree(d_counter[p]);
+        if (h_step[p]) cudaFreeHost(h_step[p]);
+        d_step[p] = h_step[p] = nullptr;
+        d_counter[p] = nullptr;
+    }
     cudaFree(d_jobs);
     d_jobs = nullptr;
-    if (h_step) cudaFreeHost(h_step);
     if (h_adm) cudaFreeHost(h_adm);
     if (h_res) cudaFreeHost(h_res);
-    d_arena = d_step = nullptr;
-    d_counter = nullptr;
-    h_step = h_adm = h_res = nullptr;
+    d_arena = nullptr;
+    h_adm = h_res = nullptr;
     if (adm_done) cudaEventDestroy(adm_done);
     adm_done = nullptr;
     if (adm_stream) cudaStreamDestroy(adm_stream);
     adm_stream = nullptr;
-    if (stream) cudaStreamDestroy(stream);
-    stream = nullptr;
+    for (int p = 0; p < 2; ++p) {
+        if (step_done[p]) cudaEventDestroy(step_done[p]);
+        if (stream[p]) cudaStreamDestroy(stream[p]);
+        step_done[p] = nullptr;
+        stream[p] = nullptr;
+    }
 }
 
 int Server::start(int dev, size_t budget_bytes, int max_act, uint64_t step_target) {
@@ -343,7 +355,12 @@ int Server::start(int dev, size_t budget_bytes, int max_act, uint64_t step_targe
     int rc = cuda_status(cudaSetDevice(device), "cudaSetDevice");
     if (rc) return rc;
     h3t12 = halton3_table();
-    if ((rc = cuda_status(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate"))) return rc;
+    for (int p = 0; p < 2; ++p) {
+        if ((rc = cuda_status(cudaStreamCreateWithFlags(&stream[p], cudaStreamNonBlocking), "cudaStreamCreate")))
+            return rc;
+        if ((rc = cuda_status(cudaEventCreateWithFlags(&step_done[p], cudaEventDisableTiming), "cudaEventCreate")))
+            return rc;
+    }
     if ((rc = cuda_status(cudaStreamCreateWithFlags(&adm_stream, cudaStreamNonBlocking), "cudaStreamCreate"))) return rc;
     if ((rc = cuda_status(cudaEventCreateWithFlags(&adm_done, cudaEventDisableTiming), "cudaEventCreate"))) return rc;
     pool.start(std::min(7u, std::thread::hardware_concurrency() / 2));
@@ -355,10 +372,13 @@ int Server::start(int dev, size_t budget_bytes, int max_act, uint64_t step_targe
     arena.reset(budget);
     step_bytes = align256((size_t)max_active * sizeof(InstanceDesc)) * kBatchGroups +
                  align256((size_t)(max_active + 1) * sizeof(uint64_t)) * kBatchGroups;
-    if ((rc = cuda_status(dev_alloc((void**)&d_step, step_bytes), "cudaMalloc step tables"))) return rc;
-    if ((rc = cuda_status(host_alloc((void**)&h_step, step_bytes), "cudaHostAlloc"))) return rc;
-    if ((rc = cuda_status(dev_alloc((void**)&d_counter, kBatchGroups * sizeof(unsigned long long)), "cudaMalloc")))
-        return rc;
+    for (int p = 0; p < 2; ++p) {
+        if ((rc = cuda_status(dev_alloc((void**)&d_step[p], step_bytes), "cudaMalloc step tables"))) return rc;
+        if ((rc = cuda_status(host_alloc((void**)&h_step[p], step_bytes), "cudaHostAlloc"))) return rc;
+        if ((rc = cuda_status(dev_alloc((void**)&d_counter[p], kBatchGroups * sizeof(unsigned long long)),
+                              "cudaMalloc")))
+            return rc;
+    }
     jobs_cap = align256((size_t)max_active * sizeof(RefitJob)) + align256((size_t)max_active * sizeof(SunJob)) +
                align256((size_t)max_active * sizeof(SunGridJob));
     if ((rc = cuda_status(dev_alloc((void**)&d_jobs, jobs_cap), "cudaMalloc job tables"))) return rc;
@@ -658,8 +678,10 @@ int Server::admit(std::vector<SRequest*>& admitted, std::string& err) {
     return rc;
 }
 
-// Queue one step over the active requests; `finishing` receives the requests whose last rays are in
-// it (their results are copied behind the launch).
+// Queue one step over the active requests that have rays left, on stream[par] with the tables of
+// parity par; `finishing` receives the requests whose last rays are in it (their results are
+// copied behind the launch, and behind the other stream's step when after_other is set: a request
+// may have a slice in both).
 // Launch parameters of the server's steps per kernel group (element list, BVH, grid): tile/CTA
 // size, resident CTAs per SM (0 = occupancy limit), tiles per work grab.  256-ray tiles and 16-tile
 // grabs for the element-list and grid groups measured 16 % more served rays/s than 128 / 4 on the
@@ -676,12 +698,14 @@ constexpr BatchTuning kServeTuning[kBatchGroups] = {{256, 0, 16}, {128, 0, 4}, {
 // are active and step_rays / active exceeds it anyway.
 constexpr uint64_t kMinSlice = 1ull << 24;
 
-int Server::step_launch(std::vector<SRequest*>& finishing, uint64_t& rays) {
+int Server::step_launch(int par, bool after_other, std::vector<SRequest*>& finishing, uint64_t& rays) {
     NvtxRange nvtx("csp server step launch");
     rays = 0;
     finishing.clear();
-    if (active.empty()) return CSP_OK;
-    const uint64_t quantum = std::max<uint64_t>(kMinSlice, step_rays / active.size());
+    size_t n_left = 0;
+    for (const SRequest* r : active) n_left += r->next_ray < r->rays ? 1 : 0;
+    if (n_left == 0) return CSP_OK;
+    const uint64_t quantum = std::max<uint64_t>(kMinSlice, step_rays / n_left);
     std::vector<InstanceDesc> desc[kBatchGroups];
     std::vector<uint64_t> tb[kBatchGroups];
     uint64_t tiles[kBatchGroups] = {};
@@ -689,6 +713,7 @@ int Server::step_launch(std::vector<SRequest*>& finishing, uint64_t& rays) {
     const size_t tb_base = desc_stride * kBatchGroups;
     const size_t tb_stride = align256((size_t)(max_active + 1) * sizeof(uint64_t));
     for (SRequest* r : active) {
+        if (r->next_ray >= r->rays) continue;  // finished in the step still in flight
         const SScene& s = *r->sc;
         const int g = r->group;
         const uint64_t slice = std::min<uint64_t>(quantum, r->rays - r->next_ray);
@@ -736,35 +761,40 @@ int Server::step_launch(std::vector<SRequest*>& finishing, uint64_t& rays) {
     for (int g = 0; g < kBatchGroups; ++g) {
         tb[g].push_back(tiles[g]);
         if (!desc[g].empty())
-            std::memcpy(h_step + desc_stride * g, desc[g].data(), desc[g].size() * sizeof(InstanceDesc));
-        std::memcpy(h_step + tb_base + tb_stride * g, tb[g].data(), tb[g].size() * sizeof(uint64_t));
+            std::memcpy(h_step[par] + desc_stride * g, desc[g].data(), desc[g].size() * sizeof(InstanceDesc));
+        std::memcpy(h_step[par] + tb_base + tb_stride * g, tb[g].data(), tb[g].size() * sizeof(uint64_t));
     }
-    int rc = cuda_status(cudaMemcpyAsync(d_step, h_step, step_bytes, cudaMemcpyHostToDevice, stream), "upload step");
-    if (!rc) rc = cuda_status(cudaMemsetAsync(d_counter, 0, kBatchGroups * sizeof(unsigned long long), stream), "memset");
+    cudaStream_t st = stream[par];
+    int rc = cuda_status(cudaMemcpyAsync(d_step[par], h_step[par], step_bytes, cudaMemcpyHostToDevice, st),
+                         "upload step");
+    if (!rc)
+        rc = cuda_status(cudaMemsetAsync(d_counter[par], 0, kBatchGroups * sizeof(unsigned long long), st), "memset");
     for (int g = 0; g < kBatchGroups && !rc; ++g) {
         if (desc[g].empty()) continue;
         BatchLaunch L;
-        L.inst = reinterpret_cast<const InstanceDesc*>(d_step + desc_stride * g);
-        L.tile_begin = reinterpret_cast<const uint64_t*>(d_step + tb_base + tb_stride * g);
+        L.inst = reinterpret_cast<const InstanceDesc*>(d_step[par] + desc_stride * g);
+        L.tile_begin = reinterpret_cast<const uint64_t*>(d_step[par] + tb_base + tb_stride * g);
         L.n_inst = (int)desc[g].size();
         L.chunk = kServeTuning[g].chunk;
         L.total_tiles = tiles[g];
-        L.next_tile = d_counter + g;
-        rc = cuda_status(launch_trace_batch(L, g, kServeTuning[g], stream), "batch_kernel");
+        L.next_tile = d_counter[par] + g;
+        rc = cuda_status(launch_trace_batch(L, g, kServeTuning[g], st), "batch_kernel");
     }
+    if (!rc && after_other && !finishing.empty())
+        rc = cuda_status(cudaStreamWaitEvent(st, step_done[1 - par], 0), "cudaStreamWaitEvent");
     for (SRequest* r : finishing) {
         if (rc) break;
         unsigned char* slot = h_res + res_slot_bytes * r->result_slot;
         rc = cuda_status(cudaMemcpyAsync(slot, d_arena + r->o_counts, (size_t)nx * ny * sizeof(uint32_t),
-                                         cudaMemcpyDeviceToHost, stream),
+                                         cudaMemcpyDeviceToHost, st),
                          "D2H flux map");
         if (!rc)
             rc = cuda_status(cudaMemcpyAsync(slot + (size_t)nx * ny * sizeof(uint32_t), d_arena + r->o_stats,
-                                             4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream),
+                                             4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st),
                              "D2H stats");
         if (!rc)
             rc = cuda_status(cudaMemcpyAsync(slot + (size_t)nx * ny * sizeof(uint32_t) + 4 * sizeof(unsigned long long),
-                                             d_arena + r->o_sun, sizeof(SunFrame), cudaMemcpyDeviceToHost, stream),
+                                             d_arena + r->o_sun, sizeof(SunFrame), cudaMemcpyDeviceToHost, st),
                              "D2H sun frame");
     }
     return rc;
@@ -772,35 +802,54 @@ int Server::step_launch(std::vector<SRequest*>& finishing, uint64_t& rays) {
 
 void Server::run_worker() {
     cudaSetDevice(device);
-    std::vector<SRequest*> finishing, admitted;
+    // the step in flight on the other stream: its finished requests are completed once it ends
+    struct InFlight {
+        bool valid = false;
+        std::vector<SRequest*> finishing;
+        uint64_t rays = 0;
+    } prev, cur;
+    std::vector<SRequest*> admitted;
+    bool adm_pending = false;  // an admission pass whose uploads may still be in flight
+    int par = 0;
     for (;;) {
         {
             std::unique_lock<std::mutex> lk(mu);
-            cv_work.wait(lk, [&] { return stopping || (!pending.empty() && !hold) || !active.empty(); });
-            if (stopping && active.empty() && (pending.empty() || hold)) break;
+            cv_work.wait(lk, [&] { return stopping || (!pending.empty() && !hold) || !active.empty() || prev.valid; });
+            if (stopping && active.empty() && (pending.empty() || hold) && !prev.valid) break;
         }
-        uint64_t rays = 0;
         std::string err;
-        // 1. launch the step over the requests already active
-        int rc = step_launch(finishing, rays);
-        // 2. admit while it runs (admission stream); the step stream waits for it, so the
-        //    synchronisation below covers both and the next step sees the admitted requests set up
+        // 1. launch step k on stream[par] over the active requests with rays left; it runs while
+        //    step k - 1 (the other stream) finishes
+        int rc = step_launch(par, prev.valid, cur.finishing, cur.rays);
+        cur.valid = !rc && (cur.rays > 0 || !cur.finishing.empty());
+        if (!rc && cur.valid) rc = cuda_status(cudaEventRecord(step_done[par], stream[par]), "cudaEventRecord");
+        // 2. admit while it runs (admission stream; its pinned staging is reused only after the last
+        //    pass's uploads are done); step k + 1 waits for the admission, so the admitted requests
+        //    join it set up
         admitted.clear();
+        if (!rc && adm_pending) rc = cuda_status(cudaEventSynchronize(adm_done), "admission");
+        adm_pending = false;
         if (!rc) rc = admit(admitted, err);
         if (!rc && !admitted.empty()) {
             rc = cuda_status(cudaEventRecord(adm_done, adm_stream), "cudaEventRecord");
-            if (!rc) rc = cuda_status(cudaStreamWaitEvent(stream, adm_done, 0), "cudaStreamWaitEvent");
+            if (!rc) rc = cuda_status(cudaStreamWaitEvent(stream[1 - par], adm_done, 0), "cudaStreamWaitEvent");
+            adm_pending = true;
         }
-        if (!rc && finishing.empty() && active.empty() && admitted.empty()) {
+        if (!rc && !cur.valid && !prev.valid && admitted.empty()) {
             // nothing fits yet (memory) and nothing runs: cannot happen, a request never exceeds
             // the budget; guard against a spin anyway
             std::unique_lock<std::mutex> lk(mu);
             cv_work.wait_for(lk, std::chrono::milliseconds(1));
         }
-        // 3. wait for the step (and the admissions' setup queued behind it)
-        if (!rc) {
+        // 3. wait for step k - 1 and complete its finished requests
+        if (!rc && prev.valid) {
             NvtxRange nvtx("csp server step wait");
-            rc = cuda_status(cudaStreamSynchronize(stream), "server step");
+            rc = cuda_status(cudaEventSynchronize(step_done[1 - par]), "server step");
+        }
+        if (!rc && !cur.valid && adm_pending) {
+            // nothing launched: let the admission finish before the loop waits for work
+            rc = cuda_status(cudaEventSynchronize(adm_done), "admission");
+            adm_pending = false;
         }
         const Clock::time_point now = Clock::now();
         std::lock_guard<std::mutex> lk(mu);
@@ -823,37 +872,48 @@ void Server::run_worker() {
             cv_done.notify_all();
             break;
         }
-        if (rays) ++steps;
-        rays_done += rays;
-        for (SRequest* r : finishing) {
-            const unsigned char* slot = h_res + res_slot_bytes * r->result_slot;
-            r->counts.assign(reinterpret_cast<const uint32_t*>(slot),
-                             reinterpret_cast<const uint32_t*>(slot) + (size_t)nx * ny);
-            std::memcpy(r->stats, slot + (size_t)nx * ny * sizeof(uint32_t), 4 * sizeof(uint64_t));
-            r->stats[0] = r->rays;
-            std::memcpy(&r->sunf, slot + (size_t)nx * ny * sizeof(uint32_t) + 4 * sizeof(unsigned long long),
-                        sizeof(SunFrame));
-            r->state = kDone;
-            r->t_done = now;
-            t_last_done = now;
-            latencies.push_back(std::chrono::duration<double>(r->t_done - r->t_submit).count());
-            ++completed;
-            arena.release(r->off, r->bytes);
-            free_res_slots.push_back(r->result_slot);
-            r->result_slot = -1;
-            active.erase(std::find(active.begin(), active.end(), r));
+        bool notify = false;
+        if (prev.valid) {
+            if (prev.rays) ++steps;
+            rays_done += prev.rays;
+            for (SRequest* r : prev.finishing) {
+                const unsigned char* slot = h_res + res_slot_bytes * r->result_slot;
+                r->counts.assign(reinterpret_cast<const uint32_t*>(slot),
+                                 reinterpret_cast<const uint32_t*>(slot) + (size_t)nx * ny);
+                std::memcpy(r->stats, slot + (size_t)nx * ny * sizeof(uint32_t), 4 * sizeof(uint64_t));
+                r->stats[0] = r->rays;
+                std::memcpy(&r->sunf, slot + (size_t)nx * ny * sizeof(uint32_t) + 4 * sizeof(unsigned long long),
+                            sizeof(SunFrame));
+                r->state = kDone;
+                r->t_done = now;
+                t_last_done = now;
+                latencies.push_back(std::chrono::duration<double>(r->t_done - r->t_submit).count());
+                ++completed;
+                arena.release(r->off, r->bytes);
+                free_res_slots.push_back(r->result_slot);
+                r->result_slot = -1;
+                active.erase(std::find(active.begin(), active.end(), r));
+                notify = true;
+            }
         }
         for (SRequest* r : admitted) {
             if (r->state == kFailed) {
                 arena.release(r->off, r->bytes);
                 free_res_slots.push_back(r->result_slot);
+                notify = true;
                 continue;
             }
             r->state = kActive;
             active.push_back(r);
+            notify = true;
         }
         peak_active = std::max(peak_active, (int)active.size());
-        if (!finishing.empty() || !admitted.empty()) cv_done.notify_all();
+        if (notify) cv_done.notify_all();
+        std::swap(prev, cur);
+        cur.valid = false;
+        cur.finishing.clear();
+        cur.rays = 0;
+        if (prev.valid) par = 1 - par;
     }
 }
 
