@@ -60,7 +60,8 @@ def _submit(srv, req):
 def test_server_results_same_alone_and_in_mix(gpu):
     from optixsoltracedemos_gb300 import native
     scene_list, reqs = _workload()
-    # step_rays small: requests above 1M rays are traced in several slices
+    # step_rays small: each request (at most 3.5M rays, below the 2^24-ray minimum slice) is traced
+    # in one slice, several requests per step
     srv = native.Server(0, memory_budget=256 << 20, max_active=8, step_rays=4 << 20)
     try:
         sids = [srv.add_scene(e) for e in scene_list]
@@ -158,6 +159,40 @@ def test_server_rejects_bad_requests(gpu):
             srv.submit(sid2, th.sun_dir, 0, 4.65e-3, 1000, poses=big)
     finally:
         srv.close()
+
+
+def test_server_sliced_requests_equal_batch(gpu):
+    """Requests of 17M to 40M rays, traced in slices of 2^24 rays over several steps that overlap on
+    the server's two step streams (one request's slices in consecutive steps, requests finishing in
+    different steps), give the flux maps and counters of one batch run of the same instances."""
+    from optixsoltracedemos_gb300 import native
+    field = scenes.large_field(n_heliostats=600, num_rays=1).elements
+    th = scenes.three_heliostats()
+    jobs = []
+    for k, (rays, el) in enumerate([(40_000_000, 60.0), (17_000_000, 30.0), (25_000_000, 45.0)]):
+        sun = scenes.sun_vector(el, -30.0 + 25.0 * k)
+        jobs.append((1, scenes.reaim(field, sun), sun, rays, 7 + k, k))
+    jobs.append((0, None, th.sun_dir, 33_000_000, 11, 3))
+    srv = native.Server(0, memory_budget=512 << 20, max_active=8)
+    try:
+        sids = [srv.add_scene(th.elements), srv.add_scene(field)]
+        ids = [srv.submit(sids[s], sun, scenes.SUN_PILLBOX, 4.65e-3, rays, seed=seed, instance=inst, poses=poses)
+               for s, poses, sun, rays, seed, inst in jobs]
+        served = [srv.wait(rid, timeout=300)[:2] for rid in ids]
+        assert srv.stats()["steps"] >= 3
+    finally:
+        srv.close()
+    b = native.Batch(0)
+    try:
+        bs = [b.add_scene(th.elements), b.add_scene(field)]
+        for s, poses, sun, rays, seed, inst in jobs:
+            b.add_instance(bs[s], sun, scenes.SUN_PILLBOX, 4.65e-3, rays, seed=seed, instance=inst, poses=poses)
+        b.run()
+        for i, (c, st) in enumerate(served):
+            np.testing.assert_array_equal(c, b.counts(i), err_msg=f"request {i}")
+            np.testing.assert_array_equal(st, b.stats(i))
+    finally:
+        b.close()
 
 
 def test_server_ray_indices_beyond_32_bits(gpu):
