@@ -82,7 +82,6 @@ struct FlatStageSmem;
 template <int kB_, int kAccel_, bool kDense_, bool kFlux_>
 struct Cfg {
     static constexpr int kB = kB_;        // CTA size = tile size (rays)
-    static constexpr int kQ = 2 * kB_;    // queue capacity: < kB left after a drain + kB pushes
     static constexpr int kAccel = kAccel_;
     static constexpr bool kFlat = kAccel_ == kAccelFlat;
     static constexpr bool kDense = kDense_;
