@@ -259,7 +259,7 @@ def batched_config(n_inst, n_heliostats, counts, extra=None):
            "instances": n_inst, "rays_total": int(counts.sum()), "rays_min": int(counts.min()),
            "rays_max": int(counts.max()), "flux_grid": [100, 100], "sun": "pillbox 4.65 mrad, elevation U(10,80) "
            "azimuth U(-120,120), heliostats re-aimed per instance", "slope_error_rad": 1.5e-3,
-           "l2_policy": "per-instance scene data (element records, field grids, sun-ray grids: ~2.3 GB for "
+           "l2_policy": "per-instance scene data (element records, field grids, sun-ray grids: ~2.5 GB for "
                         "256 instances) exceed L2; no per-ray buffers",
            "parallelism": "replicas"}
     cfg.update(extra or {})
