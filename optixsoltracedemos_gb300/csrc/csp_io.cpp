@@ -16,8 +16,10 @@
 // Writer: SolTraceSystem::write_output (lib/soltrace_system.cpp:208-264): header
 //   "number,stage,loc_x,loc_y,loc_z", one row per record, a record whose x, y, z are all zero is
 //   a marker that ends the current ray, rays are numbered from 1 in order, values printed as the
-//   C++ stream prints floats (6 significant digits, %g style).  Blocks of rays are formatted in
-//   parallel threads starting from the writer state of their first ray, then written in order.
+//   C++ stream prints floats (6 significant digits, %g style; format_g6, csp_format.h).  Blocks of
+//   rays are formatted in parallel threads starting from the writer state of their first ray, then
+//   written in order; the start states of the next batch of blocks and the writing of the last one
+//   overlap the formatting of the current one.
 //   CSP_OUT_STAGED leaves out the rows of rays that reach the receiver straight from the sun, as
 //   scripts/post_processing/clean_direct_sun.py does to the written file.
 #include <algorithm>
@@ -32,6 +34,7 @@
 #include <vector>
 
 #include "csp_c_api.h"
+#include "csp_format.h"
 #include "csp_system.h"
 
 namespace csp {
@@ -256,18 +259,6 @@ void advance(const float* hits, uint64_t b, uint64_t e, WriterState& st) {
     }
 }
 
-inline void put_float(std::string& out, float v) {
-    char buf[48];
-    auto res = std::to_chars(buf, buf + sizeof buf, v, std::chars_format::general, 6);
-    out.append(buf, res.ptr);
-}
-
-inline void put_u64(std::string& out, uint64_t v) {
-    char buf[24];
-    auto res = std::to_chars(buf, buf + sizeof buf, v);
-    out.append(buf, res.ptr);
-}
-
 // A ray whose first interaction is the receiver (a stage-2 record in slot 1): light straight from
 // the sun, which a staged SolTrace run never records (scripts/post_processing/clean_direct_sun.py:
 // 6-18 drops the rows of every ray number with a stage-2 row and no stage-1 row; a ray's rows are
@@ -275,10 +266,20 @@ inline void put_u64(std::string& out, uint64_t v) {
 // stage-2 record in slot 1).
 inline bool direct_sun(const float* hits, uint64_t ray) { return hits[4 * (ray * kMaxDepth + 1)] == 2.0f; }
 
+// longest row: a 20-digit ray number, four values of at most 16 characters, separators
+constexpr size_t kMaxRowBytes = 20 + 4 * (1 + 16) + 1;
+
 void format(const float* hits, uint64_t b, uint64_t e, WriterState st, bool staged, std::string& out) {
-    out.clear();
-    out.reserve((e - b) * 64);
+    out.resize((e - b) * 48 + 64 * kMaxRowBytes);  // about one row per ray; grown when short
+    char* p = &out[0];
+    char* end = p + out.size();
     for (uint64_t k = b * kMaxDepth; k < e * kMaxDepth; ++k) {
+        if ((size_t)(end - p) < kMaxRowBytes) {
+            const size_t used = (size_t)(p - out.data());
+            out.resize(out.size() * 2);
+            p = &out[0] + used;
+            end = &out[0] + out.size();
+        }
         const float* r = hits + 4 * k;
         if (is_marker(r)) {
             if (st.stage > 0) {
@@ -296,14 +297,15 @@ void format(const float* hits, uint64_t b, uint64_t e, WriterState st, bool stag
             st.stage++;
             continue;
         }
-        put_u64(out, st.current);
+        p = std::to_chars(p, end, st.current).ptr;
         for (int c = 0; c < 4; ++c) {
-            out.push_back(',');
-            put_float(out, r[c]);
+            *p++ = ',';
+            p = format_g6(r[c], p, end);
         }
-        out.push_back('\n');
+        *p++ = '\n';
         st.stage++;
     }
+    out.resize((size_t)(p - out.data()));
 }
 
 }  // namespace
@@ -316,29 +318,67 @@ int write_hits_csv(const float* hits, uint64_t n, const char* path, bool staged,
     }
     const char* header = "number,stage,loc_x,loc_y,loc_z\n";
     std::fwrite(header, 1, std::strlen(header), fp);
+    // batches of nt blocks: while the threads format batch i, this thread computes the start states
+    // of batch i + 1 and writes batch i - 1
     const unsigned nt = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
     const uint64_t block = 1u << 18;
-    WriterState st;
-    std::vector<std::string> bufs(nt);
-    for (uint64_t base = 0; base < n; base += block * nt) {
-        std::vector<WriterState> starts(nt);
-        std::vector<uint64_t> bb(nt), ee(nt);
-        for (unsigned t = 0; t < nt; ++t) {
-            bb[t] = std::min(n, base + t * block);
-            ee[t] = std::min(n, bb[t] + block);
-            starts[t] = st;
-            advance(hits, bb[t], ee[t], st);
-        }
+    struct Batch {
+        std::vector<WriterState> starts;
+        std::vector<uint64_t> bb, ee;
+        std::vector<std::string> bufs;
         std::vector<std::thread> th;
+    } batch[2];
+    WriterState st;
+    auto plan = [&](Batch& B, uint64_t base) {
+        B.starts.assign(nt, WriterState{});
+        B.bb.assign(nt, 0);
+        B.ee.assign(nt, 0);
+        B.bufs.resize(nt);
+        for (unsigned t = 0; t < nt; ++t) {
+            B.bb[t] = std::min(n, base + t * block);
+            B.ee[t] = std::min(n, B.bb[t] + block);
+            B.starts[t] = st;
+            advance(hits, B.bb[t], B.ee[t], st);
+        }
+    };
+    auto launch = [&](Batch& B) {
         for (unsigned t = 0; t < nt; ++t)
-            if (bb[t] < ee[t]) th.emplace_back(format, hits, bb[t], ee[t], starts[t], staged, std::ref(bufs[t]));
-        for (auto& x : th) x.join();
-        for (unsigned t = 0; t < nt; ++t)
-            if (bb[t] < ee[t] && std::fwrite(bufs[t].data(), 1, bufs[t].size(), fp) != bufs[t].size()) {
-                std::fclose(fp);
-                err = std::string("short write to ") + path;
-                return CSP_ERR_IO;
+            if (B.bb[t] < B.ee[t])
+                B.th.emplace_back(format, hits, B.bb[t], B.ee[t], B.starts[t], staged, std::ref(B.bufs[t]));
+    };
+    auto join = [&](Batch& B) {
+        for (auto& x : B.th) x.join();
+        B.th.clear();
+    };
+    bool ok = true;
+    auto write = [&](Batch& B) {
+        for (unsigned t = 0; t < nt && ok; ++t)
+            if (B.bb[t] < B.ee[t] && std::fwrite(B.bufs[t].data(), 1, B.bufs[t].size(), fp) != B.bufs[t].size())
+                ok = false;
+    };
+    const uint64_t step = block * nt;
+    if (n > 0) {
+        plan(batch[0], 0);
+        launch(batch[0]);
+        for (uint64_t base = 0, i = 0;; base += step, ++i) {
+            Batch& cur = batch[i & 1];
+            Batch& nxt = batch[(i + 1) & 1];
+            const bool more = base + step < n;
+            if (more) plan(nxt, base + step);
+            join(cur);
+            if (more) launch(nxt);
+            write(cur);
+            if (!more) break;
+            if (!ok) {
+                join(nxt);
+                break;
             }
+        }
+    }
+    if (!ok) {
+        std::fclose(fp);
+        err = std::string("short write to ") + path;
+        return CSP_ERR_IO;
     }
     if (std::fclose(fp) != 0) {
         err = std::string("could not close ") + path;

@@ -146,3 +146,20 @@ def test_csv_writer_matches_reference_format(native_lib, tmp_path, oracle32):
     big = np.tile(hits, (300, 1, 1))
     native.write_hits_csv(big, p)
     assert open(p).read().splitlines()[1:] == reference_csv_rows(big)
+
+
+def test_csv_float_text_equals_stream_format(tmp_path):
+    """The CSV writer's float formatter (csp_format.h) gives the text of std::to_chars with six
+    significant digits in general format (the C++ stream default the reference's writer uses) on
+    every 97th float bit pattern and next to every power of ten (a host program compiled from the
+    formatter's header; the whole 2^32 range passes with stride 1)."""
+    import shutil
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = str(tmp_path / "format_g6_check")
+    subprocess.run([shutil.which("g++") or "g++", "-std=c++17", "-O2", "-pthread", "-I",
+                    os.path.join(root, "optixsoltracedemos_gb300", "csrc"),
+                    os.path.join(root, "tests", "cpp", "format_g6_check.cpp"), "-o", exe], check=True)
+    r = subprocess.run([exe, "97"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout[-2000:]
+    assert r.stdout.strip().endswith("0 mismatches"), r.stdout[-500:]
