@@ -408,9 +408,16 @@ int write_compact_csv(const float* points, const uint8_t* counts, const float* r
     const uint64_t block = 1u << 16;
     WriterState st;
     uint64_t rec = 0;  // first record of the next block
-    std::vector<std::string> bufs(nt);
+    // formatted blocks double-buffered: batch i is written by `writer` while batch i + 1 is built
+    std::vector<std::string> bufs2[2] = {std::vector<std::string>(nt), std::vector<std::string>(nt)};
+    std::vector<uint64_t> written_bb[2] = {std::vector<uint64_t>(nt), std::vector<uint64_t>(nt)};
+    std::vector<uint64_t> written_ee[2] = {std::vector<uint64_t>(nt), std::vector<uint64_t>(nt)};
+    std::thread writer;
+    bool ok = true;
     std::vector<std::vector<float>> dense(nt);
-    for (uint64_t base = 0; base < n; base += block * nt) {
+    uint64_t batch_no = 0;
+    for (uint64_t base = 0; base < n; base += block * nt, ++batch_no) {
+        std::vector<std::string>& bufs = bufs2[batch_no & 1];
         std::vector<uint64_t> bb(nt), ee(nt), r0(nt);
         for (unsigned t = 0; t < nt; ++t) {
             bb[t] = std::min(n, base + t * block);
@@ -444,12 +451,22 @@ int write_compact_csv(const float* points, const uint8_t* counts, const float* r
             if (bb[t] < ee[t])
                 th.emplace_back(format, dense[t].data(), 0, ee[t] - bb[t], starts[t], staged, std::ref(bufs[t]));
         for (auto& x : th) x.join();
-        for (unsigned t = 0; t < nt; ++t)
-            if (bb[t] < ee[t] && std::fwrite(bufs[t].data(), 1, bufs[t].size(), fp) != bufs[t].size()) {
-                std::fclose(fp);
-                err = std::string("short write to ") + path;
-                return CSP_ERR_IO;
-            }
+        if (writer.joinable()) writer.join();  // the batch before is on disk
+        if (!ok) break;
+        written_bb[batch_no & 1] = bb;
+        written_ee[batch_no & 1] = ee;
+        writer = std::thread([&, slot = batch_no & 1] {
+            for (unsigned t = 0; t < nt && ok; ++t)
+                if (written_bb[slot][t] < written_ee[slot][t] &&
+                    std::fwrite(bufs2[slot][t].data(), 1, bufs2[slot][t].size(), fp) != bufs2[slot][t].size())
+                    ok = false;
+        });
+    }
+    if (writer.joinable()) writer.join();
+    if (!ok) {
+        std::fclose(fp);
+        err = std::string("short write to ") + path;
+        return CSP_ERR_IO;
     }
     if (std::fclose(fp) != 0) {
         err = std::string("could not close ") + path;
