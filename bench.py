@@ -607,7 +607,8 @@ def measure_batched(args, local, world, pg=None):
         "e2e": {"value": world * total * steps / piped_s, "unit": "rays/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
                 "path": "csp_batch_run_async / csp_batch_wait from host pose arrays to host flux maps, pipelined"},
-        "gpu_launches": 3 * steps,
+        # per run: refit, sun planes, the sun-ray grids' size / count / scan / fill, the batch kernel
+        "gpu_launches": 7 * steps,
         "clocks": clocks,
         "batched_wall_rays_per_s": world * total / max_over_ranks(statistics.median(wall), pg, f"cuda:{local}"),
         "pipelined_flux_counts_mismatching": piped_mismatch,
