@@ -24,7 +24,7 @@
 namespace csp {
 namespace {
 
-constexpr int kTraceBlock = 128;
+constexpr int kTraceBlock = 256;
 constexpr int kPrepBlock = 512;
 constexpr int kFluxBlock = 256;
 
@@ -44,12 +44,14 @@ struct TraceSmem {
     typename PlainCfg<kAccel>::Core core;
 };
 
-// Resident 128-thread CTAs per SM the register budget is cut for: eight (64 registers), which
-// measured faster than six or seven for every kernel -- more warps to cover the record stream of the
-// element-list kernel and the dependent loads of the candidate and cell lists of the others.
+// Resident 256-thread CTAs per SM the register budget is cut for: four (64 registers, 1,024
+// threads) -- more warps to cover the record stream of the element-list kernel and the dependent
+// loads of the candidate and cell lists of the others (64 registers measured faster than 72 or 77
+// for every kernel); 256-thread CTAs instead of eight of 128: the 10,000-heliostat field 32.05 ->
+// 30.23 ms per 268M rays, the single parabolic heliostat 0.3305 -> 0.3283 ms per 16M.
 template <int kAccel>
 constexpr int trace_min_blocks() {
-    return 8;
+    return 4;
 }
 
 // Persistent kernel over the tiles of one launch (static round robin); dense records out.
