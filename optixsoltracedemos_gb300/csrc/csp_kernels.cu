@@ -48,7 +48,8 @@ struct TraceSmem {
 // threads) -- more warps to cover the record stream of the element-list kernel and the dependent
 // loads of the candidate and cell lists of the others (64 registers measured faster than 72 or 77
 // for every kernel); 256-thread CTAs instead of eight of 128: the 10,000-heliostat field 32.05 ->
-// 30.23 ms per 268M rays, the single parabolic heliostat 0.3305 -> 0.3283 ms per 16M.
+// 30.23 ms per 268M rays, the single parabolic heliostat 0.3305 -> 0.3283 ms per 16M (two of 512:
+// 30.4 and 0.347 ms).
 template <int kAccel>
 constexpr int trace_min_blocks() {
     return 4;
