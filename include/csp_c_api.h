@@ -143,7 +143,9 @@ CSP_API int csp_get_accel(csp_handle h, int* mode);
 CSP_API int csp_initialize(csp_handle h);
 /* Trace num_rays rays and wait for them (run()).  Fully rewrites the num_rays x 5 hit buffer. */
 CSP_API int csp_run(csp_handle h);
-/* Enqueue the trace on `stream` (a cudaStream_t, NULL = the handle's own stream); no host sync. */
+/* Enqueue the trace on `stream` (a cudaStream_t, NULL = the handle's own stream); no host sync.
+ * It writes the handle's hit buffer, so it must not overlap another run or trace of the handle on
+ * the GPU (it also shares the handle's work counter with them). */
 CSP_API int csp_trace_async(csp_handle h, void* stream);
 /* Re-read the element poses given since initialize (same count), refit the acceleration structure
  * in place and recompute the sun plane (update()). */
@@ -159,7 +161,9 @@ CSP_API int csp_run_to_host(csp_handle h, float* dst, uint32_t* ids);
 /* Enqueue the trace of rays [first_ray, first_ray + count) on `stream` (NULL = the handle's own)
  * into caller-provided buffers of count * 5 records: device memory, or page-locked host memory
  * the device can address (the kernel then stores the records across the host link directly).
- * ids may be NULL.  No host synchronisation; the handle's own hit buffer is not touched. */
+ * ids may be NULL.  No host synchronisation; the handle's own hit buffer is not touched, so windows
+ * may be traced on several streams at once (off the handle's own stream the CTAs take tiles in a
+ * fixed order instead of from the handle's work counter). */
 CSP_API int csp_trace_into(csp_handle h, void* hits, void* ids, uint64_t first_ray, uint64_t count, void* stream);
 /* Trace all rays, then move the records in compact form for consumers of the reference's
  * write_output (lib/soltrace_system.cpp:208-264), which need every record but not the empty slots:

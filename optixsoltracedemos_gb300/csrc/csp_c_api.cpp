@@ -107,8 +107,10 @@ void System::release() {
     cap_cells = cap_items = cap_global = 0;
     cudaFree(d_sgrid);
     cudaFree(d_sgjob);
+    cudaFree(d_tile_counter);
     d_sgrid = nullptr;
     d_sgjob = nullptr;
+    d_tile_counter = nullptr;
     cap_sgrid = 0;
     cudaFree(d_cpoints);
     cudaFree(d_ccounts);
@@ -248,6 +250,9 @@ int System::initialize() {
     const auto t0 = std::chrono::steady_clock::now();
     int rc = ensure_streams();
     if (rc) return rc;
+    if (!d_tile_counter &&
+        (rc = cuda_status(dev_alloc((void**)&d_tile_counter, sizeof(unsigned long long)), "cudaMalloc tile counter")))
+        return rc;
     h3t12 = halton3_table();
     std::string err;
     if ((rc = build_elements(elements.data(), (uint32_t)elements.size(), scene, err))) return fail(rc, err);
@@ -305,6 +310,7 @@ TraceArgs System::args(uint64_t begin, uint64_t count) const {
     a.grid = grid.valid ? d_grid : nullptr;
     a.h3t12 = h3t12;
     a.sgrid = scene.prims.size() > kFlatListMax && d_sgrid ? sgjob_host.desc : nullptr;
+    a.tile_counter = d_tile_counter;
     return a;
 }
 
@@ -312,6 +318,8 @@ int System::trace_async(cudaStream_t st) {
     if (!initialized) return fail(CSP_ERR_STATE, "trace before initialize()");
     int rc = ensure_hit_buffers();
     if (rc) return rc;
+    // it writes the hit buffer: it never overlaps the handle's other launches, so the tile counter
+    // serves it on any stream
     return cuda_status(launch_trace(args(0, num_rays), (int)scene.prims.size(), st ? st : stream), "trace_kernel");
 }
 
@@ -681,6 +689,7 @@ int csp_trace_into(csp_handle h, void* hits, void* ids, uint64_t first, uint64_t
     a.ray_begin = first;
     a.count = count;
     cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : s->stream;
+    if (st != s->stream) a.tile_counter = nullptr;  // may overlap the launches on the handle's stream
     return csp::cuda_status(csp::launch_trace(a, (int)s->scene.prims.size(), st), "trace_kernel");
 }
 

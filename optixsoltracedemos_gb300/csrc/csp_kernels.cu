@@ -55,7 +55,14 @@ constexpr int trace_min_blocks() {
     return 4;
 }
 
-// Persistent kernel over the tiles of one launch (static round robin); dense records out.
+// Persistent kernel over the tiles of one launch; dense records out.  With a tile counter the CTAs
+// take guided grabs (a quarter of an even share of the tiles left, at most kTraceGrab, shrinking to
+// single tiles at the end), else static round robin.  The records do not depend on which CTA traces
+// a tile.  Guided grabs measured 27.5 ms per 268M rays of the 10,000-heliostat field against
+// 30.3 ms round robin (a CTA's tiles differ much in work, so round robin ends in a long tail), and
+// 0.325 against 0.328 ms per 16M rays of the single parabolic heliostat.
+constexpr unsigned long long kTraceGrab = 64;
+
 template <int kAccel>
 __global__ void __launch_bounds__(kTraceBlock, trace_min_blocks<kAccel>()) trace_kernel(
     const typename PlainCfg<kAccel>::Args A) {
@@ -74,8 +81,29 @@ __global__ void __launch_bounds__(kTraceBlock, trace_min_blocks<kAccel>()) trace
     const Sink none{nullptr, nullptr};
     const uint64_t tiles = (A.count + kTraceBlock - 1) / kTraceBlock;
     int qs = 0, gs = 0;
-    for (uint64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x)
-        trace_tile<C>(A, none, sm.core, &sm.stage, tile, qs, gs);
+    if (A.tile_counter) {
+        __shared__ unsigned long long s_grab, s_want;
+        unsigned long long seen = 0;  // end of this CTA's last grab (thread 0's estimate of the rest)
+        for (;;) {
+            if (threadIdx.x == 0) {
+                const unsigned long long left = tiles > seen ? tiles - seen : 0;
+                const unsigned long long want =
+                    max(1ull, min(kTraceGrab, left / ((unsigned long long)gridDim.x * 4)));
+                s_grab = atomicAdd(A.tile_counter, want);
+                s_want = want;
+            }
+            __syncthreads();
+            // every thread reads the grab before thread 0 can write the next one: trace_tile has
+            // CTA barriers, and a grab past the end ends the loop in every thread
+            const uint64_t g0 = s_grab, g1 = min((uint64_t)(g0 + s_want), tiles);
+            if (g0 >= tiles) break;
+            seen = g1;
+            for (uint64_t tile = g0; tile < g1; ++tile) trace_tile<C>(A, none, sm.core, &sm.stage, tile, qs, gs);
+        }
+    } else {
+        for (uint64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x)
+            trace_tile<C>(A, none, sm.core, &sm.stage, tile, qs, gs);
+    }
     drain<C>(A, none, sm.core, true, qs, gs);
 }
 
@@ -102,6 +130,10 @@ cudaError_t launch_trace_t(const TraceArgs& args, cudaStream_t stream) {
     typename PlainCfg<kAccel>::Args a;
     static_cast<TraceArgs&>(a) = args;
     if constexpr (PlainCfg<kAccel>::kSched) philox_keys(args.seed, a.keys);
+    if (args.tile_counter) {
+        e = cudaMemsetAsync(args.tile_counter, 0, sizeof(unsigned long long), stream);
+        if (e != cudaSuccess) return e;
+    }
     trace_kernel<kAccel><<<(unsigned)grid, kTraceBlock, sizeof(TraceSmem<kAccel>), stream>>>(a);
     return cudaGetLastError();
 }

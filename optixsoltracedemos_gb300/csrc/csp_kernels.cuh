@@ -43,6 +43,10 @@ struct TraceArgs {
     const GridDesc* grid;  // field grid of the scene, nullptr: BVH (or element list) traversal
     const float* h3t12;    // Halton base-3 partial sums after 12 digits (halton3_table), or nullptr
     const SunGrid* sgrid;  // candidate grid of the sun rays (scenes of more than 8 elements)
+    // single-scene launches: tiles handed out by this device counter (zeroed by launch_trace before
+    // the kernel) in guided grabs; nullptr: static round robin (launches that may overlap on the
+    // GPU with another of the same counter use that)
+    unsigned long long* tile_counter;
 };
 
 // Arguments of the single-scene element-list kernel: TraceArgs plus the Philox key schedule of

@@ -140,6 +140,7 @@ extern "C" int csp_trace_noalloc(int device, const csp_element* elements, uint32
                          "csp_trace_noalloc: prepare_sun_kernel");
         if (!rc && num_rays) {
             TraceArgs a;
+            a.tile_counter = nullptr;  // static round robin: nothing to allocate
             a.nodes = reinterpret_cast<const Node*>(scratch + kOffNodes);
             a.prims = reinterpret_cast<const Prim*>(scratch + kOffPrims);
             a.optics = reinterpret_cast<const Optics*>(scratch + kOffOptics);

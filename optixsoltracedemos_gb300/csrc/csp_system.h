@@ -75,6 +75,7 @@ struct System {
     unsigned char* d_sgrid = nullptr;
     size_t cap_sgrid = 0;
     SunGridJob* d_sgjob = nullptr;
+    unsigned long long* d_tile_counter = nullptr;  // guided tile grabs of the launches on `stream`
     SunGridJob sgjob_host{};
     // compact records (csp_run_to_host_compact): points, counts, block offsets, records
     float* d_cpoints = nullptr;
