@@ -63,10 +63,10 @@ BYTES_PER_RAY = 80  # 5 float4 hit records per ray, fully rewritten by every pla
 # kernel ends)
 NCU_TRAFFIC_PER_LAUNCH = 4 * (8776704 + 291551232)
 # The same for the field kernel (trace_kernel<grid>) of the 10,000-heliostat field per launch of
-# 268,435,456 rays: 64 x (9,310,208 + 297,519,360) bytes from `ncu --set full -k regex:^trace_kernel
+# 268,435,456 rays: 64 x (15,834,112 + 297,401,344) bytes from `ncu --set full -k regex:^trace_kernel
 # -s 2 -c 1` of `python bench.py --workload large_field --rays 4194304 --steps 2 --warmup 2
-# --no-cpu-baseline`, scaled by the rays
-NCU_TRAFFIC_PER_LAUNCH_FIELD = 64 * (9310208 + 297519360)
+# --no-cpu-baseline --no-accuracy --e2e-steps 0`, scaled by the rays
+NCU_TRAFFIC_PER_LAUNCH_FIELD = 64 * (15834112 + 297401344)
 # Batch kernel (field grid) on the batched workload: warp instructions and DRAM bytes per traced ray,
 # from `ncu --set full -k regex:^batch_kernel -s 2 -c 1` of `python bench.py --workload batched
 # --instances 8 --tuning 256,4,256 --steps 1 --warmup 3 --no-systems --no-cpu-baseline
